@@ -1,0 +1,420 @@
+"""ddp_gb300: GA* and dynamic A* on int32 CSR graphs for GB300 (sm_103a).
+
+Python host mirror of the C-ABI in include/ddp_gb300.h.  Every compute call
+goes to libddp_gb300.so; there is no CPU fallback — if the library or the
+GPU is missing the calls raise.
+
+Two layers:
+  * functional API: DeviceGraph, Heuristic, BatchEngine, DynamicSearch and
+    the generators / text I/O;
+  * LIB mirror: Graph, GPU_Graph, Dynamic_Graph, GPU_Dynamic_Graph, A_Star,
+    GPU_A_Star with the reference's names and return conventions
+    (lkoshale/DDP LIB/include/graph.h, dynamic_graph.h, a_star.h, a_star.cuh):
+    get_path() returns [-1] when no heuristic was set, [] when the target is
+    unreachable, else the node ids source..target.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from ._lib import DdpError, Opts, check, lib, ptr  # noqa: F401
+
+H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER = 0, 1, 2, 3
+INF = 2147483647
+
+__all__ = [
+    "CSR", "DeviceGraph", "Heuristic", "SolveResult", "BatchEngine", "DdpError", "INF",
+    "H_ZERO", "H_BFS_HOPS", "H_MANHATTAN", "H_USER", "gen_random_chain", "gen_maze",
+    "gen_updates", "gen_pairs", "read_graph_text", "write_graph_text", "read_ints_text",
+    "write_ints_text", "read_updates_text", "write_updates_text", "Graph", "GPU_Graph",
+    "Dynamic_Graph", "GPU_Dynamic_Graph", "A_Star", "GPU_A_Star",
+]
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+# ---------------------------------------------------------------------------
+# host CSR container
+@dataclass
+class CSR:
+    """Host CSR with n+1 offsets (off[n] = e).  col < 0 marks a dead arc."""
+    n: int
+    off: np.ndarray
+    col: np.ndarray
+    w: np.ndarray
+    xy: Optional[np.ndarray] = None      # (n, 2) int32 coordinates
+    perm: Optional[np.ndarray] = None    # Hamiltonian chain order (generators)
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def e(self) -> int:
+        return int(self.off[-1])
+
+    def row(self, u: int):
+        return self.col[self.off[u]:self.off[u + 1]], self.w[self.off[u]:self.off[u + 1]]
+
+    def reverse(self) -> "CSR":
+        """Reverse CSR (sources of arcs into v, increasing source order)."""
+        live = self.col >= 0
+        src = np.repeat(np.arange(self.n, dtype=np.int32), np.diff(self.off))[live]
+        dst = self.col[live]
+        ww = self.w[live]
+        order = np.lexsort((np.arange(len(dst)), dst))
+        roff = np.zeros(self.n + 1, dtype=np.int32)
+        np.add.at(roff, dst + 1, 1)
+        roff = np.cumsum(roff, dtype=np.int64).astype(np.int32)
+        return CSR(self.n, roff, _i32(src[order]), _u32(ww[order]))
+
+    def with_sentinel(self) -> "CSR":
+        """Appends an isolated node n (the reference CPU A* reads the last
+        row only up to e-1, GA_star/A_star_cpu.cpp:170; a sentinel last row
+        makes that harmless)."""
+        off = np.concatenate([self.off, [self.off[-1]]]).astype(np.int32)
+        return CSR(self.n + 1, off, self.col, self.w)
+
+    def protect_next(self) -> Optional[np.ndarray]:
+        """next[u] = chain successor of u (or -1), from the generator's perm."""
+        if self.perm is None:
+            return None
+        nxt = np.full(self.n, -1, dtype=np.int32)
+        nxt[self.perm[:-1]] = self.perm[1:]
+        return nxt
+
+
+# ---------------------------------------------------------------------------
+# generators (seeded; ddp_gen_* in csrc/gen.c)
+def gen_random_chain(n: int, avg_deg: int, wmin: int, wmax: int, seed: int) -> CSR:
+    """Directed graph: Hamiltonian chain over a seeded permutation, then
+    uniform extra arcs (no self-loops, no duplicates) up to n*avg_deg arcs,
+    weights uniform in [wmin, wmax]."""
+    e = int(n) * int(avg_deg)
+    off = np.empty(n + 1, np.int32)
+    col = np.empty(e, np.int32)
+    w = np.empty(e, np.uint32)
+    perm = np.empty(n, np.int32)
+    rc = lib().ddp_gen_random_chain(n, e, wmin, wmax, seed, ptr(off), ptr(col), ptr(w, C.c_uint32), ptr(perm))
+    if rc:
+        raise DdpError(rc, "ddp_gen_random_chain failed")
+    return CSR(n, off, col, w, perm=perm)
+
+
+def gen_maze(rows: int, cols: int, wall_p: float, seed: int) -> CSR:
+    """4-connected grid, walls with probability wall_p, a carved monotone
+    corridor (0,0) -> (rows-1, cols-1), unit weights.  extra['cell_node']
+    maps cells to node ids (-1 = wall)."""
+    cells = rows * cols
+    cell_node = np.empty(cells, np.int32)
+    off = np.empty(cells + 1, np.int32)
+    col = np.empty(4 * cells, np.int32)
+    w = np.empty(4 * cells, np.uint32)
+    xy = np.empty(2 * cells, np.int32)
+    nn = C.c_int32()
+    ne = C.c_int64()
+    rc = lib().ddp_gen_maze(rows, cols, int(round(wall_p * 1000)), seed, ptr(cell_node), C.byref(nn),
+                            C.byref(ne), ptr(off), ptr(col), ptr(w, C.c_uint32), ptr(xy))
+    if rc:
+        raise DdpError(rc, "ddp_gen_maze failed")
+    n, e = nn.value, ne.value
+    g = CSR(n, off[:n + 1].copy(), col[:e].copy(), w[:e].copy(), xy=xy[:2 * n].reshape(n, 2).copy())
+    g.extra["cell_node"] = cell_node
+    g.extra["shape"] = (rows, cols)
+    return g
+
+
+def gen_updates(g: CSR, nbatches: int, per_batch: int, inserts_per_batch: int, wmin: int, wmax: int,
+                seed: int, protect_next: Optional[np.ndarray] = None):
+    """Update batches in the Updates.txt model: per batch, `inserts_per_batch`
+    inserts of arcs absent from the pre-batch graph, then deletes drawn
+    uniformly over live unprotected arcs.  Returns (flag, u, v, w) arrays of
+    nbatches*per_batch entries."""
+    m = nbatches * per_batch
+    flag = np.empty(m, np.int32)
+    u = np.empty(m, np.int32)
+    v = np.empty(m, np.int32)
+    w = np.empty(m, np.uint32)
+    pn = protect_next if protect_next is not None else g.protect_next()
+    rc = lib().ddp_gen_updates(g.n, g.e, ptr(g.off), ptr(g.col), ptr(g.w, C.c_uint32),
+                               ptr(_i32(pn)) if pn is not None else None, nbatches, per_batch,
+                               inserts_per_batch, wmin, wmax, seed, ptr(flag), ptr(u), ptr(v),
+                               ptr(w, C.c_uint32))
+    if rc:
+        raise DdpError(rc, "ddp_gen_updates failed")
+    return flag, u, v, w
+
+
+def gen_pairs(g: CSR, npairs: int, hop_lo: int, hop_hi: int, seed: int, bfs_cap_level: int = 6,
+              threads: int = 0):
+    """(S, T, wanted_hops): per pair a seeded source, a hop target drawn
+    log-uniformly in [hop_lo, hop_hi]; targets up to bfs_cap_level hops are
+    taken from a truncated BFS level, deeper ones uniformly at random."""
+    S = np.empty(npairs, np.int32)
+    T = np.empty(npairs, np.int32)
+    want = np.empty(npairs, np.int32)
+    threads = threads or min(16, os.cpu_count() or 1)
+    rc = lib().ddp_gen_pairs(g.n, ptr(g.off), ptr(g.col), npairs, hop_lo, hop_hi, bfs_cap_level, seed,
+                             threads, ptr(S), ptr(T), ptr(want))
+    if rc:
+        raise DdpError(rc, "ddp_gen_pairs failed")
+    return S, T, want
+
+
+# ---------------------------------------------------------------------------
+# text I/O in the reference's formats
+def read_graph_text(path: str) -> CSR:
+    n = C.c_int32()
+    e = C.c_int64()
+    off = C.POINTER(C.c_int32)()
+    col = C.POINTER(C.c_int32)()
+    w = C.POINTER(C.c_uint32)()
+    check(lib().ddp_io_read_graph_text(path.encode(), C.byref(n), C.byref(e), C.byref(off), C.byref(col),
+                                       C.byref(w)))
+    try:
+        N, E = n.value, e.value
+        g = CSR(N, np.ctypeslib.as_array(off, (N + 1,)).copy(),
+                np.ctypeslib.as_array(col, (max(E, 1),))[:E].copy(),
+                np.ctypeslib.as_array(w, (max(E, 1),))[:E].copy())
+    finally:
+        for p in (off, col, w):
+            lib().ddp_free(C.cast(p, C.c_void_p))
+    return g
+
+
+def write_graph_text(path: str, g: CSR) -> None:
+    check(lib().ddp_io_write_graph_text(path.encode(), g.n, g.e, ptr(_i32(g.off)), ptr(_i32(g.col)),
+                                        ptr(_u32(g.w), C.c_uint32)))
+
+
+def read_ints_text(path: str, max_count: int) -> np.ndarray:
+    out = np.empty(max_count, np.int32)
+    cnt = C.c_int64()
+    check(lib().ddp_io_read_ints_text(path.encode(), max_count, ptr(out), C.byref(cnt)))
+    return out[:cnt.value].copy()
+
+
+def write_ints_text(path: str, vals) -> None:
+    v = _i32(vals)
+    check(lib().ddp_io_write_ints_text(path.encode(), len(v), ptr(v)))
+
+
+def read_updates_text(path: str):
+    """Returns a list of batches, each (flag, u, v, w) arrays."""
+    nb = C.c_int32()
+    cnt = C.POINTER(C.c_int32)()
+    fl, uu, vv = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    ww = C.POINTER(C.c_uint32)()
+    check(lib().ddp_io_read_updates_text(path.encode(), C.byref(nb), C.byref(cnt), C.byref(fl), C.byref(uu),
+                                         C.byref(vv), C.byref(ww)))
+    try:
+        counts = np.ctypeslib.as_array(cnt, (max(nb.value, 1),))[:nb.value].copy()
+        tot = int(counts.sum())
+        arr = [np.ctypeslib.as_array(p, (max(tot, 1),))[:tot].copy() for p in (fl, uu, vv, ww)]
+    finally:
+        for p in (cnt, fl, uu, vv, ww):
+            lib().ddp_free(C.cast(p, C.c_void_p))
+    out, k = [], 0
+    for c in counts:
+        out.append(tuple(a[k:k + c] for a in arr))
+        k += int(c)
+    return out
+
+
+def write_updates_text(path: str, batches) -> None:
+    counts = _i32([len(b[0]) for b in batches])
+    cat = [np.concatenate([b[i] for b in batches]) if batches else np.empty(0) for i in range(4)]
+    check(lib().ddp_io_write_updates_text(path.encode(), len(counts), ptr(counts), ptr(_i32(cat[0])),
+                                          ptr(_i32(cat[1])), ptr(_i32(cat[2])), ptr(_u32(cat[3]), C.c_uint32)))
+
+
+# ---------------------------------------------------------------------------
+# device objects
+def _opts(K=0, delta=0, block=0, grid=0, queue_cap=0) -> Opts:
+    return Opts(int(K), int(delta), int(block), int(grid), int(queue_cap), None)
+
+
+@dataclass
+class SolveResult:
+    cost: int
+    path: np.ndarray
+    stats: np.ndarray  # expanded, scanned, relaxed, iterations
+
+    @property
+    def found(self) -> bool:
+        return self.cost != INF
+
+
+class Heuristic:
+    def __init__(self, graph: "DeviceGraph", target: int, kind: int, user_h=None, want_values=False):
+        self.graph, self.target, self.kind = graph, int(target), int(kind)
+        self.values = np.empty(graph.n, np.int32) if want_values else None
+        uh = _i32(user_h) if user_h is not None else None
+        h = C.c_void_p()
+        check(lib().ddp_heuristic_build(graph.handle, int(target), int(kind), ptr(uh), ptr(self.values),
+                                        C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().ddp_heuristic_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceGraph:
+    """A graph uploaded to the GPU (ddp_graph)."""
+
+    def __init__(self, handle: C.c_void_p, n: int, e: int):
+        self.handle, self.n, self.e = handle, n, e
+
+    @classmethod
+    def from_csr(cls, g: CSR) -> "DeviceGraph":
+        h = C.c_void_p()
+        check(lib().ddp_graph_from_csr(g.n, g.e, ptr(_i32(g.off)), len(g.off), ptr(_i32(g.col)),
+                                       ptr(_u32(g.w), C.c_uint32), C.byref(h)))
+        dg = cls(h, g.n, g.e)
+        if g.xy is not None:
+            dg.set_coords(g.xy)
+        return dg
+
+    @classmethod
+    def load_text(cls, path: str) -> "DeviceGraph":
+        h = C.c_void_p()
+        check(lib().ddp_graph_load_text(path.encode(), C.byref(h)))
+        n = C.c_int32()
+        e = C.c_int64()
+        check(lib().ddp_graph_info(h, C.byref(n), C.byref(e), None, None))
+        return cls(h, n.value, e.value)
+
+    def set_coords(self, xy) -> None:
+        a = _i32(np.asarray(xy).reshape(-1))
+        check(lib().ddp_graph_set_coords(self.handle, ptr(a)))
+
+    def info(self):
+        n, e, lo, hi = C.c_int32(), C.c_int64(), C.c_uint32(), C.c_uint32()
+        check(lib().ddp_graph_info(self.handle, C.byref(n), C.byref(e), C.byref(lo), C.byref(hi)))
+        return dict(n=n.value, e=e.value, wmin=lo.value, wmax=hi.value)
+
+    def read_csr(self) -> CSR:
+        off = np.empty(self.n + 1, np.int32)
+        check(lib().ddp_graph_read_csr(self.handle, ptr(off), None, None))
+        e = int(off[-1])
+        col = np.empty(e, np.int32)
+        w = np.empty(e, np.uint32)
+        check(lib().ddp_graph_read_csr(self.handle, None, ptr(col), ptr(w, C.c_uint32)))
+        return CSR(self.n, off, col, w)
+
+    def heuristic(self, target: int, kind: int = H_BFS_HOPS, user_h=None, want_values=False) -> Heuristic:
+        return Heuristic(self, target, kind, user_h, want_values)
+
+    def solve(self, s: int, t: int, heuristic: Optional[Heuristic] = None, **opts) -> SolveResult:
+        q = C.c_void_p()
+        o = _opts(**opts)
+        check(lib().ddp_solve(self.handle, heuristic.handle if heuristic else None, int(s), int(t),
+                              C.byref(o), C.byref(q)))
+        try:
+            cost = C.c_int32()
+            check(lib().ddp_query_cost(q, C.byref(cost)))
+            ln = C.c_int32()
+            check(lib().ddp_path_read(q, None, 0, C.byref(ln)))
+            path = np.empty(ln.value, np.int32)
+            if ln.value:
+                check(lib().ddp_path_read(q, ptr(path), ln.value, C.byref(ln)))
+            st = np.empty(4, np.int64)
+            check(lib().ddp_query_stats(q, st.ctypes.data_as(C.POINTER(C.c_int64))))
+        finally:
+            lib().ddp_query_free(q)
+        return SolveResult(cost.value, path, st)
+
+    def close(self):
+        if self.handle:
+            lib().ddp_graph_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchEngine:
+    """Many (source, target) queries in one persistent kernel (ddp_batch)."""
+
+    def __init__(self, graph: DeviceGraph, hkind: int = H_BFS_HOPS, **opts):
+        self.graph = graph
+        b = C.c_void_p()
+        o = _opts(**opts)
+        check(lib().ddp_batch_create(graph.handle, int(hkind), C.byref(o), C.byref(b)))
+        self.handle = b
+        self.n_last = 0
+
+    def solve(self, S, T):
+        S, T = _i32(S), _i32(T)
+        n = len(S)
+        cost = np.empty(n, np.int32)
+        plen = np.empty(n, np.int32)
+        check(lib().ddp_batch_solve(self.handle, n, ptr(S), ptr(T), ptr(cost), ptr(plen)))
+        self.n_last = n
+        return cost, plen
+
+    def solve_device(self, n: int, d_S: int, d_T: int, d_cost: int, d_plen: int = 0):
+        """Device pointers (ints); stream-ordered, call sync() to wait."""
+        check(lib().ddp_batch_solve_device(self.handle, int(n), C.c_void_p(d_S), C.c_void_p(d_T),
+                                           C.c_void_p(d_cost), C.c_void_p(d_plen or None)))
+        self.n_last = n
+
+    def sync(self):
+        check(lib().ddp_batch_sync(self.handle))
+
+    def path(self, i: int) -> np.ndarray:
+        ln = C.c_int32()
+        check(lib().ddp_batch_path(self.handle, int(i), None, 0, C.byref(ln)))
+        p = np.empty(max(ln.value, 0), np.int32)
+        if ln.value > 0:
+            check(lib().ddp_batch_path(self.handle, int(i), ptr(p), ln.value, C.byref(ln)))
+        return p
+
+    def stats(self):
+        n = self.n_last
+        st = np.empty(4 * n, np.int64)
+        t0 = np.empty(n, np.int64)
+        t1 = np.empty(n, np.int64)
+        P = C.POINTER(C.c_int64)
+        check(lib().ddp_batch_stats(self.handle, st.ctypes.data_as(P), t0.ctypes.data_as(P),
+                                    t1.ctypes.data_as(P)))
+        return st.reshape(n, 4), t0, t1
+
+    def launches(self) -> int:
+        x = C.c_int32()
+        check(lib().ddp_batch_launches(self.handle, C.byref(x)))
+        return x.value
+
+    def close(self):
+        if self.handle:
+            lib().ddp_batch_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+from .lib_mirror import (A_Star, Dynamic_Graph, GPU_A_Star, GPU_Dynamic_Graph, GPU_Graph,  # noqa: E402
+                         Graph)

@@ -1,0 +1,571 @@
+// GA* search engine: device code shared by the single-query (whole grid)
+// and batched (one CTA per query slot) kernels.
+//
+// What it replaces (lkoshale/DDP, LIB/include/kernels/a_star_kernels.cu):
+//   extractMin  (:7-61)   K threads pop K heap tops
+//   A_star_expand (:67-133) one thread per node, spin lock per child
+//   keepHeapPQ + setNV + insertPQ (:138-237) heap repair, O(N) flag scan,
+//                                           round-robin re-insert
+//   checkMIN (:243-254)   stop when no heap top has f < f(t)
+//
+// How it works here:
+//   * Open list = threshold buckets on f (near-far): `near` holds entries
+//     with f < T, `far` the rest.  One iteration expands up to K entries of
+//     near (all of it when K = 0); improved children go to `next` when
+//     f < T, else to `far`.  When near and next are empty the far pile is
+//     split at T' = T + delta (or at its smallest f + delta): f < T' moves to
+//     near, the rest is compacted.  Stale entries (g changed since the push)
+//     and entries with f >= f(t) are dropped at every pop and split.
+//   * Termination (the GA* test of checkMIN, made exact): the search ends
+//     when near, next and far are all empty after pruning, i.e. no open
+//     node has f < f(t).  With an admissible heuristic g(t) is then optimal.
+//   * Expansion is warp-cooperative: 32 popped nodes per warp, their rows are
+//     concatenated by a warp prefix sum and walked 32 arcs at a time, so arc
+//     loads are 8-byte {head, w} reads of consecutive row slices.
+//   * Relaxation is lock-free: one 64-bit word per node packs (g << 32 |
+//     parent); a plain L2 read filters the (common) non-improving arcs, then
+//     a CAS loop installs strictly smaller g.  No spin locks (the reference's
+//     `while(!leaveLoop)` lock with __syncthreads inside divergent code is
+//     gone).
+//   * Pushes are warp-aggregated: one atomic per warp per target queue.
+//   * Every loop bound is data-driven; the only wait is the group barrier,
+//     which is bounded (common.cuh).
+#pragma once
+
+#include "common.cuh"
+
+namespace ddp {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Control block of one search slot (global memory).  Push counters rotate
+// over 4 phases so that a counter is reset two phases before it is used
+// again, with a single barrier per phase.
+struct SearchCtl {
+    int nq[4];            // pushes into near/next (or BFS frontier) this phase
+    int fq[4];            // pushes into far this phase
+    unsigned int mf[4];   // min f kept in far during a split phase
+    int err[4];           // ST_* raised during the phase (read after its barrier)
+    int touched;          // nodes whose state left the initial value
+    int status;           // ST_* bits
+    int iters;            // phases run
+    int pad;
+    unsigned long long expanded, scanned, relaxed, pad2;
+    unsigned int bar_count, bar_gen;  // grid barrier (single-query form)
+};
+
+// Buffers of one slot.
+struct SlotBufs {
+    unsigned long long *state;  // n, (g << 32) | parent; all-ones = unreached
+    uint2 *q0, *q1;             // near / next ping-pong, cap_q entries {node, g}
+    uint2 *f0, *f1;             // far ping-pong, cap_f entries
+    int32_t *touched;           // n: nodes whose state must be reset
+    uint32_t *hops;             // n: per-target hop heuristic (may be null)
+    SearchCtl *ctl;
+    int64_t cap_q, cap_f;
+};
+
+// ---- groups ------------------------------------------------------------------
+struct CtaGroup {
+    int *status;
+    __device__ int rank() const { return threadIdx.x; }
+    __device__ int size() const { return blockDim.x; }
+    __device__ int warp() const { return threadIdx.x >> 5; }
+    __device__ int nwarps() const { return blockDim.x >> 5; }
+    __device__ void sync() const { __syncthreads(); }
+};
+
+struct GridGroup {
+    GridBarrier bar;
+    int *status;
+    __device__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+    __device__ int size() const { return gridDim.x * blockDim.x; }
+    __device__ int warp() const { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+    __device__ int nwarps() const { return (gridDim.x * blockDim.x) >> 5; }
+    __device__ void sync() const { grid_sync(bar, status); }
+};
+
+// ---- heuristics (h(v) as uint32, INF_G = "cannot reach the target") -------
+struct HeurZero {
+    __device__ uint32_t operator()(int32_t) const { return 0; }
+};
+
+struct HeurHops {  // reverse-BFS hop count x scale (GA_star/bfs_hx.cu)
+    const uint32_t *hops;
+    uint32_t scale;
+    __device__ uint32_t operator()(int32_t v) const {
+        uint32_t x = __ldcg(hops + v);
+        if (x == HOPS_INF) return INF_G;
+        unsigned long long p = (unsigned long long)x * scale;
+        return p >= INF_G ? INF_G : (uint32_t)p;
+    }
+};
+
+struct HeurArray {  // caller-supplied h; negative = cannot reach the target
+    const int32_t *h;
+    __device__ uint32_t operator()(int32_t v) const {
+        int32_t x = __ldg(h + v);
+        return x < 0 ? INF_G : (uint32_t)x;
+    }
+};
+
+struct HeurManhattan {
+    const int32_t *xy;
+    int32_t tx, ty;
+    uint32_t scale;
+    __device__ uint32_t operator()(int32_t v) const {
+        int2 p = __ldg(reinterpret_cast<const int2 *>(xy) + v);
+        unsigned long long d = (unsigned long long)(abs(p.x - tx)) + (unsigned long long)(abs(p.y - ty));
+        d *= scale;
+        return d >= INF_G ? INF_G : (uint32_t)d;
+    }
+};
+
+// ---- warp helpers ----------------------------------------------------------
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Returns this lane's slot in a warp-aggregated append (or -1 when !pred).
+__device__ __forceinline__ int warp_append(bool pred, int *counter) {
+    unsigned m = __ballot_sync(FULL, pred);
+    if (m == 0) return -1;
+    int lane = lane_id();
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(FULL, base, leader);
+    return pred ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+__device__ __forceinline__ int warp_excl_scan(int x, int *total) {
+    int lane = lane_id();
+    int v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += y;
+    }
+    *total = __shfl_sync(FULL, v, 31);
+    return v - x;
+}
+
+// Records an error for phase `ph` (consistent control flow after the
+// barrier) and in the sticky status word (reporting).
+__device__ __forceinline__ void raise_err(SearchCtl *ctl, int ph, int bit) {
+    atomicOr(&ctl->err[ph], bit);
+    atomicOr(&ctl->status, bit);
+}
+
+__device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
+    uint32_t c = a + b;
+    return c < a ? 0xFFFFFFFFu : c;
+}
+
+// Per-warp staging of 32 popped rows (shared memory).
+struct WarpRows {
+    int excl[32];
+    int rb[32];      // first arc of the base row
+    int bdeg[32];    // base-row length (diff arcs follow)
+    int drb[32];     // first arc of the diff row
+    uint32_t g[32];
+    int u[32];
+};
+
+__device__ __forceinline__ int row_owner(const WarpRows &wr, int k) {
+    int o = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+        if (wr.excl[o + step] <= k) o += step;
+    return o;
+}
+
+__device__ __forceinline__ uint2 row_arc(const DevGraph &G, const WarpRows &wr, int o, int k,
+                                         bool fwd) {
+    int j = k - wr.excl[o];
+    if (j < wr.bdeg[o]) return fwd ? __ldg(G.arc + wr.rb[o] + j) : __ldg(G.rarc + wr.rb[o] + j);
+    j -= wr.bdeg[o];
+    return fwd ? __ldcg(G.darc + wr.drb[o] + j) : __ldcg(G.drarc + wr.drb[o] + j);
+}
+
+// ---- search parameters -------------------------------------------------------
+struct SearchParams {
+    int32_t s, t;
+    uint32_t delta;
+    int32_t K;  // 0 = whole near bucket per iteration
+};
+
+struct SearchResult {
+    uint32_t cost;  // g(t) + h(t), >= INF_G when unreachable
+    int iters;
+};
+
+// One A* run on one slot, executed collectively by every thread of `grp`.
+// Precondition: slot state is all-ones (unreached) for every node.
+template <class Grp, class Heur>
+__device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const SlotBufs &B,
+                                   const Heur &H, const SearchParams &P, WarpRows *wrows) {
+    SearchCtl *ctl = B.ctl;
+    const int lane = lane_id();
+    WarpRows &wr = wrows[threadIdx.x >> 5];
+    const bool has_diff = G.doff != nullptr;
+
+    if (grp.rank() == 0) {
+        for (int i = 0; i < 4; i++) {
+            ctl->nq[i] = 0;
+            ctl->fq[i] = 0;
+            ctl->mf[i] = 0xFFFFFFFFu;
+            ctl->err[i] = 0;
+        }
+        ctl->touched = 1;
+        ctl->iters = 0;
+        ctl->expanded = ctl->scanned = ctl->relaxed = 0;
+        B.state[P.s] = st_make(0, -1);
+        B.touched[0] = P.s;
+        B.q0[0] = make_uint2((uint32_t)P.s, 0u);
+    }
+    grp.sync();
+
+    uint2 *qcur = B.q0, *qnxt = B.q1;
+    uint2 *fcur = B.f0, *falt = B.f1;
+    int64_t nnear = 1, head = 0, nnext = 0, nfar = 0;
+    const uint32_t hs = H(P.s);
+    uint32_t T = sat_add(hs, P.delta);
+    uint32_t Tsplit = T;
+    bool splitting = false;
+    unsigned long long n_exp = 0, n_scan = 0, n_rel = 0;
+    int it = 0;
+    int status = 0;
+    const int64_t max_phases = 4 * (int64_t)G.n + (1 << 22);
+
+    for (;;) {
+        const int PH = (it + 1) & 3, RS = (it + 3) & 3;
+        // f(t) snapshot: only decreases, so a stale value only prunes less.
+        const uint64_t st_t = __ldcg(B.state + P.t);
+        const uint32_t ht = H(P.t);
+        const uint64_t ft64 = (uint64_t)st_g(st_t) + ht;
+        const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
+        int64_t end = 0;
+        if (!splitting) {
+            end = (P.K > 0) ? min(nnear, head + (int64_t)P.K) : nnear;
+            for (int64_t base = head + (int64_t)grp.warp() * 32; base < end;
+                 base += (int64_t)grp.nwarps() * 32) {
+                const int64_t idx = base + lane;
+                int u = -1, rb = 0, bdeg = 0, drb = 0, deg = 0;
+                uint32_t gu = 0;
+                if (idx < end) {
+                    uint2 en = __ldcg(qcur + idx);
+                    u = (int)en.x;
+                    gu = en.y;
+                    uint64_t su = __ldcg(B.state + u);
+                    if (st_g(su) == gu && u != P.t) {
+                        uint32_t hu = H(u);
+                        uint64_t fu = (uint64_t)gu + hu;
+                        if (fu < ft) {
+                            rb = __ldg(G.off + u);
+                            bdeg = __ldg(G.off + u + 1) - rb;
+                            deg = bdeg;
+                            if (has_diff) {
+                                drb = __ldcg(G.doff + u);
+                                deg += __ldcg(G.doff + u + 1) - drb;
+                            }
+                            n_exp++;
+                        }
+                    }
+                }
+                int total;
+                int ex = warp_excl_scan(deg, &total);
+                wr.excl[lane] = ex;
+                wr.rb[lane] = rb;
+                wr.bdeg[lane] = bdeg;
+                wr.drb[lane] = drb;
+                wr.g[lane] = gu;
+                wr.u[lane] = u;
+                __syncwarp();
+                n_scan += (lane == 0) ? (unsigned long long)total : 0ull;
+                for (int kb = 0; kb < total; kb += 32) {
+                    const int k = kb + lane;
+                    bool to_near = false, to_far = false, first = false;
+                    int v = 0;
+                    uint32_t ng = 0;
+                    if (k < total) {
+                        const int o = row_owner(wr, k);
+                        const uint2 a = row_arc(G, wr, o, k, true);
+                        v = (int)a.x;
+                        const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
+                        if (v >= 0 && ng64 < INF_G) {
+                            ng = (uint32_t)ng64;
+                            uint64_t sv = __ldcg(B.state + v);
+                            if (ng < st_g(sv)) {
+                                const uint32_t hv = H(v);
+                                const uint64_t fv = (uint64_t)ng + hv;
+                                if (fv < ft) {
+                                    const uint64_t nv = st_make(ng, wr.u[o]);
+                                    for (;;) {
+                                        uint64_t prev = atomicCAS(B.state + v, sv, nv);
+                                        if (prev == sv) {
+                                            first = st_g(sv) >= INF_G;
+                                            if (fv < T) to_near = true;
+                                            else to_far = true;
+                                            break;
+                                        }
+                                        sv = prev;
+                                        if (ng >= st_g(sv)) break;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    if (to_near || to_far) n_rel++;
+                    int slot = warp_append(to_near, &ctl->nq[PH]);
+                    if (slot >= 0) {
+                        int64_t pos = nnext + slot;
+                        if (pos < B.cap_q) qnxt[pos] = make_uint2((uint32_t)v, ng);
+                        else raise_err(ctl, PH, ST_OVERFLOW);
+                    }
+                    slot = warp_append(to_far, &ctl->fq[PH]);
+                    if (slot >= 0) {
+                        int64_t pos = nfar + slot;
+                        if (pos < B.cap_f) fcur[pos] = make_uint2((uint32_t)v, ng);
+                        else raise_err(ctl, PH, ST_OVERFLOW);
+                    }
+                    slot = warp_append(first, &ctl->touched);
+                    if (slot >= 0) B.touched[slot] = v;  // at most n first touches
+                }
+                __syncwarp();
+            }
+        } else {
+            // split the far pile at Tsplit
+            unsigned int local_min = 0xFFFFFFFFu;
+            for (int64_t base = (int64_t)grp.warp() * 32; base < nfar;
+                 base += (int64_t)grp.nwarps() * 32) {
+                const int64_t idx = base + lane;
+                bool to_near = false, keep = false;
+                uint2 en = make_uint2(0u, 0u);
+                if (idx < nfar) {
+                    en = __ldcg(fcur + idx);
+                    uint64_t sv = __ldcg(B.state + en.x);
+                    if (st_g(sv) == en.y) {
+                        uint64_t f = (uint64_t)en.y + H((int)en.x);
+                        if (f < ft) {
+                            if (f < Tsplit) {
+                                to_near = true;
+                            } else {
+                                keep = true;
+                                local_min = min(local_min, (uint32_t)f);
+                            }
+                        }
+                    }
+                }
+                int slot = warp_append(to_near, &ctl->nq[PH]);
+                if (slot >= 0) {
+                    if (slot < B.cap_q) qcur[slot] = en;
+                    else raise_err(ctl, PH, ST_OVERFLOW);
+                }
+                slot = warp_append(keep, &ctl->fq[PH]);
+                if (slot >= 0) falt[slot] = en;  // compaction never grows the pile
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) local_min = min(local_min, __shfl_xor_sync(FULL, local_min, o));
+            if (lane == 0 && local_min != 0xFFFFFFFFu) atomicMin(&ctl->mf[PH], local_min);
+        }
+
+        grp.sync();
+        if (grp.rank() == 0) {
+            ctl->nq[RS] = 0;
+            ctl->fq[RS] = 0;
+            ctl->mf[RS] = 0xFFFFFFFFu;
+            ctl->err[RS] = 0;
+        }
+        const int a = *(volatile int *)&ctl->nq[PH];
+        const int b = *(volatile int *)&ctl->fq[PH];
+        const unsigned int m = *(volatile unsigned int *)&ctl->mf[PH];
+        const int perr = *(volatile int *)&ctl->err[PH];
+        status = *(volatile int *)&ctl->status;
+        it++;
+        if ((perr & ST_OVERFLOW) || (status & ST_TIMEOUT)) break;
+        if (it > max_phases) {
+            // a search never needs this many phases; stop instead of spinning
+            if (grp.rank() == 0) atomicOr(&ctl->status, ST_TIMEOUT);
+            break;
+        }
+        if (!splitting) {
+            nnext += a;
+            nfar += b;
+            head = end;
+            if (head >= nnear) {
+                uint2 *t2 = qcur;
+                qcur = qnxt;
+                qnxt = t2;
+                nnear = nnext;
+                nnext = 0;
+                head = 0;
+                if (nnear == 0) {
+                    splitting = true;
+                    Tsplit = sat_add(T, P.delta);
+                }
+            }
+        } else {
+            uint2 *t2 = fcur;
+            fcur = falt;
+            falt = t2;
+            nfar = b;
+            nnear = a;
+            head = 0;
+            nnext = 0;
+            if (nnear > 0) {
+                T = Tsplit;
+                splitting = false;
+            } else if (nfar == 0) {
+                break;  // open list empty below f(t): done
+            } else {
+                Tsplit = sat_add(m, P.delta);
+            }
+        }
+        if (nnear > B.cap_q || nfar > B.cap_f) {
+            if (grp.rank() == 0) atomicOr(&ctl->status, ST_OVERFLOW);
+            break;  // uniform: every thread computed the same counts
+        }
+    }
+
+    // fold per-thread counters
+    if (lane == 0 && n_scan) atomicAdd(&ctl->scanned, n_scan);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_exp += __shfl_xor_sync(FULL, n_exp, o);
+        n_rel += __shfl_xor_sync(FULL, n_rel, o);
+    }
+    if (lane == 0) {
+        if (n_exp) atomicAdd(&ctl->expanded, n_exp);
+        if (n_rel) atomicAdd(&ctl->relaxed, n_rel);
+    }
+    grp.sync();
+    SearchResult r;
+    const uint64_t st_t = __ldcg(B.state + P.t);
+    const uint64_t c = (uint64_t)st_g(st_t) + H(P.t);
+    r.cost = (st_g(st_t) >= INF_G || c >= INF_G) ? 0xFFFFFFFFu : (uint32_t)c;
+    r.iters = it;
+    if (grp.rank() == 0) ctl->iters = it;
+    return r;
+}
+
+// Reverse BFS from `t` (hop counts to t), executed collectively by `grp`.
+// Replaces GA_star/bfs_hx.cu: the level loop runs on the device (no per-level
+// D2H of the frontier size), frontier expansion is warp-cooperative over
+// reverse-CSR rows, and each node is claimed once with a CAS.
+template <class Grp>
+__device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &B, int32_t t,
+                             WarpRows *wrows) {
+    SearchCtl *ctl = B.ctl;
+    const int lane = lane_id();
+    WarpRows &wr = wrows[threadIdx.x >> 5];
+    const bool has_diff = G.doff != nullptr;
+    int *fa = reinterpret_cast<int *>(B.q0);
+    int *fb = reinterpret_cast<int *>(B.q1);
+    const int64_t capf = B.cap_q * 2;  // uint2 slots reused as ints
+
+    for (int64_t i = grp.rank(); i < G.n; i += grp.size()) B.hops[i] = HOPS_INF;
+    if (grp.rank() == 0) {
+        for (int i = 0; i < 4; i++) {
+            ctl->nq[i] = 0;
+            ctl->err[i] = 0;
+        }
+    }
+    grp.sync();
+    if (grp.rank() == 0) {
+        B.hops[t] = 0;
+        fa[0] = t;
+    }
+    grp.sync();
+    int64_t nf = 1;
+    uint32_t lvl = 0;
+    int it = 0;
+    while (nf > 0) {
+        const int PH = (it + 1) & 3, RS = (it + 3) & 3;
+        for (int64_t base = (int64_t)grp.warp() * 32; base < nf; base += (int64_t)grp.nwarps() * 32) {
+            const int64_t idx = base + lane;
+            int rb = 0, bdeg = 0, drb = 0, deg = 0;
+            if (idx < nf) {
+                int u = __ldcg(fa + idx);
+                rb = __ldg(G.roff + u);
+                bdeg = __ldg(G.roff + u + 1) - rb;
+                deg = bdeg;
+                if (has_diff) {
+                    drb = __ldcg(G.droff + u);
+                    deg += __ldcg(G.droff + u + 1) - drb;
+                }
+            }
+            int total;
+            int ex = warp_excl_scan(deg, &total);
+            wr.excl[lane] = ex;
+            wr.rb[lane] = rb;
+            wr.bdeg[lane] = bdeg;
+            wr.drb[lane] = drb;
+            __syncwarp();
+            for (int kb = 0; kb < total; kb += 32) {
+                const int k = kb + lane;
+                bool claim = false;
+                int p = -1;
+                if (k < total) {
+                    const int o = row_owner(wr, k);
+                    p = (int)row_arc(G, wr, o, k, false).x;
+                    if (p >= 0 && __ldcg(B.hops + p) == HOPS_INF)
+                        claim = atomicCAS(B.hops + p, HOPS_INF, lvl + 1) == HOPS_INF;
+                }
+                int slot = warp_append(claim, &ctl->nq[PH]);
+                if (slot >= 0) {
+                    if (slot < capf) fb[slot] = p;
+                    else raise_err(ctl, PH, ST_OVERFLOW);
+                }
+            }
+            __syncwarp();
+        }
+        grp.sync();
+        if (grp.rank() == 0) {
+            ctl->nq[RS] = 0;
+            ctl->err[RS] = 0;
+        }
+        nf = *(volatile int *)&ctl->nq[PH];
+        const int perr = *(volatile int *)&ctl->err[PH];
+        const int status = *(volatile int *)&ctl->status;
+        it++;
+        lvl++;
+        int *tmp = fa;
+        fa = fb;
+        fb = tmp;
+        if ((perr & ST_OVERFLOW) || (status & ST_TIMEOUT)) break;
+    }
+    grp.sync();
+}
+
+// Parent walk t -> s into path[0..cap) in s..t order; returns the length
+// (0 when unreachable).  One thread.
+__device__ inline int32_t write_path(const SlotBufs &B, int32_t s, int32_t t, int32_t *path,
+                                     int32_t cap, int32_t n, int *status) {
+    uint64_t st = __ldcg(B.state + t);
+    if (st_g(st) >= INF_G) return 0;
+    int32_t len = 0;
+    int32_t c = t;
+    while (c >= 0 && len <= n) {
+        if (len < cap) path[len] = c;
+        len++;
+        if (c == s) break;
+        c = st_parent(__ldcg(B.state + c));
+    }
+    if (len <= cap) {
+        for (int32_t i = 0, j = len - 1; i < j; i++, j--) {
+            int32_t x = path[i];
+            path[i] = path[j];
+            path[j] = x;
+        }
+    } else {
+        // too long: second walk keeps the first `cap` ids in s..t order
+        atomicOr(status, ST_PATH_TRUNC);
+        c = t;
+        for (int32_t i = len - 1; i >= 0 && c >= 0; i--) {
+            if (i < cap) path[i] = c;
+            c = st_parent(__ldcg(B.state + c));
+        }
+    }
+    return len;
+}
+
+}  // namespace ddp

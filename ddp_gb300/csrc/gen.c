@@ -1,0 +1,430 @@
+/*
+ * Seeded workload generators for the GA* / dynamic A* path.
+ *
+ * These replace the reference's generator programs with deterministic,
+ * seed-addressed C (same results on x86_64 and aarch64; no rand(), no
+ * platform-dependent integer widths):
+ *   - random digraph with a Hamiltonian chain (GA_star/GenerateCSR.cpp
+ *     builds the CSR from an edge list; GA_star/randomGraph.py and
+ *     genGraph.py draw the edges; the chain guarantees reachability),
+ *   - 4-connected grid maze with random walls and a carved corridor
+ *     (maze/create_maze.cpp:69-113, same arc order up/down/right/left),
+ *   - insert/delete update batches (DA_star/genDynamicGraph.cpp:122-173
+ *     writes Updates.txt; here deletes are drawn too, chain arcs protected),
+ *   - source/target pairs with a target BFS hop distance.
+ * All CSR outputs here use N+1 offsets (off[N] = E).
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ddp_gb300.h"
+
+/* ---------------- PRNG: splitmix64 seeding, xoshiro256** stream -------- */
+typedef struct {
+    uint64_t s[4];
+} rng_t;
+
+static uint64_t splitmix64(uint64_t *x) {
+    uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static void rng_seed(rng_t *r, uint64_t seed, uint64_t stream) {
+    uint64_t x = seed ^ (stream * 0xD1B54A32D192ED03ull);
+    for (int i = 0; i < 4; i++) r->s[i] = splitmix64(&x);
+}
+
+static inline uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static inline uint64_t rng_next(rng_t *r) {
+    uint64_t *s = r->s;
+    uint64_t result = rotl(s[1] * 5, 7) * 9;
+    uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return result;
+}
+
+/* uniform integer in [0, n) without modulo bias (Lemire) */
+static inline uint64_t rng_below(rng_t *r, uint64_t n) {
+    if (n <= 1) return 0;
+    uint64_t x = rng_next(r) >> 32; /* 32-bit draws suffice for n < 2^32 */
+    uint64_t m = x * n;
+    uint32_t l = (uint32_t)m;
+    if (l < (uint32_t)n) {
+        uint32_t t = (uint32_t)(-(uint32_t)n) % (uint32_t)n;
+        while (l < t) {
+            x = rng_next(r) >> 32;
+            m = x * n;
+            l = (uint32_t)m;
+        }
+    }
+    return m >> 32;
+}
+
+static inline double rng_unit(rng_t *r) { return (double)(rng_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* ---------------- (u,v) hash set with multiplicity ---------------------- */
+typedef struct {
+    uint64_t *keys; /* 0 = empty, 1 = tombstone, else (u<<32 | v) + 2 */
+    uint64_t mask;
+} pairset_t;
+
+static int pairset_init(pairset_t *p, uint64_t expected) {
+    uint64_t cap = 1024;
+    while (cap < expected * 2) cap <<= 1;
+    p->keys = (uint64_t *)calloc(cap, sizeof(uint64_t));
+    p->mask = cap - 1;
+    return p->keys ? 0 : -1;
+}
+
+static inline uint64_t pair_key(uint32_t u, uint32_t v) { return (((uint64_t)u << 32) | v) + 2; }
+
+static inline uint64_t pair_hash(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    return k;
+}
+
+static int pairset_has(const pairset_t *p, uint32_t u, uint32_t v) {
+    uint64_t k = pair_key(u, v), i = pair_hash(k) & p->mask;
+    for (;;) {
+        uint64_t c = p->keys[i];
+        if (c == 0) return 0;
+        if (c == k) return 1;
+        i = (i + 1) & p->mask;
+    }
+}
+
+static void pairset_add(pairset_t *p, uint32_t u, uint32_t v) {
+    uint64_t k = pair_key(u, v), i = pair_hash(k) & p->mask;
+    for (;;) {
+        uint64_t c = p->keys[i];
+        if (c == 0 || c == 1) {
+            p->keys[i] = k;
+            return;
+        }
+        i = (i + 1) & p->mask;
+    }
+}
+
+static void pairset_del(pairset_t *p, uint32_t u, uint32_t v) {
+    uint64_t k = pair_key(u, v), i = pair_hash(k) & p->mask;
+    for (;;) {
+        uint64_t c = p->keys[i];
+        if (c == 0) return;
+        if (c == k) {
+            p->keys[i] = 1;
+            return;
+        }
+        i = (i + 1) & p->mask;
+    }
+}
+
+/* ---------------- random digraph with a Hamiltonian chain --------------- */
+int ddp_gen_random_chain(int32_t n, int64_t e_total, uint32_t wmin, uint32_t wmax, uint64_t seed,
+                         int32_t *off, int32_t *col, uint32_t *w, int32_t *perm_out) {
+    if (n < 2 || e_total < n - 1 || wmax < wmin) return -1;
+    if ((double)e_total > 0.5 * (double)n * (double)(n - 1)) return -1; /* too dense to sample */
+    rng_t r;
+    rng_seed(&r, seed, 1);
+    int32_t *perm = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t *au = (int32_t *)malloc(sizeof(int32_t) * (size_t)e_total);
+    int32_t *av = (int32_t *)malloc(sizeof(int32_t) * (size_t)e_total);
+    uint32_t *aw = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)e_total);
+    pairset_t ps;
+    if (!perm || !au || !av || !aw || pairset_init(&ps, (uint64_t)e_total)) {
+        free(perm);
+        free(au);
+        free(av);
+        free(aw);
+        return -2;
+    }
+    for (int32_t i = 0; i < n; i++) perm[i] = i;
+    for (int32_t i = n - 1; i > 0; i--) {
+        int32_t j = (int32_t)rng_below(&r, (uint64_t)i + 1);
+        int32_t t = perm[i];
+        perm[i] = perm[j];
+        perm[j] = t;
+    }
+    uint64_t wspan = (uint64_t)wmax - wmin + 1;
+    int64_t m = 0;
+    for (int32_t i = 0; i + 1 < n; i++) {
+        au[m] = perm[i];
+        av[m] = perm[i + 1];
+        aw[m] = wmin + (uint32_t)rng_below(&r, wspan);
+        pairset_add(&ps, (uint32_t)perm[i], (uint32_t)perm[i + 1]);
+        m++;
+    }
+    while (m < e_total) {
+        uint32_t u = (uint32_t)rng_below(&r, (uint64_t)n);
+        uint32_t v = (uint32_t)rng_below(&r, (uint64_t)n);
+        if (u == v || pairset_has(&ps, u, v)) continue;
+        pairset_add(&ps, u, v);
+        au[m] = (int32_t)u;
+        av[m] = (int32_t)v;
+        aw[m] = wmin + (uint32_t)rng_below(&r, wspan);
+        m++;
+    }
+    /* counting sort by source, stable in generation order */
+    memset(off, 0, sizeof(int32_t) * ((size_t)n + 1));
+    for (int64_t i = 0; i < m; i++) off[au[i] + 1]++;
+    for (int32_t i = 0; i < n; i++) off[i + 1] += off[i];
+    int32_t *fill = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    memcpy(fill, off, sizeof(int32_t) * (size_t)n);
+    for (int64_t i = 0; i < m; i++) {
+        int32_t k = fill[au[i]]++;
+        col[k] = av[i];
+        w[k] = aw[i];
+    }
+    if (perm_out) memcpy(perm_out, perm, sizeof(int32_t) * (size_t)n);
+    free(fill);
+    free(perm);
+    free(au);
+    free(av);
+    free(aw);
+    free(ps.keys);
+    return 0;
+}
+
+/* ---------------- grid maze ---------------------------------------------- */
+int ddp_gen_maze(int32_t rows, int32_t cols, uint32_t wall_permille, uint64_t seed,
+                 int32_t *cell_node, int32_t *n_nodes, int64_t *n_arcs, int32_t *off, int32_t *col,
+                 uint32_t *w, int32_t *xy) {
+    if (rows < 1 || cols < 1 || wall_permille > 1000) return -1;
+    rng_t r;
+    rng_seed(&r, seed, 2);
+    int64_t cells = (int64_t)rows * cols;
+    uint8_t *wall = (uint8_t *)malloc((size_t)cells);
+    if (!wall) return -2;
+    for (int64_t i = 0; i < cells; i++) wall[i] = rng_below(&r, 1000) < wall_permille;
+    /* carve a random monotone corridor (0,0) -> (rows-1, cols-1) */
+    int32_t i = 0, j = 0;
+    wall[0] = 0;
+    while (i != rows - 1 || j != cols - 1) {
+        if (i == rows - 1) j++;
+        else if (j == cols - 1) i++;
+        else if (rng_below(&r, 2)) j++;
+        else i++;
+        wall[(int64_t)i * cols + j] = 0;
+    }
+    int32_t n = 0;
+    for (int64_t c = 0; c < cells; c++) cell_node[c] = wall[c] ? -1 : n++;
+    int64_t m = 0;
+    for (i = 0; i < rows; i++) {
+        for (j = 0; j < cols; j++) {
+            int64_t c = (int64_t)i * cols + j;
+            if (wall[c]) continue;
+            int32_t u = cell_node[c];
+            off[u] = (int32_t)m;
+            xy[2 * u] = j;
+            xy[2 * u + 1] = i;
+            /* arc order of maze/create_maze.cpp:93-111: up, down, right, left */
+            if (i > 0 && !wall[c - cols]) { col[m] = cell_node[c - cols]; w[m++] = 1; }
+            if (i < rows - 1 && !wall[c + cols]) { col[m] = cell_node[c + cols]; w[m++] = 1; }
+            if (j < cols - 1 && !wall[c + 1]) { col[m] = cell_node[c + 1]; w[m++] = 1; }
+            if (j > 0 && !wall[c - 1]) { col[m] = cell_node[c - 1]; w[m++] = 1; }
+        }
+    }
+    off[n] = (int32_t)m;
+    *n_nodes = n;
+    *n_arcs = m;
+    free(wall);
+    return 0;
+}
+
+/* ---------------- update batches ---------------------------------------- */
+typedef struct {
+    int32_t u, v;
+    uint32_t w;
+} arc_t;
+
+int ddp_gen_updates(int32_t n, int64_t e, const int32_t *off, const int32_t *col, const uint32_t *w,
+                    const int32_t *protect_next, int32_t nbatches, int32_t per_batch,
+                    int32_t inserts_per_batch, uint32_t wmin, uint32_t wmax, uint64_t seed,
+                    int32_t *flag, int32_t *uu, int32_t *vv, uint32_t *ww) {
+    if (n < 2 || inserts_per_batch > per_batch || wmax < wmin) return -1;
+    rng_t r;
+    rng_seed(&r, seed, 3);
+    int64_t total_ins = (int64_t)nbatches * inserts_per_batch;
+    pairset_t ps;
+    if (pairset_init(&ps, (uint64_t)(e + total_ins))) return -2;
+    arc_t *pool = (arc_t *)malloc(sizeof(arc_t) * (size_t)(e + total_ins + 1));
+    arc_t *pending = (arc_t *)malloc(sizeof(arc_t) * (size_t)(inserts_per_batch + 1));
+    if (!pool || !pending) {
+        free(ps.keys);
+        free(pool);
+        free(pending);
+        return -2;
+    }
+    int64_t np = 0;
+    for (int32_t u = 0; u < n; u++) {
+        for (int32_t k = off[u]; k < off[u + 1]; k++) {
+            int32_t v = col[k];
+            if (v < 0) continue;
+            pairset_add(&ps, (uint32_t)u, (uint32_t)v);
+            if (protect_next && protect_next[u] == v) continue;
+            pool[np].u = u;
+            pool[np].v = v;
+            pool[np].w = w[k];
+            np++;
+        }
+    }
+    uint64_t wspan = (uint64_t)wmax - wmin + 1;
+    int64_t o = 0;
+    int32_t ndel = per_batch - inserts_per_batch;
+    for (int32_t b = 0; b < nbatches; b++) {
+        /* inserts: arcs absent from the pre-batch graph */
+        for (int32_t k = 0; k < inserts_per_batch; k++) {
+            uint32_t u, v;
+            do {
+                u = (uint32_t)rng_below(&r, (uint64_t)n);
+                v = (uint32_t)rng_below(&r, (uint64_t)n);
+            } while (u == v || pairset_has(&ps, u, v));
+            pairset_add(&ps, u, v);
+            pending[k].u = (int32_t)u;
+            pending[k].v = (int32_t)v;
+            pending[k].w = wmin + (uint32_t)rng_below(&r, wspan);
+            flag[o] = 1;
+            uu[o] = (int32_t)u;
+            vv[o] = (int32_t)v;
+            ww[o] = pending[k].w;
+            o++;
+        }
+        /* deletes: uniform over live, unprotected arcs of the pre-batch graph */
+        for (int32_t k = 0; k < ndel; k++) {
+            if (np == 0) {
+                flag[o] = 0;
+                uu[o] = vv[o] = -1;
+                ww[o] = 0;
+                o++;
+                continue;
+            }
+            int64_t idx = (int64_t)rng_below(&r, (uint64_t)np);
+            arc_t a = pool[idx];
+            pool[idx] = pool[np - 1];
+            np--;
+            pairset_del(&ps, (uint32_t)a.u, (uint32_t)a.v);
+            flag[o] = 0;
+            uu[o] = a.u;
+            vv[o] = a.v;
+            ww[o] = a.w;
+            o++;
+        }
+        for (int32_t k = 0; k < inserts_per_batch; k++) pool[np++] = pending[k];
+    }
+    free(ps.keys);
+    free(pool);
+    free(pending);
+    return 0;
+}
+
+/* ---------------- source/target pairs ----------------------------------- */
+typedef struct {
+    int32_t n;
+    const int32_t *off, *col;
+    int32_t npairs, hop_lo, hop_hi, bfs_cap;
+    uint64_t seed;
+    int32_t *S, *T, *want;
+    int32_t next;
+    pthread_mutex_t mu;
+} pairs_ctx;
+
+static void *pairs_worker(void *arg) {
+    pairs_ctx *c = (pairs_ctx *)arg;
+    int32_t n = c->n;
+    int32_t *dist = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t *q = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    for (int32_t i = 0; i < n; i++) dist[i] = -1;
+    for (;;) {
+        pthread_mutex_lock(&c->mu);
+        int32_t p = c->next < c->npairs ? c->next++ : -1;
+        pthread_mutex_unlock(&c->mu);
+        if (p < 0) break;
+        rng_t r;
+        rng_seed(&r, c->seed, 0x100000000ull + (uint64_t)p);
+        int32_t s = (int32_t)rng_below(&r, (uint64_t)n);
+        double lo = log((double)c->hop_lo), hi = log((double)c->hop_hi + 1.0);
+        int32_t d = (int32_t)floor(exp(lo + (hi - lo) * rng_unit(&r)));
+        if (d < c->hop_lo) d = c->hop_lo;
+        if (d > c->hop_hi) d = c->hop_hi;
+        c->want[p] = d;
+        c->S[p] = s;
+        int32_t t = -1;
+        if (d <= c->bfs_cap) {
+            /* truncated forward BFS from s to level d */
+            int32_t qh = 0, qt = 0, level_begin = 0, level_end = 0;
+            dist[s] = 0;
+            q[qt++] = s;
+            int32_t last_lvl_b = 0, last_lvl_e = 1;
+            for (int32_t lvl = 0; lvl < d && qh < qt; lvl++) {
+                level_begin = qh;
+                level_end = qt;
+                for (int32_t i = level_begin; i < level_end; i++) {
+                    int32_t u = q[i];
+                    for (int32_t k = c->off[u]; k < c->off[u + 1]; k++) {
+                        int32_t v = c->col[k];
+                        if (v >= 0 && dist[v] < 0) {
+                            dist[v] = lvl + 1;
+                            q[qt++] = v;
+                        }
+                    }
+                }
+                qh = level_end;
+                if (qt > qh) {
+                    last_lvl_b = qh;
+                    last_lvl_e = qt;
+                }
+            }
+            if (last_lvl_e > last_lvl_b && !(last_lvl_b == 0 && last_lvl_e == 1))
+                t = q[last_lvl_b + (int32_t)rng_below(&r, (uint64_t)(last_lvl_e - last_lvl_b))];
+            for (int32_t i = 0; i < qt; i++) dist[q[i]] = -1;
+        }
+        if (t < 0) {
+            do {
+                t = (int32_t)rng_below(&r, (uint64_t)n);
+            } while (t == s && n > 1);
+        }
+        c->T[p] = t;
+    }
+    free(dist);
+    free(q);
+    return NULL;
+}
+
+int ddp_gen_pairs(int32_t n, const int32_t *off, const int32_t *col, int32_t npairs, int32_t hop_lo,
+                  int32_t hop_hi, int32_t bfs_cap_level, uint64_t seed, int32_t threads, int32_t *S,
+                  int32_t *T, int32_t *want_hops) {
+    if (n < 2 || npairs < 0 || hop_lo < 1 || hop_hi < hop_lo) return -1;
+    pairs_ctx c;
+    c.n = n;
+    c.off = off;
+    c.col = col;
+    c.npairs = npairs;
+    c.hop_lo = hop_lo;
+    c.hop_hi = hop_hi;
+    c.bfs_cap = bfs_cap_level;
+    c.seed = seed;
+    c.S = S;
+    c.T = T;
+    c.want = want_hops;
+    c.next = 0;
+    pthread_mutex_init(&c.mu, NULL);
+    if (threads < 1) threads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, pairs_worker, &c);
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&c.mu);
+    return 0;
+}

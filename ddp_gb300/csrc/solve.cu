@@ -1,0 +1,791 @@
+// Heuristic build, single-query GA* and the batched multi-query engine.
+//
+// Replaces GA_star/bfs_hx.cu (heuristic program), LIB/include/a_star.cu
+// (GPU_A_Star host loop of 5 kernels + ~12 host<->device crossings per
+// iteration) with one cooperative kernel per query (single form) or one
+// persistent kernel per batch (batched form).
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "graph.cuh"
+#include "solve.cuh"
+
+namespace ddp {
+
+constexpr int MAX_WARPS = 32;
+
+// ---- slot arrays -------------------------------------------------------------
+size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops) {
+    size_t b = 0;
+    b += sizeof(unsigned long long) * (size_t)n;  // state
+    b += sizeof(int32_t) * (size_t)n;             // touched
+    if (hops) b += sizeof(uint32_t) * (size_t)n;
+    b += 2 * sizeof(uint2) * (size_t)cap_q;
+    b += 2 * sizeof(uint2) * (size_t)cap_f;
+    b += sizeof(SearchCtl);
+    return b;
+}
+
+int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, bool hops,
+                cudaStream_t st) {
+    sa = SlotArrays();
+    sa.n = n;
+    sa.nslots = nslots;
+    sa.cap_q = cap_q;
+    sa.cap_f = cap_f;
+    const size_t S = (size_t)nslots;
+    DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)n * S));
+    DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * S));
+    if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
+    DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * 2 * S));
+    DDP_CUDA(cudaMalloc(&sa.f, sizeof(uint2) * (size_t)cap_f * 2 * S));
+    DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
+    DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * S, st));
+    DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl) * S, st));
+    return DDP_OK;
+}
+
+void slots_free(SlotArrays &sa) {
+    cudaFree(sa.state);
+    cudaFree(sa.touched);
+    cudaFree(sa.hops);
+    cudaFree(sa.q);
+    cudaFree(sa.f);
+    cudaFree(sa.ctl);
+    sa = SlotArrays();
+}
+
+__device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
+    SlotBufs b;
+    const size_t n = (size_t)sa.n;
+    b.state = sa.state + n * i;
+    b.touched = sa.touched + n * i;
+    b.hops = sa.hops ? sa.hops + n * i : nullptr;
+    b.q0 = sa.q + (size_t)sa.cap_q * 2 * i;
+    b.q1 = b.q0 + sa.cap_q;
+    b.f0 = sa.f + (size_t)sa.cap_f * 2 * i;
+    b.f1 = b.f0 + sa.cap_f;
+    b.ctl = sa.ctl + i;
+    b.cap_q = sa.cap_q;
+    b.cap_f = sa.cap_f;
+    return b;
+}
+
+__device__ __forceinline__ long long global_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---- kernels -------------------------------------------------------------------
+// Clears the state words a finished search touched (slot 0 .. nslots-1).
+__global__ void k_reset_touched(SlotArrays sa) {
+    SlotBufs B = slot_of(sa, blockIdx.y);
+    const int cnt = B.ctl->touched;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+        B.state[B.touched[i]] = ~0ull;
+}
+
+// Single-query reverse BFS (heuristic build) over the whole grid.
+__global__ void __launch_bounds__(512) k_bfs_single(DevGraph G, SlotArrays sa, uint32_t *hops,
+                                                    int32_t t) {
+    __shared__ WarpRows wrows[MAX_WARPS];
+    SlotBufs B = slot_of(sa, 0);
+    B.hops = hops;
+    GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
+    run_bfs_hops(grp, G, B, t, wrows);
+}
+
+// Single-query GA* over the whole grid (cooperative launch).
+template <class Heur>
+__global__ void __launch_bounds__(512)
+    k_solve_single(DevGraph G, SlotArrays sa, Heur H, SearchParams P, int32_t *out, int32_t *path,
+                   int32_t path_cap) {
+    __shared__ WarpRows wrows[MAX_WARPS];
+    SlotBufs B = slot_of(sa, 0);
+    GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
+    SearchResult r = run_search(grp, G, B, H, P, wrows);
+    if (grp.rank() == 0) {
+        out[0] = r.cost >= INF_G ? DDP_INF : (int32_t)r.cost;
+        out[1] = write_path(B, P.s, P.t, path, path_cap, G.n, &B.ctl->status);
+        out[2] = B.ctl->status;
+        out[3] = r.iters;
+    }
+}
+
+// Batched GA*: one CTA per slot, queries claimed from a shared counter so
+// that CTAs finishing short searches take the next query (dynamic load
+// balance over uneven depths).
+template <int HK>
+__global__ void __launch_bounds__(512) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
+    __shared__ WarpRows wrows[MAX_WARPS];
+    __shared__ int sq;
+    SlotBufs B = slot_of(sa, blockIdx.x);
+    CtaGroup grp{&B.ctl->status};
+    for (;;) {
+        if (threadIdx.x == 0) sq = atomicAdd(A.work, 1);
+        __syncthreads();
+        const int q = sq;
+        __syncthreads();
+        if (q >= A.nq) break;
+        const int32_t s = __ldg(A.S + q), t = __ldg(A.T + q);
+        long long t0 = 0;
+        if (threadIdx.x == 0) {
+            t0 = global_ns();
+            B.ctl->status = 0;
+        }
+        if (s < 0 || s >= G.n || t < 0 || t >= G.n) {
+            if (threadIdx.x == 0) {
+                A.cost[q] = DDP_INF;
+                if (A.plen) A.plen[q] = -1;
+                atomicOr(A.status, ST_OVERFLOW << 8);  // "invalid query" bit
+            }
+            continue;
+        }
+        __syncthreads();
+        SearchParams P{s, t, A.delta, A.K};
+        SearchResult r;
+        if (HK == 1) {
+            run_bfs_hops(grp, G, B, t, wrows);
+            r = run_search(grp, G, B, HeurHops{B.hops, G.wmin}, P, wrows);
+        } else if (HK == 2) {
+            int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
+            r = run_search(grp, G, B, HeurManhattan{G.xy, tp.x, tp.y, G.wmin}, P, wrows);
+        } else {
+            r = run_search(grp, G, B, HeurZero{}, P, wrows);
+        }
+        if (threadIdx.x == 0) {
+            const int st = B.ctl->status;
+            int32_t len = 0;
+            if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths)
+                len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
+                                 &B.ctl->status);
+            A.cost[q] = (st & (ST_OVERFLOW | ST_TIMEOUT)) ? -1
+                        : (r.cost >= INF_G)                ? DDP_INF
+                                                           : (int32_t)r.cost;
+            if (A.plen) A.plen[q] = len;
+            if (A.qstatus) A.qstatus[q] = B.ctl->status;
+            if (A.stats) {
+                A.stats[4 * (size_t)q + 0] = (long long)B.ctl->expanded;
+                A.stats[4 * (size_t)q + 1] = (long long)B.ctl->scanned;
+                A.stats[4 * (size_t)q + 2] = (long long)B.ctl->relaxed;
+                A.stats[4 * (size_t)q + 3] = (long long)r.iters;
+            }
+            atomicOr(A.status, B.ctl->status);
+        }
+        __syncthreads();
+        const int cnt = B.ctl->touched;
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) B.state[B.touched[i]] = ~0ull;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (A.tstart) A.tstart[q] = t0;
+            if (A.tend) A.tend[q] = global_ns();
+        }
+    }
+}
+
+// ---- launch helpers ---------------------------------------------------------
+static int sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+template <class K>
+static int coop_grid(K kernel, int block, int want) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    int maxg = per_sm * sm_count();
+    if (maxg < 1) maxg = 1;
+    if (want > 0 && want < maxg) return want;
+    return maxg;
+}
+
+template <class K>
+static cudaError_t coop_launch(K kernel, int grid, int block, void **args, cudaStream_t st) {
+    return cudaLaunchCooperativeKernel((const void *)kernel, dim3(grid), dim3(block), args, 0, st);
+}
+
+uint32_t auto_delta(const ddp_graph *g) {
+    // bucket width ~ a typical arc weight: wide enough for parallel buckets,
+    // narrow enough to keep re-expansions rare
+    uint32_t d = (g->wmin + g->wmax) / 2;
+    return d < 1 ? 1 : d;
+}
+
+}  // namespace ddp
+
+using namespace ddp;
+
+// ---- single-query workspace ------------------------------------------------
+struct Workspace {
+    SlotArrays sa;
+    int32_t *d_out = nullptr;   // cost, path len, status, iters
+    int32_t *d_path = nullptr;  // n
+    int64_t cap = 0;
+};
+
+namespace ddp {
+void workspace_release(ddp_graph *g) {
+    if (!g->ws) return;
+    slots_free(g->ws->sa);
+    cudaFree(g->ws->d_out);
+    cudaFree(g->ws->d_path);
+    delete g->ws;
+    g->ws = nullptr;
+}
+
+static int workspace_ensure(ddp_graph *g, int64_t cap) {
+    if (g->ws && g->ws->cap >= cap) return DDP_OK;
+    workspace_release(g);
+    Workspace *w = new Workspace();
+    g->ws = w;
+    int rc = slots_alloc(w->sa, g->n, 1, cap, cap, false, g->stream);
+    if (rc) {
+        workspace_release(g);
+        return rc;
+    }
+    w->cap = cap;
+    DDP_CUDA(cudaMalloc(&w->d_out, sizeof(int32_t) * 8));
+    DDP_CUDA(cudaMalloc(&w->d_path, sizeof(int32_t) * (size_t)g->n));
+    return DDP_OK;
+}
+}  // namespace ddp
+
+struct ddp_heuristic {
+    ddp_graph *g = nullptr;
+    int kind = DDP_H_ZERO;
+    int32_t target = -1;
+    uint32_t *d_hops = nullptr;  // BFS kind
+    int32_t *d_h = nullptr;      // USER kind
+    int32_t tx = 0, ty = 0;      // MANHATTAN kind
+};
+
+struct ddp_query {
+    int32_t cost = DDP_INF;
+    std::vector<int32_t> path;
+    int64_t stats[4] = {0, 0, 0, 0};
+};
+
+extern "C" {
+
+int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_t *user_h,
+                        int32_t *out_h, ddp_heuristic **out) {
+    if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (target < 0 || target >= g->n) return fail(DDP_ERR_INVALID, "target out of range");
+    std::lock_guard<std::mutex> lk(g->mu);
+    ddp_heuristic *h = new ddp_heuristic();
+    h->g = g;
+    h->kind = kind;
+    h->target = target;
+    std::vector<int32_t> host;
+    switch (kind) {
+    case DDP_H_ZERO:
+        if (out_h) std::fill(out_h, out_h + g->n, 0);
+        break;
+    case DDP_H_BFS_HOPS: {
+        int rc = workspace_ensure(g, (int64_t)g->n + 1024);
+        if (rc) {
+            delete h;
+            return rc;
+        }
+        cudaError_t e = cudaMalloc(&h->d_hops, sizeof(uint32_t) * (size_t)g->n);
+        if (e != cudaSuccess) {
+            delete h;
+            return cuda_fail(e, "cudaMalloc(hops)");
+        }
+        DevGraph G = graph_view(g);
+        SlotArrays sa = g->ws->sa;
+        DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl), g->stream));
+        int grid = coop_grid(k_bfs_single, 512, 0);
+        void *args[] = {&G, &sa, &h->d_hops, &target};
+        e = coop_launch(k_bfs_single, grid, 512, args, g->stream);
+        if (e != cudaSuccess) {
+            cudaFree(h->d_hops);
+            delete h;
+            return cuda_fail(e, "k_bfs_single launch");
+        }
+        SearchCtl ctl;
+        DDP_CUDA(cudaMemcpyAsync(&ctl, sa.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, g->stream));
+        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        if (ctl.status & (ST_OVERFLOW | ST_TIMEOUT)) {
+            cudaFree(h->d_hops);
+            delete h;
+            return fail(ctl.status & ST_TIMEOUT ? DDP_ERR_TIMEOUT : DDP_ERR_QUEUE_OVERFLOW,
+                        "heuristic BFS did not complete");
+        }
+        if (out_h) {
+            std::vector<uint32_t> hops((size_t)g->n);
+            DDP_CUDA(cudaMemcpy(hops.data(), h->d_hops, sizeof(uint32_t) * (size_t)g->n,
+                                cudaMemcpyDeviceToHost));
+            for (int32_t i = 0; i < g->n; i++)
+                out_h[i] = hops[(size_t)i] == HOPS_INF ? -1
+                                                        : (int32_t)std::min<uint64_t>(
+                                                              (uint64_t)hops[(size_t)i] * g->wmin,
+                                                              (uint64_t)INT32_MAX - 1);
+        }
+        break;
+    }
+    case DDP_H_MANHATTAN: {
+        if (!g->d_xy) {
+            delete h;
+            return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
+        }
+        h->tx = g->h_xy[2 * (size_t)target];
+        h->ty = g->h_xy[2 * (size_t)target + 1];
+        if (out_h)
+            for (int32_t i = 0; i < g->n; i++) {
+                int64_t d = llabs((long long)g->h_xy[2 * (size_t)i] - h->tx) +
+                            llabs((long long)g->h_xy[2 * (size_t)i + 1] - h->ty);
+                out_h[i] = (int32_t)std::min<int64_t>(d * g->wmin, INT32_MAX - 1);
+            }
+        break;
+    }
+    case DDP_H_USER: {
+        if (!user_h) {
+            delete h;
+            return fail(DDP_ERR_INVALID, "user_h is null");
+        }
+        cudaError_t e = cudaMalloc(&h->d_h, sizeof(int32_t) * (size_t)g->n);
+        if (e != cudaSuccess) {
+            delete h;
+            return cuda_fail(e, "cudaMalloc(h)");
+        }
+        DDP_CUDA(cudaMemcpy(h->d_h, user_h, sizeof(int32_t) * (size_t)g->n,
+                            cudaMemcpyHostToDevice));
+        if (out_h) std::memcpy(out_h, user_h, sizeof(int32_t) * (size_t)g->n);
+        break;
+    }
+    default:
+        delete h;
+        return fail(DDP_ERR_INVALID, "unknown heuristic kind");
+    }
+    *out = h;
+    return DDP_OK;
+}
+
+int ddp_heuristic_free(ddp_heuristic *h) {
+    if (!h) return DDP_OK;
+    cudaFree(h->d_hops);
+    cudaFree(h->d_h);
+    delete h;
+    return DDP_OK;
+}
+
+int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t target,
+              const ddp_opts *opts, ddp_query **out) {
+    if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (source < 0 || source >= g->n || target < 0 || target >= g->n)
+        return fail(DDP_ERR_INVALID, "source/target out of range");
+    if (h && h->g != g) return fail(DDP_ERR_INVALID, "heuristic belongs to another graph");
+    if (h && h->kind != DDP_H_ZERO && h->target != target)
+        return fail(DDP_ERR_INVALID, "heuristic was built for another target");
+    ddp_opts o = opts ? *opts : ddp_opts{};
+    std::lock_guard<std::mutex> lk(g->mu);
+    cudaStream_t st = o.stream ? (cudaStream_t)o.stream : g->stream;
+    const int block = o.block > 0 ? std::min(o.block, 512) : 512;
+    int64_t cap = o.queue_cap > 0 ? o.queue_cap : (int64_t)g->n + 1024;
+    const uint32_t delta = o.delta > 0 ? (uint32_t)o.delta : auto_delta(g);
+    DevGraph G = graph_view(g);
+    SearchParams P{source, target, delta, o.K};
+    for (int attempt = 0; attempt < 4; attempt++) {
+        int rc = workspace_ensure(g, cap);
+        if (rc) return rc;
+        Workspace *w = g->ws;
+        DDP_CUDA(cudaMemsetAsync(w->sa.ctl, 0, sizeof(SearchCtl), st));
+        cudaError_t e;
+        const int kind = h ? h->kind : DDP_H_ZERO;
+        if (kind == DDP_H_BFS_HOPS) {
+            HeurHops H{h->d_hops, g->wmin};
+            int grid = coop_grid(k_solve_single<HeurHops>, block, o.grid);
+            void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
+            e = coop_launch(k_solve_single<HeurHops>, grid, block, args, st);
+        } else if (kind == DDP_H_MANHATTAN) {
+            HeurManhattan H{g->d_xy, h->tx, h->ty, g->wmin};
+            int grid = coop_grid(k_solve_single<HeurManhattan>, block, o.grid);
+            void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
+            e = coop_launch(k_solve_single<HeurManhattan>, grid, block, args, st);
+        } else if (kind == DDP_H_USER) {
+            HeurArray H{h->d_h};
+            int grid = coop_grid(k_solve_single<HeurArray>, block, o.grid);
+            void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
+            e = coop_launch(k_solve_single<HeurArray>, grid, block, args, st);
+        } else {
+            HeurZero H{};
+            int grid = coop_grid(k_solve_single<HeurZero>, block, o.grid);
+            void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
+            e = coop_launch(k_solve_single<HeurZero>, grid, block, args, st);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "k_solve_single launch");
+        k_reset_touched<<<dim3(256, 1), 256, 0, st>>>(w->sa);
+        DDP_CUDA(cudaGetLastError());
+        int32_t res[4];
+        SearchCtl ctl;
+        DDP_CUDA(cudaMemcpyAsync(res, w->d_out, sizeof(res), cudaMemcpyDeviceToHost, st));
+        DDP_CUDA(cudaMemcpyAsync(&ctl, w->sa.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, st));
+        DDP_CUDA(cudaStreamSynchronize(st));
+        if (res[2] & ST_TIMEOUT) return fail(DDP_ERR_TIMEOUT, "search barrier timed out");
+        if (res[2] & ST_OVERFLOW) {
+            if (o.queue_cap > 0) return fail(DDP_ERR_QUEUE_OVERFLOW, "search queue overflow");
+            cap *= 2;  // automatic capacity: grow and retry
+            continue;
+        }
+        ddp_query *q = new ddp_query();
+        q->cost = res[0];
+        q->stats[0] = (int64_t)ctl.expanded;
+        q->stats[1] = (int64_t)ctl.scanned;
+        q->stats[2] = (int64_t)ctl.relaxed;
+        q->stats[3] = res[3];
+        if (res[1] > 0) {
+            q->path.resize((size_t)res[1]);
+            cudaError_t ce = cudaMemcpy(q->path.data(), w->d_path, sizeof(int32_t) * (size_t)res[1],
+                                        cudaMemcpyDeviceToHost);
+            if (ce != cudaSuccess) {
+                delete q;
+                return cuda_fail(ce, "path readback");
+            }
+        }
+        *out = q;
+        return DDP_OK;
+    }
+    return fail(DDP_ERR_QUEUE_OVERFLOW, "search queue overflow after retries");
+}
+
+int ddp_query_cost(const ddp_query *q, int32_t *cost) {
+    if (!q || !cost) return fail(DDP_ERR_INVALID, "null argument");
+    *cost = q->cost;
+    return DDP_OK;
+}
+
+int ddp_path_read(const ddp_query *q, int32_t *buf, int32_t cap, int32_t *len) {
+    if (!q || !len) return fail(DDP_ERR_INVALID, "null argument");
+    *len = (int32_t)q->path.size();
+    if (buf && cap > 0)
+        std::memcpy(buf, q->path.data(), sizeof(int32_t) * std::min<size_t>((size_t)cap, q->path.size()));
+    return DDP_OK;
+}
+
+int ddp_query_stats(const ddp_query *q, int64_t *stats4) {
+    if (!q || !stats4) return fail(DDP_ERR_INVALID, "null argument");
+    for (int i = 0; i < 4; i++) stats4[i] = q->stats[i];
+    return DDP_OK;
+}
+
+int ddp_query_free(ddp_query *q) {
+    delete q;
+    return DDP_OK;
+}
+
+}  // extern "C"
+
+// ---- batched engine ----------------------------------------------------------
+struct ddp_batch {
+    ddp_graph *g = nullptr;
+    int hkind = DDP_H_ZERO;
+    ddp_opts o{};
+    cudaStream_t stream = nullptr;
+    int block = 512;
+    SlotArrays sa;
+    // device buffers sized for the largest batch seen
+    int32_t cap_q_n = 0;
+    int32_t *d_S = nullptr, *d_T = nullptr, *d_cost = nullptr, *d_plen = nullptr, *d_paths = nullptr;
+    int32_t *d_qstatus = nullptr;
+    long long *d_stats = nullptr, *d_t0 = nullptr, *d_t1 = nullptr;
+    int *d_work = nullptr, *d_status = nullptr;
+    int32_t path_cap = 0;
+    int32_t last_n = 0;
+    int32_t launches = 0;
+    // CUDA graph of the last device-pointer solve
+    cudaGraphExec_t gexec = nullptr;
+    const void *gkey[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int32_t gkey_n = -1;
+    // paths of queries re-run on the single-query engine
+    std::map<int32_t, std::vector<int32_t>> overflow_paths;
+};
+
+namespace ddp {
+
+static int batch_grow(ddp_batch *b, int32_t n) {
+    if (n <= b->cap_q_n) return DDP_OK;
+    cudaFree(b->d_S);
+    cudaFree(b->d_T);
+    cudaFree(b->d_cost);
+    cudaFree(b->d_plen);
+    cudaFree(b->d_paths);
+    cudaFree(b->d_qstatus);
+    cudaFree(b->d_stats);
+    cudaFree(b->d_t0);
+    cudaFree(b->d_t1);
+    const size_t N = (size_t)n;
+    DDP_CUDA(cudaMalloc(&b->d_S, sizeof(int32_t) * N));
+    DDP_CUDA(cudaMalloc(&b->d_T, sizeof(int32_t) * N));
+    DDP_CUDA(cudaMalloc(&b->d_cost, sizeof(int32_t) * N));
+    DDP_CUDA(cudaMalloc(&b->d_plen, sizeof(int32_t) * N));
+    DDP_CUDA(cudaMalloc(&b->d_paths, sizeof(int32_t) * N * (size_t)b->path_cap));
+    DDP_CUDA(cudaMalloc(&b->d_qstatus, sizeof(int32_t) * N));
+    DDP_CUDA(cudaMalloc(&b->d_stats, sizeof(long long) * 4 * N));
+    DDP_CUDA(cudaMalloc(&b->d_t0, sizeof(long long) * N));
+    DDP_CUDA(cudaMalloc(&b->d_t1, sizeof(long long) * N));
+    b->cap_q_n = n;
+    return DDP_OK;
+}
+
+static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, const int32_t *dT,
+                                int32_t *dcost, int32_t *dplen) {
+    BatchArgs A;
+    A.S = dS;
+    A.T = dT;
+    A.nq = n;
+    A.cost = dcost;
+    A.plen = dplen;
+    A.paths = b->d_paths;
+    A.path_cap = b->path_cap;
+    A.qstatus = b->d_qstatus;
+    A.stats = b->d_stats;
+    A.tstart = b->d_t0;
+    A.tend = b->d_t1;
+    A.work = b->d_work;
+    A.status = b->d_status;
+    A.delta = b->o.delta > 0 ? (uint32_t)b->o.delta : auto_delta(b->g);
+    A.K = b->o.K;
+    DevGraph G = graph_view(b->g);
+    cudaError_t e = cudaMemsetAsync(b->d_work, 0, sizeof(int) * 2, b->stream);
+    if (e != cudaSuccess) return e;
+    const int grid = b->sa.nslots;
+    if (b->hkind == DDP_H_BFS_HOPS) k_batch<1><<<grid, b->block, 0, b->stream>>>(G, b->sa, A);
+    else if (b->hkind == DDP_H_MANHATTAN) k_batch<2><<<grid, b->block, 0, b->stream>>>(G, b->sa, A);
+    else k_batch<0><<<grid, b->block, 0, b->stream>>>(G, b->sa, A);
+    return cudaGetLastError();
+}
+
+}  // namespace ddp
+
+extern "C" {
+
+int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out) {
+    if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS && hkind != DDP_H_MANHATTAN)
+        return fail(DDP_ERR_INVALID, "batch heuristic must be ZERO, BFS_HOPS or MANHATTAN");
+    if (hkind == DDP_H_MANHATTAN && !g->d_xy)
+        return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
+    ddp_batch *b = new ddp_batch();
+    b->g = g;
+    b->hkind = hkind;
+    if (opts) b->o = *opts;
+    b->block = b->o.block > 0 ? std::min(b->o.block, 512) : 512;
+    b->path_cap = 1024;
+    cudaError_t e = b->o.stream ? cudaSuccess : cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (b->o.stream) b->stream = (cudaStream_t)b->o.stream;
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    // slots: occupancy-limited, then memory-limited (half of free memory)
+    int per_sm = 0;
+    if (hkind == DDP_H_BFS_HOPS)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, b->block, 0);
+    else if (hkind == DDP_H_MANHATTAN)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, b->block, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<0>, b->block, 0);
+    int nslots = std::max(1, per_sm) * sm_count();
+    if (b->o.grid > 0) nslots = b->o.grid;
+    const int64_t cap = b->o.queue_cap > 0 ? b->o.queue_cap : (int64_t)g->n / 2 + 4096;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    const size_t per = slot_bytes(g->n, cap, cap, hkind == DDP_H_BFS_HOPS);
+    const size_t budget = freeb / 2;
+    if ((size_t)nslots * per > budget) nslots = (int)std::max<size_t>(1, budget / per);
+    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap, hkind == DDP_H_BFS_HOPS, b->stream);
+    if (rc == DDP_OK) {
+        cudaError_t e1 = cudaMalloc(&b->d_work, sizeof(int) * 2);
+        if (e1 != cudaSuccess) rc = cuda_fail(e1, "cudaMalloc(work)");
+        else b->d_status = b->d_work + 1;
+    }
+    if (rc) {
+        ddp_batch_free(b);
+        return rc;
+    }
+    *out = b;
+    return DDP_OK;
+}
+
+int ddp_batch_solve_device(ddp_batch *b, int32_t n, const int32_t *d_sources,
+                           const int32_t *d_targets, int32_t *d_cost, int32_t *d_path_len) {
+    if (!b || n < 0 || (n > 0 && (!d_sources || !d_targets || !d_cost)))
+        return fail(DDP_ERR_INVALID, "bad batch arguments");
+    std::lock_guard<std::mutex> lk(b->g->mu);
+    int rc = batch_grow(b, n);
+    if (rc) return rc;
+    if (n == 0) return DDP_OK;
+    const void *key[5] = {d_sources, d_targets, d_cost, d_path_len, nullptr};
+    bool hit = b->gexec && b->gkey_n == n;
+    for (int i = 0; i < 4 && hit; i++) hit = key[i] == b->gkey[i];
+    if (!hit) {
+        if (b->gexec) {
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+        cudaGraph_t graph;
+        DDP_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+        if (e != cudaSuccess) return cuda_fail(e, "batch capture");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            b->gexec = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+        for (int i = 0; i < 4; i++) b->gkey[i] = key[i];
+        b->gkey_n = n;
+    }
+    DDP_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    b->overflow_paths.clear();
+    b->last_n = n;
+    b->launches = 1;
+    return DDP_OK;
+}
+
+int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32_t *targets,
+                    int32_t *out_cost, int32_t *out_path_len) {
+    if (!b || n < 0 || (n > 0 && (!sources || !targets || !out_cost)))
+        return fail(DDP_ERR_INVALID, "bad batch arguments");
+    {
+        std::lock_guard<std::mutex> lk(b->g->mu);
+        int rc = batch_grow(b, n);
+        if (rc) return rc;
+        if (n == 0) return DDP_OK;
+        b->overflow_paths.clear();
+        DDP_CUDA(cudaMemcpyAsync(b->d_S, sources, sizeof(int32_t) * (size_t)n,
+                                 cudaMemcpyHostToDevice, b->stream));
+        DDP_CUDA(cudaMemcpyAsync(b->d_T, targets, sizeof(int32_t) * (size_t)n,
+                                 cudaMemcpyHostToDevice, b->stream));
+        cudaError_t e = batch_launch(b, n, b->d_S, b->d_T, b->d_cost, b->d_plen);
+        if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
+        b->last_n = n;
+        b->launches = 1;
+        DDP_CUDA(cudaMemcpyAsync(out_cost, b->d_cost, sizeof(int32_t) * (size_t)n,
+                                 cudaMemcpyDeviceToHost, b->stream));
+        if (out_path_len)
+            DDP_CUDA(cudaMemcpyAsync(out_path_len, b->d_plen, sizeof(int32_t) * (size_t)n,
+                                     cudaMemcpyDeviceToHost, b->stream));
+        DDP_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    // queries that outgrew the slot queues are re-run on the single-query
+    // engine, which grows its queues as needed
+    bool any = false;
+    for (int32_t i = 0; i < n; i++) any |= out_cost[i] == -1;
+    if (any) {
+        for (int32_t i = 0; i < n; i++) {
+            if (out_cost[i] != -1) continue;
+            if (sources[i] < 0 || sources[i] >= b->g->n || targets[i] < 0 || targets[i] >= b->g->n)
+                return fail(DDP_ERR_INVALID, "query endpoint out of range");
+            ddp_heuristic *h = nullptr;
+            int rc = ddp_heuristic_build(b->g, targets[i], b->hkind, nullptr, nullptr, &h);
+            if (rc) return rc;
+            ddp_query *q = nullptr;
+            rc = ddp_solve(b->g, h, sources[i], targets[i], &b->o, &q);
+            ddp_heuristic_free(h);
+            if (rc) return rc;
+            out_cost[i] = q->cost;
+            if (out_path_len) out_path_len[i] = (int32_t)q->path.size();
+            b->overflow_paths[i] = q->path;
+            ddp_query_free(q);
+        }
+    }
+    return DDP_OK;
+}
+
+int ddp_batch_sync(ddp_batch *b) {
+    if (!b) return fail(DDP_ERR_INVALID, "null batch");
+    DDP_CUDA(cudaStreamSynchronize(b->stream));
+    return DDP_OK;
+}
+
+int ddp_batch_path(ddp_batch *b, int32_t i, int32_t *buf, int32_t cap, int32_t *len) {
+    if (!b || !len || i < 0 || i >= b->last_n) return fail(DDP_ERR_INVALID, "bad path request");
+    auto it = b->overflow_paths.find(i);
+    if (it != b->overflow_paths.end()) {
+        *len = (int32_t)it->second.size();
+        if (buf && cap > 0)
+            std::memcpy(buf, it->second.data(), sizeof(int32_t) * std::min<size_t>(cap, it->second.size()));
+        return DDP_OK;
+    }
+    int32_t l = 0;
+    DDP_CUDA(cudaStreamSynchronize(b->stream));
+    DDP_CUDA(cudaMemcpy(&l, b->d_plen + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    *len = l;
+    if (l > b->path_cap) {
+        // the slot buffer kept only a prefix; recompute the path on the
+        // single-query engine
+        ddp_heuristic *h = nullptr;
+        int32_t s, t;
+        DDP_CUDA(cudaMemcpy(&s, b->d_S + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        DDP_CUDA(cudaMemcpy(&t, b->d_T + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        int rc = ddp_heuristic_build(b->g, t, b->hkind, nullptr, nullptr, &h);
+        if (rc) return rc;
+        ddp_query *q = nullptr;
+        rc = ddp_solve(b->g, h, s, t, &b->o, &q);
+        ddp_heuristic_free(h);
+        if (rc) return rc;
+        *len = (int32_t)q->path.size();
+        if (buf && cap > 0)
+            std::memcpy(buf, q->path.data(), sizeof(int32_t) * std::min<size_t>(cap, q->path.size()));
+        ddp_query_free(q);
+        return DDP_OK;
+    }
+    if (buf && cap > 0 && l > 0)
+        DDP_CUDA(cudaMemcpy(buf, b->d_paths + (size_t)i * b->path_cap,
+                            sizeof(int32_t) * std::min(cap, l), cudaMemcpyDeviceToHost));
+    return DDP_OK;
+}
+
+int ddp_batch_stats(ddp_batch *b, int64_t *stats, int64_t *t_start_ns, int64_t *t_end_ns) {
+    if (!b) return fail(DDP_ERR_INVALID, "null batch");
+    const size_t n = (size_t)b->last_n;
+    DDP_CUDA(cudaStreamSynchronize(b->stream));
+    if (stats && n)
+        DDP_CUDA(cudaMemcpy(stats, b->d_stats, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost));
+    if (t_start_ns && n)
+        DDP_CUDA(cudaMemcpy(t_start_ns, b->d_t0, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+    if (t_end_ns && n)
+        DDP_CUDA(cudaMemcpy(t_end_ns, b->d_t1, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+    return DDP_OK;
+}
+
+int ddp_batch_launches(const ddp_batch *b, int32_t *launches) {
+    if (!b || !launches) return fail(DDP_ERR_INVALID, "null argument");
+    *launches = b->launches;
+    return DDP_OK;
+}
+
+int ddp_batch_free(ddp_batch *b) {
+    if (!b) return DDP_OK;
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    slots_free(b->sa);
+    cudaFree(b->d_S);
+    cudaFree(b->d_T);
+    cudaFree(b->d_cost);
+    cudaFree(b->d_plen);
+    cudaFree(b->d_paths);
+    cudaFree(b->d_qstatus);
+    cudaFree(b->d_stats);
+    cudaFree(b->d_t0);
+    cudaFree(b->d_t1);
+    cudaFree(b->d_work);
+    if (b->stream && !b->o.stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return DDP_OK;
+}
+
+}  // extern "C"

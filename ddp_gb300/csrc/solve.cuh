@@ -1,0 +1,40 @@
+// Slot arrays and kernel argument blocks of the search kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace ddp {
+
+struct SearchCtl;
+
+// Memory of `nslots` independent search slots (one per concurrent query).
+struct SlotArrays {
+    int32_t n = 0;
+    int nslots = 0;
+    int64_t cap_q = 0, cap_f = 0;
+    unsigned long long *state = nullptr;  // nslots x n
+    int32_t *touched = nullptr;           // nslots x n
+    uint32_t *hops = nullptr;             // nslots x n (per-target heuristic) or null
+    uint2 *q = nullptr;                   // nslots x 2 x cap_q
+    uint2 *f = nullptr;                   // nslots x 2 x cap_f
+    SearchCtl *ctl = nullptr;             // nslots
+};
+
+struct BatchArgs {
+    const int32_t *S, *T;
+    int32_t nq;
+    int32_t *cost, *plen, *paths;
+    int32_t path_cap;
+    int32_t *qstatus;
+    long long *stats, *tstart, *tend;
+    int *work, *status;
+    uint32_t delta;
+    int32_t K;
+};
+
+size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops);
+int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, bool hops,
+                cudaStream_t st);
+void slots_free(SlotArrays &sa);
+
+}  // namespace ddp

@@ -1,0 +1,181 @@
+/*
+ * ddp_gb300 — GA* and dynamic A* on int32 CSR graphs, GB300 (sm_103a).
+ *
+ * C-ABI boundary.  Plain pointers and sizes, opaque handles, integer status
+ * codes; no C++ or torch types cross it.  Each entry point names the
+ * reference interface (lkoshale/DDP, LIB/include and the standalone
+ * programs) that it replaces.
+ *
+ * Conventions shared by every entry point:
+ *   - Graphs are directed, node ids 0..n-1, arc weights uint32 (the
+ *     reference's `unsigned int` weights), costs int32 with DDP_INF
+ *     (= INT_MAX) for "unreachable", as the reference's Cx array.
+ *   - A cost is f(t) = g(t) + h(t), the value the reference reports as
+ *     Cx[target] (LIB/include/a_star.h:239-245, GA_star/A_star_cpu.cpp:191).
+ *     With the heuristics built here h(t) = 0, so the cost is the path weight.
+ *   - Offsets may be given in the reference's layout (n entries, the last
+ *     row ends at e) or with a sentinel (n+1 entries); both are accepted.
+ *   - Host arrays passed in are copied before the call returns; the caller
+ *     keeps ownership.  Handles own their device memory.
+ *   - Calls on one handle are serialised by the handle; different handles
+ *     may be used from different threads.
+ *   - On failure a call returns a non-zero DDP_ERR_* code and
+ *     ddp_last_error() describes it (per calling thread).  Nothing calls
+ *     exit(): the reference's gpuErrchk -> exit(code)
+ *     (LIB/include/utils.cuh:10-18) becomes a returned status.
+ */
+#ifndef DDP_GB300_H
+#define DDP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DDP_INF 2147483647
+
+enum ddp_status {
+    DDP_OK = 0,
+    DDP_ERR_INVALID = 1,        /* bad argument (range, size, null)            */
+    DDP_ERR_CUDA = 2,           /* CUDA runtime error                          */
+    DDP_ERR_IO = 3,             /* file missing / malformed                    */
+    DDP_ERR_OOM = 4,            /* device or host allocation failed            */
+    DDP_ERR_QUEUE_OVERFLOW = 5, /* a search queue outgrew its capacity         */
+    DDP_ERR_TIMEOUT = 6,        /* a bounded device-side wait gave up          */
+    DDP_ERR_NO_DEVICE = 7       /* no usable CUDA device                       */
+};
+
+/* Heuristic kinds for ddp_heuristic_build. */
+enum ddp_heuristic_kind {
+    DDP_H_ZERO = 0,      /* h = 0 (Dijkstra order)                              */
+    DDP_H_BFS_HOPS = 1,  /* reverse-BFS hop count to the target x min arc
+                            weight (GA_star/bfs_hx.cu on the reverse graph of
+                            DA_star/genOpCSR.cpp); unreachable -> pruned      */
+    DDP_H_MANHATTAN = 2, /* |dx| + |dy| on node coordinates x min arc weight   */
+    DDP_H_USER = 3       /* caller-supplied array (a_star.h:34 set_huiristics) */
+};
+
+typedef struct ddp_graph ddp_graph;         /* device-resident CSR + reverse CSR */
+typedef struct ddp_heuristic ddp_heuristic; /* device-resident h for one target  */
+typedef struct ddp_query ddp_query;         /* result of one single-query solve  */
+typedef struct ddp_batch ddp_batch;         /* multi-query engine (slots)        */
+
+/* Search options (all fields 0 = automatic). */
+typedef struct ddp_opts {
+    int32_t K;         /* nodes expanded per iteration (the reference's K queues);
+                          0 = the whole current bucket                          */
+    int32_t delta;     /* bucket width on f; 0 = chosen from the arc weights    */
+    int32_t block;     /* threads per CTA                                        */
+    int32_t grid;      /* CTAs (single query) or concurrent slots (batch)        */
+    int64_t queue_cap; /* entries per search queue                               */
+    void *stream;      /* cudaStream_t; NULL = the handle's own stream           */
+} ddp_opts;
+
+/* ---- library ----------------------------------------------------------- */
+const char *ddp_last_error(void);
+int ddp_version(void);
+/* Number of CUDA devices visible (0 on a machine without a GPU). */
+int ddp_device_count(void);
+
+/* ---- graph: LIB/include/graph.h:13-43 (Graph<T>), graph.cuh:12-89
+ *      (GPU_Graph<T>::__gpu_alloc H2D copy) ----------------------------- */
+/* n nodes, e arcs; offsets has n (reference layout) or n+1 entries
+ * (offsets_len); cols[e] with col < 0 = absent arc; weights[e]. */
+int ddp_graph_from_csr(int32_t n, int64_t e, const int32_t *offsets, int32_t offsets_len,
+                       const int32_t *cols, const uint32_t *weights, ddp_graph **out);
+/* Reads the reference's graph.txt format ("N E", E cols, N offsets,
+ * E weights; Graph<T>::read_graph, graph.h:93-118) and uploads it. */
+int ddp_graph_load_text(const char *path, ddp_graph **out);
+/* Node coordinates (x,y interleaved, 2n int32) for the Manhattan heuristic. */
+int ddp_graph_set_coords(ddp_graph *g, const int32_t *xy);
+int ddp_graph_info(const ddp_graph *g, int32_t *n, int64_t *e, uint32_t *wmin, uint32_t *wmax);
+/* Copies the current forward CSR back (offsets n+1, cols/weights e). */
+int ddp_graph_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights);
+int ddp_graph_free(ddp_graph *g);
+
+/* ---- heuristic: GA_star/bfs_hx.cu (program), LIB a_star.h:34
+ *      set_huiristics(U*) ------------------------------------------------ */
+/* Builds h for `target` on the device.  user_h (DDP_H_USER only) holds n
+ * values; negative values mean "target unreachable from here".  out_h
+ * (optional, n values) receives h, -1 for nodes that cannot reach target. */
+int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_t *user_h,
+                        int32_t *out_h, ddp_heuristic **out);
+int ddp_heuristic_free(ddp_heuristic *h);
+
+/* ---- single query GA*: LIB a_star.cu:109-303 (GPU_A_Star::get_path) ----- */
+/* h may be NULL (h = 0).  The result handle holds the cost and the path. */
+int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t target,
+              const ddp_opts *opts, ddp_query **out);
+/* Cost of a finished query (DDP_INF when the target is unreachable). */
+int ddp_query_cost(const ddp_query *q, int32_t *cost);
+/* Path source..target (a_star.cu:281-301).  *len = full length (0 when
+ * unreachable); at most cap ids are written. */
+int ddp_path_read(const ddp_query *q, int32_t *buf, int32_t cap, int32_t *len);
+/* Device counters of the query: [0] nodes expanded, [1] arcs scanned,
+ * [2] successful relaxations, [3] search iterations. */
+int ddp_query_stats(const ddp_query *q, int64_t *stats4);
+int ddp_query_free(ddp_query *q);
+
+/* ---- batched multi-query engine (no reference counterpart: the
+ *      reference solves one (s,t) per process, GA_v2.cu:301-305) --------- */
+/* hkind: DDP_H_ZERO, DDP_H_BFS_HOPS (per target, built inside the batch)
+ * or DDP_H_MANHATTAN. */
+int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out);
+/* Solves n queries from host arrays; out_cost[n]; out_path_len[n] optional. */
+int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32_t *targets,
+                    int32_t *out_cost, int32_t *out_path_len);
+/* Same with device pointers and no host synchronisation (stream-ordered on
+ * the batch's stream); d_cost / d_path_len are device arrays of n. */
+int ddp_batch_solve_device(ddp_batch *b, int32_t n, const int32_t *d_sources,
+                           const int32_t *d_targets, int32_t *d_cost, int32_t *d_path_len);
+/* Waits for the batch stream. */
+int ddp_batch_sync(ddp_batch *b);
+/* Path of query i of the last solve (source..target). */
+int ddp_batch_path(ddp_batch *b, int32_t i, int32_t *buf, int32_t cap, int32_t *len);
+/* Per-query device counters of the last solve: stats[4*i + k] as in
+ * ddp_query_stats; start/end (optional) = device timestamps in ns. */
+int ddp_batch_stats(ddp_batch *b, int64_t *stats, int64_t *t_start_ns, int64_t *t_end_ns);
+/* Kernel launches of the last solve (for accounting). */
+int ddp_batch_launches(const ddp_batch *b, int32_t *launches);
+int ddp_batch_free(ddp_batch *b);
+
+/* ---- host-side text I/O in the reference's formats --------------------- */
+/* graph.txt (graph.h:93-118); *off gets n+1 entries.  Free with ddp_free. */
+int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **off,
+                           int32_t **col, uint32_t **w);
+/* Writes the reference layout (n offsets, no sentinel).  off has n+1. */
+int ddp_io_write_graph_text(const char *path, int32_t n, int64_t e, const int32_t *off,
+                            const int32_t *col, const uint32_t *w);
+/* Hx.txt: n whitespace-separated ints (bfs_hx.cu:158-172). */
+int ddp_io_read_ints_text(const char *path, int64_t max, int32_t *out, int64_t *count);
+int ddp_io_write_ints_text(const char *path, int64_t n, const int32_t *vals);
+/* Updates.txt (DA_dyn_cpu.cu:1295-1326): batches of "count" then count
+ * lines "flag u v w".  Arrays are allocated; free with ddp_free. */
+int ddp_io_read_updates_text(const char *path, int32_t *nbatches, int32_t **counts,
+                             int32_t **flag, int32_t **u, int32_t **v, uint32_t **w);
+int ddp_io_write_updates_text(const char *path, int32_t nbatches, const int32_t *counts,
+                              const int32_t *flag, const int32_t *u, const int32_t *v,
+                              const uint32_t *w);
+void ddp_free(void *p);
+
+/* ---- seeded generators (GA_star/GenerateCSR.cpp + randomGraph.py,
+ *      maze/create_maze.cpp, DA_star/genDynamicGraph.cpp) --------------- */
+int ddp_gen_random_chain(int32_t n, int64_t e_total, uint32_t wmin, uint32_t wmax, uint64_t seed,
+                         int32_t *off, int32_t *col, uint32_t *w, int32_t *perm_out);
+int ddp_gen_maze(int32_t rows, int32_t cols, uint32_t wall_permille, uint64_t seed,
+                 int32_t *cell_node, int32_t *n_nodes, int64_t *n_arcs, int32_t *off, int32_t *col,
+                 uint32_t *w, int32_t *xy);
+int ddp_gen_updates(int32_t n, int64_t e, const int32_t *off, const int32_t *col, const uint32_t *w,
+                    const int32_t *protect_next, int32_t nbatches, int32_t per_batch,
+                    int32_t inserts_per_batch, uint32_t wmin, uint32_t wmax, uint64_t seed,
+                    int32_t *flag, int32_t *uu, int32_t *vv, uint32_t *ww);
+int ddp_gen_pairs(int32_t n, const int32_t *off, const int32_t *col, int32_t npairs, int32_t hop_lo,
+                  int32_t hop_hi, int32_t bfs_cap_level, uint64_t seed, int32_t threads, int32_t *S,
+                  int32_t *T, int32_t *want_hops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DDP_GB300_H */
