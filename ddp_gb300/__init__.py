@@ -24,12 +24,14 @@ import numpy as np
 
 from ._lib import DdpError, Opts, check, lib, ptr  # noqa: F401
 
-H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER = 0, 1, 2, 3
+H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED = 0, 1, 2, 3, 4
 INF = 2147483647
+# per-query counters: expanded, scanned, relaxed, phases, bfs_reached, bfs_scanned
+STATS = 6
 
 __all__ = [
     "CSR", "DeviceGraph", "Heuristic", "SolveResult", "BatchEngine", "DdpError", "INF",
-    "H_ZERO", "H_BFS_HOPS", "H_MANHATTAN", "H_USER", "gen_random_chain", "gen_maze",
+    "H_ZERO", "H_BFS_HOPS", "H_MANHATTAN", "H_USER", "H_BFS_CAPPED", "gen_random_chain", "gen_maze",
     "gen_updates", "gen_pairs", "read_graph_text", "write_graph_text", "read_ints_text",
     "write_ints_text", "read_updates_text", "write_updates_text", "Graph", "GPU_Graph",
     "Dynamic_Graph", "GPU_Dynamic_Graph", "A_Star", "GPU_A_Star",
@@ -238,15 +240,17 @@ def write_updates_text(path: str, batches) -> None:
 
 # ---------------------------------------------------------------------------
 # device objects
-def _opts(K=0, delta=0, block=0, grid=0, queue_cap=0) -> Opts:
-    return Opts(int(K), int(delta), int(block), int(grid), int(queue_cap), None)
+def _opts(K=0, delta=0, block=0, grid=0, queue_cap=0, stream=None, group=0) -> Opts:
+    """stream: a cudaStream_t as an int (e.g. torch's stream.cuda_stream);
+    group: CTAs per query slot in the batch engine."""
+    return Opts(int(K), int(delta), int(block), int(grid), int(queue_cap), stream or None, int(group), 0)
 
 
 @dataclass
 class SolveResult:
     cost: int
     path: np.ndarray
-    stats: np.ndarray  # expanded, scanned, relaxed, iterations
+    stats: np.ndarray  # expanded, scanned, relaxed, phases, bfs_reached, bfs_scanned
 
     @property
     def found(self) -> bool:
@@ -334,7 +338,7 @@ class DeviceGraph:
             path = np.empty(ln.value, np.int32)
             if ln.value:
                 check(lib().ddp_path_read(q, ptr(path), ln.value, C.byref(ln)))
-            st = np.empty(4, np.int64)
+            st = np.empty(STATS, np.int64)
             check(lib().ddp_query_stats(q, st.ctypes.data_as(C.POINTER(C.c_int64))))
         finally:
             lib().ddp_query_free(q)
@@ -391,13 +395,19 @@ class BatchEngine:
 
     def stats(self):
         n = self.n_last
-        st = np.empty(4 * n, np.int64)
+        st = np.empty(STATS * n, np.int64)
         t0 = np.empty(n, np.int64)
         t1 = np.empty(n, np.int64)
         P = C.POINTER(C.c_int64)
         check(lib().ddp_batch_stats(self.handle, st.ctypes.data_as(P), t0.ctypes.data_as(P),
                                     t1.ctypes.data_as(P)))
-        return st.reshape(n, 4), t0, t1
+        return st.reshape(n, STATS), t0, t1
+
+    def info(self):
+        sl, cap, blk, grp = C.c_int32(), C.c_int64(), C.c_int32(), C.c_int32()
+        check(lib().ddp_batch_info(self.handle, C.byref(sl), C.byref(cap), C.byref(blk)))
+        check(lib().ddp_batch_group(self.handle, C.byref(grp)))
+        return dict(slots=sl.value, queue_cap=cap.value, block=blk.value, group=grp.value)
 
     def launches(self) -> int:
         x = C.c_int32()

@@ -17,7 +17,7 @@ vp = C.c_void_p
 
 class Opts(C.Structure):
     _fields_ = [("K", C.c_int32), ("delta", C.c_int32), ("block", C.c_int32), ("grid", C.c_int32),
-                ("queue_cap", C.c_int64), ("stream", C.c_void_p)]
+                ("queue_cap", C.c_int64), ("stream", C.c_void_p), ("group", C.c_int32), ("reserved", C.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -44,6 +44,8 @@ SIGNATURES = {
     "ddp_batch_sync": (C.c_int, [vp]),
     "ddp_batch_path": (C.c_int, [vp, C.c_int32, i32p, C.c_int32, i32p]),
     "ddp_batch_stats": (C.c_int, [vp, i64p, i64p, i64p]),
+    "ddp_batch_info": (C.c_int, [vp, i32p, i64p, i32p]),
+    "ddp_batch_group": (C.c_int, [vp, i32p]),
     "ddp_batch_launches": (C.c_int, [vp, i32p]),
     "ddp_batch_free": (C.c_int, [vp]),
     "ddp_io_read_graph_text": (C.c_int, [C.c_char_p, i32p, i64p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(u32p)]),

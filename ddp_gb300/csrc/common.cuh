@@ -73,17 +73,17 @@ struct GridBarrier {
     unsigned int *gen;    // generation counter
 };
 
-// Barrier over all CTAs of a cooperative launch (co-residency guaranteed by
-// cudaLaunchCooperativeKernel).  Bounded: returns false after SPIN_LIMIT
-// polls and sets ST_TIMEOUT in *status.
-__device__ __forceinline__ void grid_sync(const GridBarrier &b, int *status) {
+// Barrier over `nblocks` CTAs of a cooperative launch (co-residency
+// guaranteed by cudaLaunchCooperativeKernel).  Bounded: gives up after
+// SPIN_LIMIT polls and sets ST_TIMEOUT in *status.
+__device__ __forceinline__ void grid_sync(const GridBarrier &b, unsigned int nblocks, int *status) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int *vgen = b.gen;
         unsigned int g = *vgen;
         __threadfence();
         unsigned int arrived = atomicAdd(b.count, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == nblocks - 1) {
             *b.count = 0;
             __threadfence();
             atomicAdd(b.gen, 1u);

@@ -51,6 +51,10 @@ struct SearchCtl {
     int iters;            // phases run
     int pad;
     unsigned long long expanded, scanned, relaxed, pad2;
+    unsigned long long bfs_reached, bfs_scanned;  // heuristic BFS work
+    unsigned int tag;     // hop-array tag of the current query (batch)
+    unsigned int hcap;    // hop cap of the last BFS
+    int cur_q;            // query the slot is working on (batch)
     unsigned int bar_count, bar_gen;  // grid barrier (single-query form)
 };
 
@@ -82,7 +86,19 @@ struct GridGroup {
     __device__ int size() const { return gridDim.x * blockDim.x; }
     __device__ int warp() const { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
     __device__ int nwarps() const { return (gridDim.x * blockDim.x) >> 5; }
-    __device__ void sync() const { grid_sync(bar, status); }
+    __device__ void sync() const { grid_sync(bar, gridDim.x, status); }
+};
+
+// G consecutive CTAs of a cooperative launch working on one query.
+struct SubGridGroup {
+    GridBarrier bar;
+    int *status;
+    int G;
+    __device__ int rank() const { return (blockIdx.x % G) * blockDim.x + threadIdx.x; }
+    __device__ int size() const { return G * blockDim.x; }
+    __device__ int warp() const { return rank() >> 5; }
+    __device__ int nwarps() const { return size() >> 5; }
+    __device__ void sync() const { grid_sync(bar, (unsigned)G, status); }
 };
 
 // ---- heuristics (h(v) as uint32, INF_G = "cannot reach the target") -------
@@ -93,10 +109,15 @@ struct HeurZero {
 struct HeurHops {  // reverse-BFS hop count x scale (GA_star/bfs_hx.cu)
     const uint32_t *hops;
     uint32_t scale;
+    uint32_t cap;  // hops assumed for unreached nodes (HOPS_INF = cannot reach t)
+    uint32_t tag;  // 0: plain levels; else epoch-tagged words (run_bfs_hops)
     __device__ uint32_t operator()(int32_t v) const {
-        uint32_t x = __ldcg(hops + v);
-        if (x == HOPS_INF) return INF_G;
-        unsigned long long p = (unsigned long long)x * scale;
+        const uint32_t x = __ldcg(hops + v);
+        uint32_t hv;
+        if (tag) hv = ((x & 0xFFFFFF00u) == tag) ? (x & 0xFFu) : cap;
+        else hv = (x == HOPS_INF) ? cap : x;
+        if (hv == HOPS_INF) return INF_G;
+        unsigned long long p = (unsigned long long)hv * scale;
         return p >= INF_G ? INF_G : (uint32_t)p;
     }
 };
@@ -231,6 +252,10 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     uint32_t T = sat_add(hs, P.delta);
     uint32_t Tsplit = T;
     bool splitting = false;
+    // compaction: a split pass at the current T that only drops stale and
+    // pruned far entries, run when the far pile fills up between splits
+    bool compacting = false;
+    int64_t far_after_compact = 0;
     unsigned long long n_exp = 0, n_scan = 0, n_rel = 0;
     int it = 0;
     int status = 0;
@@ -333,7 +358,10 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                 __syncwarp();
             }
         } else {
-            // split the far pile at Tsplit
+            // split the far pile at Tsplit (or compact it at T)
+            const uint32_t thr = compacting ? T : Tsplit;
+            uint2 *dst = compacting ? qnxt : qcur;
+            const int64_t dbase = compacting ? nnext : 0;
             unsigned int local_min = 0xFFFFFFFFu;
             for (int64_t base = (int64_t)grp.warp() * 32; base < nfar;
                  base += (int64_t)grp.nwarps() * 32) {
@@ -346,7 +374,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     if (st_g(sv) == en.y) {
                         uint64_t f = (uint64_t)en.y + H((int)en.x);
                         if (f < ft) {
-                            if (f < Tsplit) {
+                            if (f < thr) {
                                 to_near = true;
                             } else {
                                 keep = true;
@@ -357,7 +385,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                 }
                 int slot = warp_append(to_near, &ctl->nq[PH]);
                 if (slot >= 0) {
-                    if (slot < B.cap_q) qcur[slot] = en;
+                    if (dbase + slot < B.cap_q) dst[dbase + slot] = en;
                     else raise_err(ctl, PH, ST_OVERFLOW);
                 }
                 slot = warp_append(keep, &ctl->fq[PH]);
@@ -387,7 +415,16 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             if (grp.rank() == 0) atomicOr(&ctl->status, ST_TIMEOUT);
             break;
         }
-        if (!splitting) {
+        if (compacting) {
+            uint2 *t2 = fcur;
+            fcur = falt;
+            falt = t2;
+            nfar = b;
+            nnext += a;
+            far_after_compact = nfar;
+            compacting = false;
+            splitting = false;
+        } else if (!splitting) {
             nnext += a;
             nfar += b;
             head = end;
@@ -402,6 +439,10 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     splitting = true;
                     Tsplit = sat_add(T, P.delta);
                 }
+            }
+            if (!splitting && nfar > B.cap_f / 2 && nfar - far_after_compact > B.cap_f / 8) {
+                compacting = true;
+                splitting = true;  // the split code path runs the compaction
             }
         } else {
             uint2 *t2 = fcur;
@@ -451,9 +492,19 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
 // Replaces GA_star/bfs_hx.cu: the level loop runs on the device (no per-level
 // D2H of the frontier size), frontier expansion is warp-cooperative over
 // reverse-CSR rows, and each node is claimed once with a CAS.
+//
+// tag == 0: hops[] is first filled with HOPS_INF and then holds plain levels.
+// tag != 0: hops[] is not cleared; a word is valid for this run when its high
+//   24 bits equal tag >> 8, its low 8 bits hold the level (so levels stop at
+//   254).  This lets a batch slot reuse the array per query without a fill.
+// budget > 0: the BFS stops after the first level at which it has reached
+//   `budget` nodes.  Returns the cap for unreached nodes in hop units:
+//   HOPS_INF when the BFS ran to completion (unreached = cannot reach t),
+//   else L+1 with L the last level claimed (unreached nodes are at least
+//   L+1 hops away), so min(hops, cap) x wmin stays admissible and consistent.
 template <class Grp>
-__device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &B, int32_t t,
-                             WarpRows *wrows) {
+__device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &B, int32_t t,
+                                 WarpRows *wrows, uint32_t tag, int64_t budget) {
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     WarpRows &wr = wrows[threadIdx.x >> 5];
@@ -461,25 +512,36 @@ __device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &
     int *fa = reinterpret_cast<int *>(B.q0);
     int *fb = reinterpret_cast<int *>(B.q1);
     const int64_t capf = B.cap_q * 2;  // uint2 slots reused as ints
+    const uint32_t max_lvl = tag ? 254u : 0xFFFFFFF0u;
 
-    for (int64_t i = grp.rank(); i < G.n; i += grp.size()) B.hops[i] = HOPS_INF;
+    if (!tag)
+        for (int64_t i = grp.rank(); i < G.n; i += grp.size()) B.hops[i] = HOPS_INF;
     if (grp.rank() == 0) {
         for (int i = 0; i < 4; i++) {
             ctl->nq[i] = 0;
             ctl->err[i] = 0;
         }
+        ctl->bfs_scanned = 0;
+        ctl->bfs_reached = 0;
     }
     grp.sync();
     if (grp.rank() == 0) {
-        B.hops[t] = 0;
+        B.hops[t] = tag;  // level 0
         fa[0] = t;
     }
     grp.sync();
     int64_t nf = 1;
     uint32_t lvl = 0;
     int it = 0;
+    unsigned long long b_reached = 1, b_scanned = 0;
+    bool complete = true;
     while (nf > 0) {
+        if (lvl >= max_lvl || (budget > 0 && (int64_t)b_reached >= budget)) {
+            complete = false;
+            break;
+        }
         const int PH = (it + 1) & 3, RS = (it + 3) & 3;
+        const uint32_t claim_val = tag | (lvl + 1);
         for (int64_t base = (int64_t)grp.warp() * 32; base < nf; base += (int64_t)grp.nwarps() * 32) {
             const int64_t idx = base + lane;
             int rb = 0, bdeg = 0, drb = 0, deg = 0;
@@ -500,6 +562,7 @@ __device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &
             wr.bdeg[lane] = bdeg;
             wr.drb[lane] = drb;
             __syncwarp();
+            if (lane == 0) b_scanned += (unsigned long long)total;
             for (int kb = 0; kb < total; kb += 32) {
                 const int k = kb + lane;
                 bool claim = false;
@@ -507,8 +570,11 @@ __device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &
                 if (k < total) {
                     const int o = row_owner(wr, k);
                     p = (int)row_arc(G, wr, o, k, false).x;
-                    if (p >= 0 && __ldcg(B.hops + p) == HOPS_INF)
-                        claim = atomicCAS(B.hops + p, HOPS_INF, lvl + 1) == HOPS_INF;
+                    if (p >= 0) {
+                        const uint32_t x = __ldcg(B.hops + p);
+                        const bool seen = tag ? ((x & 0xFFFFFF00u) == tag) : (x != HOPS_INF);
+                        if (!seen) claim = atomicCAS(B.hops + p, x, claim_val) == x;
+                    }
                 }
                 int slot = warp_append(claim, &ctl->nq[PH]);
                 if (slot >= 0) {
@@ -524,6 +590,7 @@ __device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &
             ctl->err[RS] = 0;
         }
         nf = *(volatile int *)&ctl->nq[PH];
+        b_reached += (unsigned long long)nf;
         const int perr = *(volatile int *)&ctl->err[PH];
         const int status = *(volatile int *)&ctl->status;
         it++;
@@ -533,7 +600,10 @@ __device__ void run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &
         fb = tmp;
         if ((perr & ST_OVERFLOW) || (status & ST_TIMEOUT)) break;
     }
+    if (lane == 0 && b_scanned) atomicAdd(&ctl->bfs_scanned, b_scanned);
+    if (grp.rank() == 0) ctl->bfs_reached = b_reached;
     grp.sync();
+    return complete ? HOPS_INF : lvl + 1;
 }
 
 // Parent walk t -> s into path[0..cap) in s..t order; returns the length

@@ -44,7 +44,10 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.f, sizeof(uint2) * (size_t)cap_f * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
+    DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
+    DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
     DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * S, st));
+    if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
     DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl) * S, st));
     return DDP_OK;
 }
@@ -56,6 +59,7 @@ void slots_free(SlotArrays &sa) {
     cudaFree(sa.q);
     cudaFree(sa.f);
     cudaFree(sa.ctl);
+    cudaFree(sa.epoch);
     sa = SlotArrays();
 }
 
@@ -92,12 +96,13 @@ __global__ void k_reset_touched(SlotArrays sa) {
 
 // Single-query reverse BFS (heuristic build) over the whole grid.
 __global__ void __launch_bounds__(512) k_bfs_single(DevGraph G, SlotArrays sa, uint32_t *hops,
-                                                    int32_t t) {
+                                                    int32_t t, long long budget) {
     __shared__ WarpRows wrows[MAX_WARPS];
     SlotBufs B = slot_of(sa, 0);
     B.hops = hops;
     GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
-    run_bfs_hops(grp, G, B, t, wrows);
+    const uint32_t cap = run_bfs_hops(grp, G, B, t, wrows, 0u, (int64_t)budget);
+    if (grp.rank() == 0) B.ctl->hcap = cap;
 }
 
 // Single-query GA* over the whole grid (cooperative launch).
@@ -117,74 +122,102 @@ __global__ void __launch_bounds__(512)
     }
 }
 
-// Batched GA*: one CTA per slot, queries claimed from a shared counter so
-// that CTAs finishing short searches take the next query (dynamic load
-// balance over uneven depths).
-template <int HK>
-__global__ void __launch_bounds__(512) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
-    __shared__ WarpRows wrows[MAX_WARPS];
-    __shared__ int sq;
-    SlotBufs B = slot_of(sa, blockIdx.x);
-    CtaGroup grp{&B.ctl->status};
+// Batched GA*: each slot is a group of CTAs (one CTA, or `group` CTAs of a
+// cooperative launch) that claims queries from a shared counter, so groups
+// finishing short searches take the next query (dynamic load balance over
+// uneven depths).  Fewer, wider groups keep fewer per-query state arrays live
+// at once, which lets them stay resident in L2.
+template <int HK, class Grp>
+__device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B, const BatchArgs &A,
+                           uint32_t *epoch, WarpRows *wrows) {
+    SearchCtl *ctl = B.ctl;
+    long long t0 = 0;
     for (;;) {
-        if (threadIdx.x == 0) sq = atomicAdd(A.work, 1);
-        __syncthreads();
-        const int q = sq;
-        __syncthreads();
+        if (grp.rank() == 0) {
+            const int q = atomicAdd(A.work, 1);
+            ctl->cur_q = q;
+            ctl->status = 0;
+            ctl->bfs_reached = 0;
+            ctl->bfs_scanned = 0;
+            if (HK == 1) {
+                // per-query tag: the slot's hop array needs no clearing
+                uint32_t ep = (*epoch + 1) & 0xFFFFFFu;
+                if (ep == 0) ep = 1;  // tag 0 is never used (arrays start zeroed)
+                *epoch = ep;
+                ctl->tag = ep << 8;
+            }
+            t0 = global_ns();
+        }
+        grp.sync();
+        const int q = *(volatile int *)&ctl->cur_q;
         if (q >= A.nq) break;
         const int32_t s = __ldg(A.S + q), t = __ldg(A.T + q);
-        long long t0 = 0;
-        if (threadIdx.x == 0) {
-            t0 = global_ns();
-            B.ctl->status = 0;
-        }
         if (s < 0 || s >= G.n || t < 0 || t >= G.n) {
-            if (threadIdx.x == 0) {
+            if (grp.rank() == 0) {
                 A.cost[q] = DDP_INF;
                 if (A.plen) A.plen[q] = -1;
-                atomicOr(A.status, ST_OVERFLOW << 8);  // "invalid query" bit
+                if (A.qstatus) A.qstatus[q] = -1;
             }
+            grp.sync();
             continue;
         }
-        __syncthreads();
         SearchParams P{s, t, A.delta, A.K};
         SearchResult r;
         if (HK == 1) {
-            run_bfs_hops(grp, G, B, t, wrows);
-            r = run_search(grp, G, B, HeurHops{B.hops, G.wmin}, P, wrows);
+            const uint32_t tag = *(volatile uint32_t *)&ctl->tag;
+            const uint32_t cap = run_bfs_hops(grp, G, B, t, wrows, tag, A.bfs_budget);
+            r = run_search(grp, G, B, HeurHops{B.hops, G.wmin, cap, tag}, P, wrows);
         } else if (HK == 2) {
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
             r = run_search(grp, G, B, HeurManhattan{G.xy, tp.x, tp.y, G.wmin}, P, wrows);
         } else {
             r = run_search(grp, G, B, HeurZero{}, P, wrows);
         }
-        if (threadIdx.x == 0) {
-            const int st = B.ctl->status;
+        if (grp.rank() == 0) {
+            const int st = ctl->status;
             int32_t len = 0;
             if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths)
                 len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
-                                 &B.ctl->status);
+                                 &ctl->status);
             A.cost[q] = (st & (ST_OVERFLOW | ST_TIMEOUT)) ? -1
                         : (r.cost >= INF_G)                ? DDP_INF
                                                            : (int32_t)r.cost;
             if (A.plen) A.plen[q] = len;
-            if (A.qstatus) A.qstatus[q] = B.ctl->status;
+            if (A.qstatus) A.qstatus[q] = ctl->status;
             if (A.stats) {
-                A.stats[4 * (size_t)q + 0] = (long long)B.ctl->expanded;
-                A.stats[4 * (size_t)q + 1] = (long long)B.ctl->scanned;
-                A.stats[4 * (size_t)q + 2] = (long long)B.ctl->relaxed;
-                A.stats[4 * (size_t)q + 3] = (long long)r.iters;
+                long long *st6 = A.stats + DDP_STATS * (size_t)q;
+                st6[0] = (long long)ctl->expanded;
+                st6[1] = (long long)ctl->scanned;
+                st6[2] = (long long)ctl->relaxed;
+                st6[3] = (long long)r.iters;
+                st6[4] = HK == 1 ? (long long)ctl->bfs_reached : 0;
+                st6[5] = HK == 1 ? (long long)ctl->bfs_scanned : 0;
             }
-            atomicOr(A.status, B.ctl->status);
+            atomicOr(A.status, ctl->status);
         }
-        __syncthreads();
-        const int cnt = B.ctl->touched;
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) B.state[B.touched[i]] = ~0ull;
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        grp.sync();
+        const int cnt = *(volatile int *)&ctl->touched;
+        for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
+        grp.sync();
+        if (grp.rank() == 0) {
             if (A.tstart) A.tstart[q] = t0;
             if (A.tend) A.tend[q] = global_ns();
         }
+    }
+}
+
+template <int HK>
+__global__ void __launch_bounds__(512, 2) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
+    __shared__ WarpRows wrows[MAX_WARPS];
+    if (A.group <= 1) {
+        SlotBufs B = slot_of(sa, blockIdx.x);
+        CtaGroup grp{&B.ctl->status};
+        batch_loop<HK>(grp, G, B, A, sa.epoch + blockIdx.x, wrows);
+    } else {
+        const int slot = blockIdx.x / A.group;
+        SlotBufs B = slot_of(sa, slot);
+        SubGridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status, A.group};
+        batch_loop<HK>(grp, G, B, A, sa.epoch + slot, wrows);
     }
 }
 
@@ -210,6 +243,12 @@ template <class K>
 static cudaError_t coop_launch(K kernel, int grid, int block, void **args, cudaStream_t st) {
     return cudaLaunchCooperativeKernel((const void *)kernel, dim3(grid), dim3(block), args, 0, st);
 }
+
+static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CAPPED; }
+
+// Nodes a capped heuristic BFS reaches before it stops (at the end of the
+// level that crosses this count).
+int64_t bfs_budget(int32_t n) { return std::max<int64_t>(4096, (int64_t)n / 32); }
 
 uint32_t auto_delta(const ddp_graph *g) {
     // bucket width ~ a typical arc weight: wide enough for parallel buckets,
@@ -264,12 +303,13 @@ struct ddp_heuristic {
     uint32_t *d_hops = nullptr;  // BFS kind
     int32_t *d_h = nullptr;      // USER kind
     int32_t tx = 0, ty = 0;      // MANHATTAN kind
+    uint32_t cap = HOPS_INF;     // hop cap of a BFS kind (HOPS_INF = exact)
 };
 
 struct ddp_query {
     int32_t cost = DDP_INF;
     std::vector<int32_t> path;
-    int64_t stats[4] = {0, 0, 0, 0};
+    int64_t stats[DDP_STATS] = {0, 0, 0, 0, 0, 0};
 };
 
 extern "C" {
@@ -289,7 +329,8 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
     case DDP_H_ZERO:
         if (out_h) std::fill(out_h, out_h + g->n, 0);
         break;
-    case DDP_H_BFS_HOPS: {
+    case DDP_H_BFS_HOPS:
+    case DDP_H_BFS_CAPPED: {
         int rc = workspace_ensure(g, (int64_t)g->n + 1024);
         if (rc) {
             delete h;
@@ -304,7 +345,8 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
         SlotArrays sa = g->ws->sa;
         DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl), g->stream));
         int grid = coop_grid(k_bfs_single, 512, 0);
-        void *args[] = {&G, &sa, &h->d_hops, &target};
+        long long budget = kind == DDP_H_BFS_CAPPED ? (long long)bfs_budget(g->n) : 0;
+        void *args[] = {&G, &sa, &h->d_hops, &target, &budget};
         e = coop_launch(k_bfs_single, grid, 512, args, g->stream);
         if (e != cudaSuccess) {
             cudaFree(h->d_hops);
@@ -320,10 +362,14 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
             return fail(ctl.status & ST_TIMEOUT ? DDP_ERR_TIMEOUT : DDP_ERR_QUEUE_OVERFLOW,
                         "heuristic BFS did not complete");
         }
+        h->cap = ctl.hcap;
         if (out_h) {
             std::vector<uint32_t> hops((size_t)g->n);
             DDP_CUDA(cudaMemcpy(hops.data(), h->d_hops, sizeof(uint32_t) * (size_t)g->n,
                                 cudaMemcpyDeviceToHost));
+            for (int32_t i = 0; i < g->n; i++) {
+                if (hops[(size_t)i] == HOPS_INF) hops[(size_t)i] = h->cap;
+            }
             for (int32_t i = 0; i < g->n; i++)
                 out_h[i] = hops[(size_t)i] == HOPS_INF ? -1
                                                         : (int32_t)std::min<uint64_t>(
@@ -402,8 +448,8 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
         DDP_CUDA(cudaMemsetAsync(w->sa.ctl, 0, sizeof(SearchCtl), st));
         cudaError_t e;
         const int kind = h ? h->kind : DDP_H_ZERO;
-        if (kind == DDP_H_BFS_HOPS) {
-            HeurHops H{h->d_hops, g->wmin};
+        if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) {
+            HeurHops H{h->d_hops, g->wmin, h->cap, 0u};
             int grid = coop_grid(k_solve_single<HeurHops>, block, o.grid);
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurHops>, grid, block, args, st);
@@ -443,6 +489,8 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
         q->stats[1] = (int64_t)ctl.scanned;
         q->stats[2] = (int64_t)ctl.relaxed;
         q->stats[3] = res[3];
+        q->stats[4] = 0;
+        q->stats[5] = 0;
         if (res[1] > 0) {
             q->path.resize((size_t)res[1]);
             cudaError_t ce = cudaMemcpy(q->path.data(), w->d_path, sizeof(int32_t) * (size_t)res[1],
@@ -472,9 +520,9 @@ int ddp_path_read(const ddp_query *q, int32_t *buf, int32_t cap, int32_t *len) {
     return DDP_OK;
 }
 
-int ddp_query_stats(const ddp_query *q, int64_t *stats4) {
-    if (!q || !stats4) return fail(DDP_ERR_INVALID, "null argument");
-    for (int i = 0; i < 4; i++) stats4[i] = q->stats[i];
+int ddp_query_stats(const ddp_query *q, int64_t *stats) {
+    if (!q || !stats) return fail(DDP_ERR_INVALID, "null argument");
+    for (int i = 0; i < DDP_STATS; i++) stats[i] = q->stats[i];
     return DDP_OK;
 }
 
@@ -502,6 +550,8 @@ struct ddp_batch {
     int32_t path_cap = 0;
     int32_t last_n = 0;
     int32_t launches = 0;
+    int group = 1;  // CTAs per query slot
+    bool no_graph = false;
     // CUDA graph of the last device-pointer solve
     cudaGraphExec_t gexec = nullptr;
     const void *gkey[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -530,7 +580,7 @@ static int batch_grow(ddp_batch *b, int32_t n) {
     DDP_CUDA(cudaMalloc(&b->d_plen, sizeof(int32_t) * N));
     DDP_CUDA(cudaMalloc(&b->d_paths, sizeof(int32_t) * N * (size_t)b->path_cap));
     DDP_CUDA(cudaMalloc(&b->d_qstatus, sizeof(int32_t) * N));
-    DDP_CUDA(cudaMalloc(&b->d_stats, sizeof(long long) * 4 * N));
+    DDP_CUDA(cudaMalloc(&b->d_stats, sizeof(long long) * DDP_STATS * N));
     DDP_CUDA(cudaMalloc(&b->d_t0, sizeof(long long) * N));
     DDP_CUDA(cudaMalloc(&b->d_t1, sizeof(long long) * N));
     b->cap_q_n = n;
@@ -554,15 +604,24 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     A.work = b->d_work;
     A.status = b->d_status;
     A.delta = b->o.delta > 0 ? (uint32_t)b->o.delta : auto_delta(b->g);
+    A.bfs_budget = b->hkind == DDP_H_BFS_CAPPED ? bfs_budget(b->g->n) : 0;
     A.K = b->o.K;
+    A.group = b->group;
     DevGraph G = graph_view(b->g);
     cudaError_t e = cudaMemsetAsync(b->d_work, 0, sizeof(int) * 2, b->stream);
     if (e != cudaSuccess) return e;
-    const int grid = b->sa.nslots;
-    if (b->hkind == DDP_H_BFS_HOPS) k_batch<1><<<grid, b->block, 0, b->stream>>>(G, b->sa, A);
-    else if (b->hkind == DDP_H_MANHATTAN) k_batch<2><<<grid, b->block, 0, b->stream>>>(G, b->sa, A);
-    else k_batch<0><<<grid, b->block, 0, b->stream>>>(G, b->sa, A);
-    return cudaGetLastError();
+    // fresh control blocks (barrier counters included) for every launch
+    e = cudaMemsetAsync(b->sa.ctl, 0, sizeof(SearchCtl) * (size_t)b->sa.nslots, b->stream);
+    if (e != cudaSuccess) return e;
+    const int grid = b->sa.nslots * b->group;
+    SlotArrays sa = b->sa;
+    void *args[] = {&G, &sa, &A};
+    const void *fn = is_bfs_kind(b->hkind)           ? (const void *)k_batch<1>
+                     : (b->hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
+                                                     : (const void *)k_batch<0>;
+    if (b->group > 1)
+        return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
+    return cudaLaunchKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
 }
 
 }  // namespace ddp
@@ -572,8 +631,8 @@ extern "C" {
 int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out) {
     if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS && hkind != DDP_H_MANHATTAN)
-        return fail(DDP_ERR_INVALID, "batch heuristic must be ZERO, BFS_HOPS or MANHATTAN");
+    if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN)
+        return fail(DDP_ERR_INVALID, "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED or MANHATTAN");
     if (hkind == DDP_H_MANHATTAN && !g->d_xy)
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_batch *b = new ddp_batch();
@@ -590,21 +649,24 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     }
     // slots: occupancy-limited, then memory-limited (half of free memory)
     int per_sm = 0;
-    if (hkind == DDP_H_BFS_HOPS)
+    if (is_bfs_kind(hkind))
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, b->block, 0);
     else if (hkind == DDP_H_MANHATTAN)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, b->block, 0);
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<0>, b->block, 0);
-    int nslots = std::max(1, per_sm) * sm_count();
-    if (b->o.grid > 0) nslots = b->o.grid;
-    const int64_t cap = b->o.queue_cap > 0 ? b->o.queue_cap : (int64_t)g->n / 2 + 4096;
+    b->group = std::max(1, b->o.group);
+    const int coresident = std::max(1, per_sm) * sm_count();
+    if (b->group > coresident) b->group = coresident;
+    int nslots = coresident / b->group;
+    if (b->o.grid > 0) nslots = std::min(b->o.grid, b->group > 1 ? nslots : b->o.grid);
+    const int64_t cap = b->o.queue_cap > 0 ? b->o.queue_cap : (int64_t)g->n + 4096;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    const size_t per = slot_bytes(g->n, cap, cap, hkind == DDP_H_BFS_HOPS);
+    const size_t per = slot_bytes(g->n, cap, cap, is_bfs_kind(hkind));
     const size_t budget = freeb / 2;
     if ((size_t)nslots * per > budget) nslots = (int)std::max<size_t>(1, budget / per);
-    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap, hkind == DDP_H_BFS_HOPS, b->stream);
+    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap, is_bfs_kind(hkind), b->stream);
     if (rc == DDP_OK) {
         cudaError_t e1 = cudaMalloc(&b->d_work, sizeof(int) * 2);
         if (e1 != cudaSuccess) rc = cuda_fail(e1, "cudaMalloc(work)");
@@ -629,22 +691,36 @@ int ddp_batch_solve_device(ddp_batch *b, int32_t n, const int32_t *d_sources,
     const void *key[5] = {d_sources, d_targets, d_cost, d_path_len, nullptr};
     bool hit = b->gexec && b->gkey_n == n;
     for (int i = 0; i < 4 && hit; i++) hit = key[i] == b->gkey[i];
+    if (b->no_graph) {
+        // capture was refused once (e.g. a cooperative launch): launch directly
+        cudaError_t e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
+        if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
+        b->overflow_paths.clear();
+        b->last_n = n;
+        b->launches = 1;
+        return DDP_OK;
+    }
     if (!hit) {
         if (b->gexec) {
             cudaGraphExecDestroy(b->gexec);
             b->gexec = nullptr;
         }
-        cudaGraph_t graph;
+        cudaGraph_t graph = nullptr;
         DDP_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
-        if (e != cudaSuccess) return cuda_fail(e, "batch capture");
-        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&b->gexec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) {
+        if (e == cudaSuccess && e2 == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            (void)cudaGetLastError();
             b->gexec = nullptr;
-            return cuda_fail(e, "cudaGraphInstantiate");
+            b->no_graph = true;
+            e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
+            if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
+            b->overflow_paths.clear();
+            b->last_n = n;
+            b->launches = 1;
+            return DDP_OK;
         }
         for (int i = 0; i < 4; i++) b->gkey[i] = key[i];
         b->gkey_n = n;
@@ -694,7 +770,10 @@ int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32
             int rc = ddp_heuristic_build(b->g, targets[i], b->hkind, nullptr, nullptr, &h);
             if (rc) return rc;
             ddp_query *q = nullptr;
-            rc = ddp_solve(b->g, h, sources[i], targets[i], &b->o, &q);
+            ddp_opts so = b->o;
+            so.queue_cap = 0;  // the single-query engine grows its queues itself
+            so.grid = 0;
+            rc = ddp_solve(b->g, h, sources[i], targets[i], &so, &q);
             ddp_heuristic_free(h);
             if (rc) return rc;
             out_cost[i] = q->cost;
@@ -735,7 +814,10 @@ int ddp_batch_path(ddp_batch *b, int32_t i, int32_t *buf, int32_t cap, int32_t *
         int rc = ddp_heuristic_build(b->g, t, b->hkind, nullptr, nullptr, &h);
         if (rc) return rc;
         ddp_query *q = nullptr;
-        rc = ddp_solve(b->g, h, s, t, &b->o, &q);
+        ddp_opts so = b->o;
+        so.queue_cap = 0;
+        so.grid = 0;
+        rc = ddp_solve(b->g, h, s, t, &so, &q);
         ddp_heuristic_free(h);
         if (rc) return rc;
         *len = (int32_t)q->path.size();
@@ -755,11 +837,25 @@ int ddp_batch_stats(ddp_batch *b, int64_t *stats, int64_t *t_start_ns, int64_t *
     const size_t n = (size_t)b->last_n;
     DDP_CUDA(cudaStreamSynchronize(b->stream));
     if (stats && n)
-        DDP_CUDA(cudaMemcpy(stats, b->d_stats, sizeof(long long) * 4 * n, cudaMemcpyDeviceToHost));
+        DDP_CUDA(cudaMemcpy(stats, b->d_stats, sizeof(long long) * DDP_STATS * n, cudaMemcpyDeviceToHost));
     if (t_start_ns && n)
         DDP_CUDA(cudaMemcpy(t_start_ns, b->d_t0, sizeof(long long) * n, cudaMemcpyDeviceToHost));
     if (t_end_ns && n)
         DDP_CUDA(cudaMemcpy(t_end_ns, b->d_t1, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+    return DDP_OK;
+}
+
+int ddp_batch_info(const ddp_batch *b, int32_t *slots, int64_t *queue_cap, int32_t *block) {
+    if (!b) return fail(DDP_ERR_INVALID, "null batch");
+    if (slots) *slots = b->sa.nslots;
+    if (queue_cap) *queue_cap = b->sa.cap_q;
+    if (block) *block = b->block;
+    return DDP_OK;
+}
+
+int ddp_batch_group(const ddp_batch *b, int32_t *group) {
+    if (!b || !group) return fail(DDP_ERR_INVALID, "null argument");
+    *group = b->group;
     return DDP_OK;
 }
 

@@ -18,6 +18,7 @@ struct SlotArrays {
     uint2 *q = nullptr;                   // nslots x 2 x cap_q
     uint2 *f = nullptr;                   // nslots x 2 x cap_f
     SearchCtl *ctl = nullptr;             // nslots
+    uint32_t *epoch = nullptr;            // nslots: per-query tag counter of the hop array
 };
 
 struct BatchArgs {
@@ -30,6 +31,8 @@ struct BatchArgs {
     int *work, *status;
     uint32_t delta;
     int32_t K;
+    int64_t bfs_budget;  // capped heuristic BFS (0 = run to completion)
+    int group;           // CTAs per query slot
 };
 
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops);

@@ -53,7 +53,11 @@ enum ddp_heuristic_kind {
                             weight (GA_star/bfs_hx.cu on the reverse graph of
                             DA_star/genOpCSR.cpp); unreachable -> pruned      */
     DDP_H_MANHATTAN = 2, /* |dx| + |dy| on node coordinates x min arc weight   */
-    DDP_H_USER = 3       /* caller-supplied array (a_star.h:34 set_huiristics) */
+    DDP_H_USER = 3,      /* caller-supplied array (a_star.h:34 set_huiristics) */
+    DDP_H_BFS_CAPPED = 4 /* DDP_H_BFS_HOPS with the BFS stopped after the level
+                            where it has reached max(4096, n/32) nodes; nodes
+                            not reached get (last level + 1) x min weight,
+                            which stays admissible and consistent            */
 };
 
 typedef struct ddp_graph ddp_graph;         /* device-resident CSR + reverse CSR */
@@ -70,6 +74,8 @@ typedef struct ddp_opts {
     int32_t grid;      /* CTAs (single query) or concurrent slots (batch)        */
     int64_t queue_cap; /* entries per search queue                               */
     void *stream;      /* cudaStream_t; NULL = the handle's own stream           */
+    int32_t group;     /* batch: CTAs working on one query (1 = one CTA)          */
+    int32_t reserved;
 } ddp_opts;
 
 /* ---- library ----------------------------------------------------------- */
@@ -112,15 +118,20 @@ int ddp_query_cost(const ddp_query *q, int32_t *cost);
 /* Path source..target (a_star.cu:281-301).  *len = full length (0 when
  * unreachable); at most cap ids are written. */
 int ddp_path_read(const ddp_query *q, int32_t *buf, int32_t cap, int32_t *len);
-/* Device counters of the query: [0] nodes expanded, [1] arcs scanned,
- * [2] successful relaxations, [3] search iterations. */
-int ddp_query_stats(const ddp_query *q, int64_t *stats4);
+/* Device counters of a query, DDP_STATS values: [0] nodes expanded,
+ * [1] arcs scanned, [2] successful relaxations, [3] search phases,
+ * [4] nodes reached by the heuristic BFS, [5] reverse arcs it scanned
+ * (4 and 5 are filled when the heuristic BFS runs inside a batch). */
+#define DDP_STATS 6
+int ddp_query_stats(const ddp_query *q, int64_t *stats);
 int ddp_query_free(ddp_query *q);
 
 /* ---- batched multi-query engine (no reference counterpart: the
  *      reference solves one (s,t) per process, GA_v2.cu:301-305) --------- */
-/* hkind: DDP_H_ZERO, DDP_H_BFS_HOPS (per target, built inside the batch)
- * or DDP_H_MANHATTAN. */
+/* hkind: DDP_H_ZERO, DDP_H_BFS_HOPS / DDP_H_BFS_CAPPED (per target, built
+ * inside the batch kernel) or DDP_H_MANHATTAN.  A query whose search outgrew
+ * its slot's queues reports cost -1 from ddp_batch_solve_device;
+ * ddp_batch_solve re-runs such queries on the single-query engine. */
 int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out);
 /* Solves n queries from host arrays; out_cost[n]; out_path_len[n] optional. */
 int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32_t *targets,
@@ -133,9 +144,14 @@ int ddp_batch_solve_device(ddp_batch *b, int32_t n, const int32_t *d_sources,
 int ddp_batch_sync(ddp_batch *b);
 /* Path of query i of the last solve (source..target). */
 int ddp_batch_path(ddp_batch *b, int32_t i, int32_t *buf, int32_t cap, int32_t *len);
-/* Per-query device counters of the last solve: stats[4*i + k] as in
- * ddp_query_stats; start/end (optional) = device timestamps in ns. */
+/* Per-query device counters of the last solve: stats[DDP_STATS*i + k] as
+ * in ddp_query_stats; start/end (optional) = device timestamps in ns. */
 int ddp_batch_stats(ddp_batch *b, int64_t *stats, int64_t *t_start_ns, int64_t *t_end_ns);
+/* Engine shape: concurrent query slots, queue capacity per slot, threads
+ * per CTA. */
+int ddp_batch_info(const ddp_batch *b, int32_t *slots, int64_t *queue_cap, int32_t *block);
+/* CTAs per query slot of the batch engine. */
+int ddp_batch_group(const ddp_batch *b, int32_t *group);
 /* Kernel launches of the last solve (for accounting). */
 int ddp_batch_launches(const ddp_batch *b, int32_t *launches);
 int ddp_batch_free(ddp_batch *b);

@@ -230,3 +230,45 @@ def test_config1_full_size(gpu, oracle):
     assert r.cost == _oracle_cost(oracle, gs, hh, s, t)
     ok, why = oracle.check_path(g.off, g.col, g.w, r.path, s, t, r.cost)
     assert ok, why
+
+
+def test_capped_bfs_heuristic(gpu, oracle):
+    """DDP_H_BFS_CAPPED: exact hops up to the cap, cap elsewhere; costs stay
+    exact (single query and batch)."""
+    d = gpu
+    g = d.gen_random_chain(200000, 8, 1, 100, 91).with_sentinel()
+    dg = d.DeviceGraph.from_csr(g)
+    S, T, _ = d.gen_pairs(d.CSR(g.n, g.off, g.col, g.w), 24, 4, 400, 15)
+    be = d.BatchEngine(dg, d.H_BFS_CAPPED, grid=24)
+    cost, _ = be.solve(S, T)
+    for i in range(len(S)):
+        s, t = int(S[i]), int(T[i])
+        href = oracle.bfs_heuristic(g.n, g.off[:-1], g.col, g.w, t)
+        h = dg.heuristic(t, d.H_BFS_CAPPED, want_values=True)
+        # capped values never exceed the exact hops (admissible)
+        reach = href >= 0
+        assert (h.values[reach] <= href[reach]).all()
+        assert (h.values[reach] >= np.minimum(href[reach], h.values[reach].max())).all()
+        want = _oracle_cost(oracle, g, href, s, t)
+        assert dg.solve(s, t, h).cost == want
+        assert cost[i] == want
+        h.close()
+    be.close()
+
+
+@pytest.mark.parametrize("group", [2, 7])
+def test_batch_multi_cta_groups(gpu, oracle, group):
+    """Slots made of several cooperative CTAs give the same exact costs."""
+    d = gpu
+    g = d.gen_random_chain(50000, 8, 1, 100, 123).with_sentinel()
+    dg = d.DeviceGraph.from_csr(g)
+    S, T, _ = d.gen_pairs(d.CSR(g.n, g.off, g.col, g.w), 40, 4, 400, 8)
+    be = d.BatchEngine(dg, d.H_BFS_CAPPED, group=group)
+    assert be.info()["group"] == group
+    cost, plen = be.solve(S, T)
+    for i in range(len(S)):
+        href = oracle.bfs_heuristic(g.n, g.off[:-1], g.col, g.w, int(T[i]))
+        assert cost[i] == _oracle_cost(oracle, g, href, int(S[i]), int(T[i])), i
+        ok, why = oracle.check_path(g.off, g.col, g.w, be.path(i), int(S[i]), int(T[i]), int(cost[i]))
+        assert ok, why
+    be.close()
