@@ -60,7 +60,7 @@ def args_parse():
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--delta", type=int, default=0)
     p.add_argument("--K", type=int, default=0)
-    p.add_argument("--group", type=int, default=1, help="CTAs per query slot")
+    p.add_argument("--group", type=int, default=19, help="CTAs per query slot")
     p.add_argument("--heuristic", default="capped", choices=["capped", "bfs", "zero"],
                    help="capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
                         "get last level + 1); bfs: full reverse BFS; zero: h = 0")
@@ -349,7 +349,8 @@ def main():
                      "kernel": "k_batch<1>", "algorithmic_bytes_per_launch": alg,
                      "kernel_ms": 1000 * kernel_s},
         "work_per_query": {"phases_mean": float(st[:, 3].mean()), "expanded_mean": float(st[:, 0].mean()), "arcs_scanned_mean": float(st[:, 1].mean()),
-                           "relaxed_mean": float(st[:, 2].mean()), "bfs_reached_mean": float(st[:, 4].mean())},
+                           "relaxed_mean": float(st[:, 2].mean()), "bfs_reached_mean": float(st[:, 4].mean()),
+                           "far_scanned_mean": float(st[:, 6].mean()), "touched_mean": float(st[:, 7].mean())},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(S.nbytes + T.nbytes),
                 "d2h_bytes_per_step": int(2 * 4 * pairs), "exact_vs_device_run": exact_vs_batch},

@@ -26,8 +26,9 @@ from ._lib import DdpError, Opts, check, lib, ptr  # noqa: F401
 
 H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED = 0, 1, 2, 3, 4
 INF = 2147483647
-# per-query counters: expanded, scanned, relaxed, phases, bfs_reached, bfs_scanned
-STATS = 6
+# per-query counters: expanded, scanned, relaxed, phases, bfs_reached,
+# bfs_scanned, far_scanned, touched
+STATS = 8
 
 __all__ = [
     "CSR", "DeviceGraph", "Heuristic", "SolveResult", "BatchEngine", "DdpError", "INF",

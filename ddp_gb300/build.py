@@ -24,6 +24,8 @@ LIB = os.path.join(PKG, "libddp_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
+# extra nvcc flags for tuning builds, e.g. DDP_NVCC_EXTRA="-DDDP_ARCS=2"
+NVCC_FLAGS += os.environ.get("DDP_NVCC_EXTRA", "").split()
 CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-Wall", "-pthread", "-I" + INCLUDE, "-I" + CSRC]
 
 

@@ -46,12 +46,14 @@ struct SearchCtl {
     int fq[4];            // pushes into far this phase
     unsigned int mf[4];   // min f kept in far during a split phase
     int err[4];           // ST_* raised during the phase (read after its barrier)
+    int ck[4];            // chunks of 32 entries claimed so far in the phase
     int touched;          // nodes whose state left the initial value
     int status;           // ST_* bits
     int iters;            // phases run
     int pad;
     unsigned long long expanded, scanned, relaxed, pad2;
     unsigned long long bfs_reached, bfs_scanned;  // heuristic BFS work
+    unsigned long long far_scanned;               // far entries read by splits
     unsigned int tag;     // hop-array tag of the current query (batch)
     unsigned int hcap;    // hop cap of the last BFS
     int cur_q;            // query the slot is working on (batch)
@@ -169,6 +171,14 @@ __device__ __forceinline__ int warp_excl_scan(int x, int *total) {
     return v - x;
 }
 
+// Claims the next chunk of a phase for this warp (dynamic balance: warps
+// that finish early take more chunks).  Returns the chunk index.
+__device__ __forceinline__ int64_t claim_chunk(int *counter) {
+    int c = 0;
+    if ((threadIdx.x & 31) == 0) c = atomicAdd(counter, 1);
+    return (int64_t)__shfl_sync(0xffffffffu, c, 0);
+}
+
 // Records an error for phase `ph` (consistent control flow after the
 // barrier) and in the sticky status word (reporting).
 __device__ __forceinline__ void raise_err(SearchCtl *ctl, int ph, int bit) {
@@ -181,7 +191,10 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
     return c < a ? 0xFFFFFFFFu : c;
 }
 
-// Per-warp staging of 32 popped rows (shared memory).
+// Per-warp shared memory: staging of 32 popped rows, and staging buffers
+// for queue pushes (flushed with one atomic per >= 32 entries, so the L2
+// round trip of a queue reservation is paid once per flush instead of once
+// per 32 arcs, and the stores are coalesced).
 struct WarpRows {
     int excl[32];
     int rb[32];      // first arc of the base row
@@ -189,7 +202,41 @@ struct WarpRows {
     int drb[32];     // first arc of the diff row
     uint32_t g[32];
     int u[32];
+    uint2 sn[64];    // staged near/next pushes
+    uint2 sf[64];    // staged far pushes
+    int st[64];      // staged first touches / BFS frontier pushes
 };
+
+// Copies a warp's staged entries to dst[base + reserved ..] (all lanes).
+template <class T>
+__device__ __forceinline__ void stage_flush(T *buf, int &cnt, int *counter, T *dst, int64_t base,
+                                            int64_t cap, SearchCtl *ctl, int ph);
+
+template <class T>
+__device__ __forceinline__ void stage_push(bool pred, T val, T *buf, int &cnt, int *counter, T *dst,
+                                           int64_t base, int64_t cap, SearchCtl *ctl, int ph) {
+    const unsigned m = __ballot_sync(FULL, pred);
+    if (pred) buf[cnt + __popc(m & ((1u << (threadIdx.x & 31)) - 1u))] = val;
+    cnt += __popc(m);
+    if (cnt >= 32) stage_flush(buf, cnt, counter, dst, base, cap, ctl, ph);
+}
+
+template <class T>
+__device__ __forceinline__ void stage_flush(T *buf, int &cnt, int *counter, T *dst, int64_t base,
+                                            int64_t cap, SearchCtl *ctl, int ph) {
+    if (cnt == 0) return;  // warp-uniform
+    __syncwarp();
+    int b = 0;
+    if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, cnt);
+    b = __shfl_sync(FULL, b, 0);
+    for (int i = threadIdx.x & 31; i < cnt; i += 32) {
+        const int64_t pos = base + b + i;
+        if (pos < cap) dst[pos] = buf[i];
+        else raise_err(ctl, ph, ST_OVERFLOW);
+    }
+    __syncwarp();
+    cnt = 0;
+}
 
 __device__ __forceinline__ int row_owner(const WarpRows &wr, int k) {
     int o = 0;
@@ -235,10 +282,12 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             ctl->fq[i] = 0;
             ctl->mf[i] = 0xFFFFFFFFu;
             ctl->err[i] = 0;
+            ctl->ck[i] = 0;
         }
         ctl->touched = 1;
         ctl->iters = 0;
         ctl->expanded = ctl->scanned = ctl->relaxed = 0;
+        ctl->far_scanned = 0;
         B.state[P.s] = st_make(0, -1);
         B.touched[0] = P.s;
         B.q0[0] = make_uint2((uint32_t)P.s, 0u);
@@ -271,29 +320,34 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
         int64_t end = 0;
         if (!splitting) {
             end = (P.K > 0) ? min(nnear, head + (int64_t)P.K) : nnear;
-            for (int64_t base = head + (int64_t)grp.warp() * 32; base < end;
-                 base += (int64_t)grp.nwarps() * 32) {
+            int c_n = 0, c_f = 0, c_t = 0;  // staged pushes of this warp
+            // chunk claims are prefetched one ahead to hide their round trip
+            int64_t cnext = claim_chunk(&ctl->ck[PH]);
+            for (int64_t base = head + 32 * cnext; base < end; base = head + 32 * cnext) {
+                cnext = claim_chunk(&ctl->ck[PH]);
                 const int64_t idx = base + lane;
                 int u = -1, rb = 0, bdeg = 0, drb = 0, deg = 0;
                 uint32_t gu = 0;
                 if (idx < end) {
-                    uint2 en = __ldcg(qcur + idx);
+                    const uint2 en = __ldcg(qcur + idx);
                     u = (int)en.x;
                     gu = en.y;
-                    uint64_t su = __ldcg(B.state + u);
-                    if (st_g(su) == gu && u != P.t) {
-                        uint32_t hu = H(u);
-                        uint64_t fu = (uint64_t)gu + hu;
-                        if (fu < ft) {
-                            rb = __ldg(G.off + u);
-                            bdeg = __ldg(G.off + u + 1) - rb;
-                            deg = bdeg;
-                            if (has_diff) {
-                                drb = __ldcg(G.doff + u);
-                                deg += __ldcg(G.doff + u + 1) - drb;
-                            }
-                            n_exp++;
-                        }
+                    // independent loads issued together (speculatively for
+                    // entries that turn out stale)
+                    const uint64_t su = __ldcg(B.state + u);
+                    const uint32_t hu = H(u);
+                    const int r0 = __ldg(G.off + u), r1 = __ldg(G.off + u + 1);
+                    int d0 = 0, d1 = 0;
+                    if (has_diff) {
+                        d0 = __ldcg(G.doff + u);
+                        d1 = __ldcg(G.doff + u + 1);
+                    }
+                    if (st_g(su) == gu && u != P.t && (uint64_t)gu + hu < ft) {
+                        rb = r0;
+                        bdeg = r1 - r0;
+                        drb = d0;
+                        deg = bdeg + (d1 - d0);
+                        n_exp++;
                     }
                 }
                 int total;
@@ -306,65 +360,87 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                 wr.u[lane] = u;
                 __syncwarp();
                 n_scan += (lane == 0) ? (unsigned long long)total : 0ull;
-                for (int kb = 0; kb < total; kb += 32) {
-                    const int k = kb + lane;
-                    bool to_near = false, to_far = false, first = false;
-                    int v = 0;
-                    uint32_t ng = 0;
-                    if (k < total) {
-                        const int o = row_owner(wr, k);
-                        const uint2 a = row_arc(G, wr, o, k, true);
-                        v = (int)a.x;
-                        const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
-                        if (v >= 0 && ng64 < INF_G) {
-                            ng = (uint32_t)ng64;
-                            uint64_t sv = __ldcg(B.state + v);
-                            if (ng < st_g(sv)) {
-                                const uint32_t hv = H(v);
-                                const uint64_t fv = (uint64_t)ng + hv;
-                                if (fv < ft) {
-                                    const uint64_t nv = st_make(ng, wr.u[o]);
-                                    for (;;) {
-                                        uint64_t prev = atomicCAS(B.state + v, sv, nv);
-                                        if (prev == sv) {
-                                            first = st_g(sv) >= INF_G;
-                                            if (fv < T) to_near = true;
-                                            else to_far = true;
-                                            break;
-                                        }
-                                        sv = prev;
-                                        if (ng >= st_g(sv)) break;
-                                    }
-                                }
-                            }
+                // ARCS arcs per lane per step; every stage issues all of its
+                // loads / atomics before consuming any result
+#ifndef DDP_ARCS
+#define DDP_ARCS 2
+#endif
+                constexpr int ARCS = DDP_ARCS;
+                for (int kb = 0; kb < total; kb += 32 * ARCS) {
+                    int v[ARCS], o[ARCS];
+                    uint32_t ng[ARCS], hv[ARCS];
+                    uint64_t sv[ARCS], prev[ARCS];
+                    bool live[ARCS], go[ARCS];
+#pragma unroll
+                    for (int r = 0; r < ARCS; r++) {
+                        const int k = kb + 32 * r + lane;
+                        live[r] = false;
+                        v[r] = 0;
+                        ng[r] = 0;
+                        o[r] = 0;
+                        if (k < total) {
+                            o[r] = row_owner(wr, k);
+                            const uint2 a = row_arc(G, wr, o[r], k, true);
+                            v[r] = (int)a.x;
+                            const uint64_t ng64 = (uint64_t)wr.g[o[r]] + a.y;
+                            live[r] = v[r] >= 0 && ng64 < INF_G;
+                            ng[r] = (uint32_t)ng64;
                         }
                     }
-                    if (to_near || to_far) n_rel++;
-                    int slot = warp_append(to_near, &ctl->nq[PH]);
-                    if (slot >= 0) {
-                        int64_t pos = nnext + slot;
-                        if (pos < B.cap_q) qnxt[pos] = make_uint2((uint32_t)v, ng);
-                        else raise_err(ctl, PH, ST_OVERFLOW);
+#pragma unroll
+                    for (int r = 0; r < ARCS; r++) sv[r] = live[r] ? __ldcg(B.state + v[r]) : 0ull;
+#pragma unroll
+                    for (int r = 0; r < ARCS; r++) {
+                        live[r] = live[r] && ng[r] < st_g(sv[r]);
+                        hv[r] = live[r] ? H(v[r]) : 0u;
                     }
-                    slot = warp_append(to_far, &ctl->fq[PH]);
-                    if (slot >= 0) {
-                        int64_t pos = nfar + slot;
-                        if (pos < B.cap_f) fcur[pos] = make_uint2((uint32_t)v, ng);
-                        else raise_err(ctl, PH, ST_OVERFLOW);
+#pragma unroll
+                    for (int r = 0; r < ARCS; r++) {
+                        go[r] = live[r] && (uint64_t)ng[r] + hv[r] < ft;
+                        prev[r] = go[r] ? atomicCAS(B.state + v[r], sv[r], st_make(ng[r], wr.u[o[r]])) : sv[r];
                     }
-                    slot = warp_append(first, &ctl->touched);
-                    if (slot >= 0) B.touched[slot] = v;  // at most n first touches
+#pragma unroll
+                    for (int r = 0; r < ARCS; r++) {
+                        bool to_near = false, to_far = false, first = false;
+                        if (go[r]) {
+                            uint64_t cur = sv[r];
+                            uint64_t got = prev[r];
+                            // retry only when another relaxation got in between
+                            while (got != cur) {
+                                cur = got;
+                                if (ng[r] >= st_g(cur)) break;
+                                got = atomicCAS(B.state + v[r], cur, st_make(ng[r], wr.u[o[r]]));
+                            }
+                            if (got == cur) {
+                                first = st_g(cur) >= INF_G;
+                                const uint64_t fv = (uint64_t)ng[r] + hv[r];
+                                if (fv < T) to_near = true;
+                                else to_far = true;
+                            }
+                        }
+                        if (to_near || to_far) n_rel++;
+                        const uint2 en = make_uint2((uint32_t)v[r], ng[r]);
+                        stage_push(to_near, en, wr.sn, c_n, &ctl->nq[PH], qnxt, nnext, B.cap_q, ctl, PH);
+                        stage_push(to_far, en, wr.sf, c_f, &ctl->fq[PH], fcur, nfar, B.cap_f, ctl, PH);
+                        // at most n first touches: the touched log never overflows
+                        stage_push(first, v[r], wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, PH);
+                    }
                 }
                 __syncwarp();
             }
+            stage_flush(wr.sn, c_n, &ctl->nq[PH], qnxt, nnext, B.cap_q, ctl, PH);
+            stage_flush(wr.sf, c_f, &ctl->fq[PH], fcur, nfar, B.cap_f, ctl, PH);
+            stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, PH);
         } else {
             // split the far pile at Tsplit (or compact it at T)
             const uint32_t thr = compacting ? T : Tsplit;
+            if (grp.rank() == 0) ctl->far_scanned += (unsigned long long)nfar;
             uint2 *dst = compacting ? qnxt : qcur;
             const int64_t dbase = compacting ? nnext : 0;
             unsigned int local_min = 0xFFFFFFFFu;
-            for (int64_t base = (int64_t)grp.warp() * 32; base < nfar;
-                 base += (int64_t)grp.nwarps() * 32) {
+            int c_n = 0, c_f = 0;
+            for (int64_t base = 32 * claim_chunk(&ctl->ck[PH]); base < nfar;
+                 base = 32 * claim_chunk(&ctl->ck[PH])) {
                 const int64_t idx = base + lane;
                 bool to_near = false, keep = false;
                 uint2 en = make_uint2(0u, 0u);
@@ -383,14 +459,12 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                         }
                     }
                 }
-                int slot = warp_append(to_near, &ctl->nq[PH]);
-                if (slot >= 0) {
-                    if (dbase + slot < B.cap_q) dst[dbase + slot] = en;
-                    else raise_err(ctl, PH, ST_OVERFLOW);
-                }
-                slot = warp_append(keep, &ctl->fq[PH]);
-                if (slot >= 0) falt[slot] = en;  // compaction never grows the pile
+                stage_push(to_near, en, wr.sn, c_n, &ctl->nq[PH], dst, dbase, B.cap_q, ctl, PH);
+                // compaction never grows the pile
+                stage_push(keep, en, wr.sf, c_f, &ctl->fq[PH], falt, 0, B.cap_f, ctl, PH);
             }
+            stage_flush(wr.sn, c_n, &ctl->nq[PH], dst, dbase, B.cap_q, ctl, PH);
+            stage_flush(wr.sf, c_f, &ctl->fq[PH], falt, 0, B.cap_f, ctl, PH);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) local_min = min(local_min, __shfl_xor_sync(FULL, local_min, o));
             if (lane == 0 && local_min != 0xFFFFFFFFu) atomicMin(&ctl->mf[PH], local_min);
@@ -402,6 +476,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             ctl->fq[RS] = 0;
             ctl->mf[RS] = 0xFFFFFFFFu;
             ctl->err[RS] = 0;
+            ctl->ck[RS] = 0;
         }
         const int a = *(volatile int *)&ctl->nq[PH];
         const int b = *(volatile int *)&ctl->fq[PH];
@@ -520,6 +595,7 @@ __device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBu
         for (int i = 0; i < 4; i++) {
             ctl->nq[i] = 0;
             ctl->err[i] = 0;
+            ctl->ck[i] = 0;
         }
         ctl->bfs_scanned = 0;
         ctl->bfs_reached = 0;
@@ -542,7 +618,8 @@ __device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBu
         }
         const int PH = (it + 1) & 3, RS = (it + 3) & 3;
         const uint32_t claim_val = tag | (lvl + 1);
-        for (int64_t base = (int64_t)grp.warp() * 32; base < nf; base += (int64_t)grp.nwarps() * 32) {
+        int c_b = 0;
+        for (int64_t base = 32 * claim_chunk(&ctl->ck[PH]); base < nf; base = 32 * claim_chunk(&ctl->ck[PH])) {
             const int64_t idx = base + lane;
             int rb = 0, bdeg = 0, drb = 0, deg = 0;
             if (idx < nf) {
@@ -576,18 +653,16 @@ __device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBu
                         if (!seen) claim = atomicCAS(B.hops + p, x, claim_val) == x;
                     }
                 }
-                int slot = warp_append(claim, &ctl->nq[PH]);
-                if (slot >= 0) {
-                    if (slot < capf) fb[slot] = p;
-                    else raise_err(ctl, PH, ST_OVERFLOW);
-                }
+                stage_push(claim, p, wr.st, c_b, &ctl->nq[PH], fb, 0, capf, ctl, PH);
             }
             __syncwarp();
         }
+        stage_flush(wr.st, c_b, &ctl->nq[PH], fb, 0, capf, ctl, PH);
         grp.sync();
         if (grp.rank() == 0) {
             ctl->nq[RS] = 0;
             ctl->err[RS] = 0;
+            ctl->ck[RS] = 0;
         }
         nf = *(volatile int *)&ctl->nq[PH];
         b_reached += (unsigned long long)nf;

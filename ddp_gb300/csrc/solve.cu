@@ -16,7 +16,7 @@
 
 namespace ddp {
 
-constexpr int MAX_WARPS = 32;
+constexpr int MAX_WARPS = 16;  // blocks of at most 512 threads
 
 // ---- slot arrays -------------------------------------------------------------
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops) {
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(512) k_bfs_single(DevGraph G, SlotArrays sa, u
 
 // Single-query GA* over the whole grid (cooperative launch).
 template <class Heur>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, 2)
     k_solve_single(DevGraph G, SlotArrays sa, Heur H, SearchParams P, int32_t *out, int32_t *path,
                    int32_t path_cap) {
     __shared__ WarpRows wrows[MAX_WARPS];
@@ -192,6 +192,8 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
                 st6[3] = (long long)r.iters;
                 st6[4] = HK == 1 ? (long long)ctl->bfs_reached : 0;
                 st6[5] = HK == 1 ? (long long)ctl->bfs_scanned : 0;
+                st6[6] = (long long)ctl->far_scanned;
+                st6[7] = (long long)ctl->touched;
             }
             atomicOr(A.status, ctl->status);
         }
@@ -253,7 +255,7 @@ int64_t bfs_budget(int32_t n) { return std::max<int64_t>(4096, (int64_t)n / 32);
 uint32_t auto_delta(const ddp_graph *g) {
     // bucket width ~ a typical arc weight: wide enough for parallel buckets,
     // narrow enough to keep re-expansions rare
-    uint32_t d = (g->wmin + g->wmax) / 2;
+    uint32_t d = (g->wmin + g->wmax) / 4;
     return d < 1 ? 1 : d;
 }
 
@@ -309,7 +311,7 @@ struct ddp_heuristic {
 struct ddp_query {
     int32_t cost = DDP_INF;
     std::vector<int32_t> path;
-    int64_t stats[DDP_STATS] = {0, 0, 0, 0, 0, 0};
+    int64_t stats[DDP_STATS] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 extern "C" {
@@ -491,6 +493,8 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
         q->stats[3] = res[3];
         q->stats[4] = 0;
         q->stats[5] = 0;
+        q->stats[6] = (int64_t)ctl.far_scanned;
+        q->stats[7] = (int64_t)ctl.touched;
         if (res[1] > 0) {
             q->path.resize((size_t)res[1]);
             cudaError_t ce = cudaMemcpy(q->path.data(), w->d_path, sizeof(int32_t) * (size_t)res[1],
@@ -663,10 +667,13 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     const int64_t cap = b->o.queue_cap > 0 ? b->o.queue_cap : (int64_t)g->n + 4096;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    const size_t per = slot_bytes(g->n, cap, cap, is_bfs_kind(hkind));
+    // the far pile holds every open node beyond the current bucket: twice the
+    // node count leaves room for stale copies between compactions
+    const int64_t cap_f = b->o.queue_cap > 0 ? b->o.queue_cap : 2 * (int64_t)g->n + 4096;
+    const size_t per = slot_bytes(g->n, cap, cap_f, is_bfs_kind(hkind));
     const size_t budget = freeb / 2;
     if ((size_t)nslots * per > budget) nslots = (int)std::max<size_t>(1, budget / per);
-    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap, is_bfs_kind(hkind), b->stream);
+    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap_f, is_bfs_kind(hkind), b->stream);
     if (rc == DDP_OK) {
         cudaError_t e1 = cudaMalloc(&b->d_work, sizeof(int) * 2);
         if (e1 != cudaSuccess) rc = cuda_fail(e1, "cudaMalloc(work)");

@@ -121,8 +121,10 @@ int ddp_path_read(const ddp_query *q, int32_t *buf, int32_t cap, int32_t *len);
 /* Device counters of a query, DDP_STATS values: [0] nodes expanded,
  * [1] arcs scanned, [2] successful relaxations, [3] search phases,
  * [4] nodes reached by the heuristic BFS, [5] reverse arcs it scanned
- * (4 and 5 are filled when the heuristic BFS runs inside a batch). */
-#define DDP_STATS 6
+ * (4 and 5 are filled when the heuristic BFS runs inside a batch),
+ * [6] open-list entries re-read by bucket splits, [7] distinct nodes
+ * reached. */
+#define DDP_STATS 8
 int ddp_query_stats(const ddp_query *q, int64_t *stats);
 int ddp_query_free(ddp_query *q);
 
