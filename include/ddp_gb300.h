@@ -158,6 +158,26 @@ int ddp_batch_group(const ddp_batch *b, int32_t *group);
 int ddp_batch_launches(const ddp_batch *b, int32_t *launches);
 int ddp_batch_free(ddp_batch *b);
 
+/* ---- reverse-BFS hop counts without device allocation ------------------
+ * No counterpart in the reference.  For callers that cannot let a library
+ * call cudaMalloc (for example a service that gives all device memory to its
+ * own pool at start-up, or one that must not fail on a late allocation while
+ * serving): every input and output is a device array the caller owns, and
+ * the scratch this kernel needs lives in a fixed array inside the library
+ * (about 8 MiB, held on every GPU that loads the library until exit).
+ *   d_rev_offsets: n+1 int32, reverse CSR offsets (row v = arcs into v)
+ *   d_rev_sources: int32 sources of those arcs (negative = absent arc)
+ *   d_hops: n int32 out, hops from v to target, -1 when target is
+ *           unreachable (the Hx.txt convention of GA_star/bfs_hx.cu)
+ * n is limited to DDP_NOALLOC_MAX_NODES; larger graphs are rejected with
+ * DDP_ERR_INVALID.  The first call on a device looks up the scratch address
+ * (make it before any stream capture).  The call is synchronous on `stream`
+ * (NULL = default stream).  All calls share the one scratch array: calls that
+ * overlap on the GPU race, so serialise them. */
+#define DDP_NOALLOC_MAX_NODES 1048576
+int ddp_bfs_hops_noalloc(int32_t n, const int32_t *d_rev_offsets, const int32_t *d_rev_sources,
+                         int32_t target, int32_t *d_hops, void *stream);
+
 /* ---- host-side text I/O in the reference's formats --------------------- */
 /* graph.txt (graph.h:93-118); *off gets n+1 entries.  Free with ddp_free. */
 int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **off,
