@@ -35,7 +35,7 @@ __all__ = [
     "H_ZERO", "H_BFS_HOPS", "H_MANHATTAN", "H_USER", "H_BFS_CAPPED", "gen_random_chain", "gen_maze",
     "gen_updates", "gen_pairs", "read_graph_text", "write_graph_text", "read_ints_text",
     "write_ints_text", "read_updates_text", "write_updates_text", "Graph", "GPU_Graph",
-    "Dynamic_Graph", "GPU_Dynamic_Graph", "A_Star", "GPU_A_Star",
+    "Dynamic_Graph", "GPU_Dynamic_Graph", "A_Star", "GPU_A_Star", "DynamicSearch",
 ]
 
 
@@ -418,6 +418,58 @@ class BatchEngine:
     def close(self):
         if self.handle:
             lib().ddp_batch_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DynamicSearch:
+    """A resident A* search that follows edge-update batches (ddp_dyn):
+    replaces DA_star/DA_dyn_cpu.cu.  The graph switches to growable rows."""
+
+    def __init__(self, graph: DeviceGraph, source: int, target: int, hkind: int = H_BFS_HOPS, **opts):
+        self.graph = graph
+        o = _opts(**opts)
+        h = C.c_void_p()
+        check(lib().ddp_dyn_create(graph.handle, int(source), int(target), int(hkind), C.byref(o), C.byref(h)))
+        self.handle = h
+
+    @property
+    def cost(self) -> int:
+        c = C.c_int32()
+        check(lib().ddp_dyn_cost(self.handle, C.byref(c)))
+        return c.value
+
+    def update(self, flag, u, v, w) -> int:
+        """One batch: flag 1 insert, 0 delete, 2 set weight.  Returns the cost."""
+        flag, u, v, w = _i32(flag), _i32(u), _i32(v), _u32(w)
+        c = C.c_int32()
+        check(lib().ddp_dyn_update(self.handle, len(flag), ptr(flag), ptr(u), ptr(v), ptr(w, C.c_uint32),
+                                   C.byref(c)))
+        return c.value
+
+    def path(self) -> np.ndarray:
+        ln = C.c_int32()
+        check(lib().ddp_dyn_path(self.handle, None, 0, C.byref(ln)))
+        p = np.empty(ln.value, np.int32)
+        if ln.value:
+            check(lib().ddp_dyn_path(self.handle, ptr(p), ln.value, C.byref(ln)))
+        return p
+
+    def stats(self) -> dict:
+        st = np.empty(10, np.int64)
+        check(lib().ddp_dyn_stats(self.handle, st.ctypes.data_as(C.POINTER(C.c_int64))))
+        keys = ["cost", "path_len", "status", "phases", "invalidated", "reseeded", "relaxed", "hops_lowered",
+                "expanded", "scanned"]
+        return dict(zip(keys, st.tolist()))
+
+    def close(self):
+        if self.handle:
+            lib().ddp_dyn_free(self.handle)
             self.handle = None
 
     def __del__(self):

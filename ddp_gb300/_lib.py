@@ -48,6 +48,12 @@ SIGNATURES = {
     "ddp_batch_group": (C.c_int, [vp, i32p]),
     "ddp_batch_launches": (C.c_int, [vp, i32p]),
     "ddp_batch_free": (C.c_int, [vp]),
+    "ddp_dyn_create": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(Opts), C.POINTER(vp)]),
+    "ddp_dyn_update": (C.c_int, [vp, C.c_int32, i32p, i32p, i32p, u32p, i32p]),
+    "ddp_dyn_cost": (C.c_int, [vp, i32p]),
+    "ddp_dyn_path": (C.c_int, [vp, i32p, C.c_int32, i32p]),
+    "ddp_dyn_stats": (C.c_int, [vp, i64p]),
+    "ddp_dyn_free": (C.c_int, [vp]),
     "ddp_bfs_hops_noalloc": (C.c_int, [C.c_int32, vp, vp, C.c_int32, vp, vp]),
     "ddp_io_read_graph_text": (C.c_int, [C.c_char_p, i32p, i64p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(u32p)]),
     "ddp_io_write_graph_text": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, i32p, i32p, u32p]),

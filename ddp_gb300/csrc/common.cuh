@@ -60,7 +60,20 @@ struct DevGraph {
     const uint2 *darc;
     const int32_t *droff; // n+1
     const uint2 *drarc;
+    // Dynamic graphs keep explicit row ends (rows grow in place and move to
+    // the end of the arc array when full): row u = [off[u], oend[u]).
+    // Null for static graphs, where row u ends at off[u+1].
+    const int32_t *oend;
+    const int32_t *roend;
 };
+
+__device__ __forceinline__ int row_end(const int32_t *off, const int32_t *oend, int u) {
+    return oend ? __ldcg(oend + u) : __ldg(off + u + 1);
+}
+
+__device__ __forceinline__ int row_begin(const int32_t *off, const int32_t *oend, int u) {
+    return oend ? __ldcg(off + u) : __ldg(off + u);
+}
 
 // ---- bounded-wait barriers -------------------------------------------------
 // Spin limit for every device-side wait: ~2^22 polls with backoff (seconds),

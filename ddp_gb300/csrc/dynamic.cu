@@ -1,0 +1,774 @@
+// Dynamic A*: edge insert / delete / weight-change batches with incremental
+// repair of a resident search.
+//
+// Replaces DA_star/DA_dyn_cpu.cu (lkoshale/DDP): per batch the reference
+// builds a diff CSR on the host (insertDiff/createDiffGraph :1928-2005),
+// propagates inserts over all N nodes (propogateAdd :488-556,
+// insert_propagate :558-648), marks deleted arcs on the host
+// (removeDelEdges :2008-2043), re-parents nodes under spin locks with an
+// ancestor walk to refuse cycles (propogateDel :378-486, delete_propagate
+// :650-904), repairs remaining parent cycles on the host between rounds
+// (check_remove_cycle :2138-2254, 4 N-array transfers per round), optionally
+// re-runs GA* (:1642-1793), and folds the diff into a new CSR on the host
+// (mergeDiff :2080-2128).
+//
+// Here, per batch:
+//   host: the batch is resolved on a host mirror of the graph with the
+//         reference's semantics (deletes and weight changes hit the first
+//         live u->v arc of the pre-batch graph; inserts are appended to
+//         their row), and only the touched arc slots / row bounds are
+//         scattered to the device.  Rows carry slack and move to the end of
+//         the arc array when full, so there is no per-batch merge.
+//   device, one cooperative kernel:
+//     A. heuristic repair: an inserted arc can shorten hop distances to the
+//        target; hops are lowered by decrease propagation over the reverse
+//        graph, so h stays admissible and consistent;
+//     B. invalidation: a deleted (or heavier) arc that is the parent arc of
+//        its head invalidates the head's subtree of the shortest-path tree
+//        (found by walking child arcs whose head names the node as parent);
+//     C. re-seeding: every invalidated node takes the best g over its live
+//        in-arcs from valid nodes (reads first, then writes), and is queued;
+//     D. inserted (and lighter) arcs relax their head from a reached tail;
+//     E. the A* resumes from the retained open list (it runs in keep mode:
+//        nodes beyond f(t) stay open), and stops when no open node has
+//        f < f(t).
+// No parent cycles can arise: parents always point to strictly earlier
+// relaxations, and invalidated subtrees are rebuilt from valid nodes only.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "engine.cuh"
+#include "graph.cuh"
+#include "solve.cuh"
+
+enum { UPD_INS = 1, UPD_TREE = 2, UPD_LIGHTER = 3 };
+
+// Host mirror of a dynamic graph: rows with explicit [beg, end) and a
+// capacity, forward and reverse.
+struct DynMirror {
+    int32_t n = 0;
+    std::vector<int32_t> beg, end, cap;
+    std::vector<uint2> arc;
+    std::vector<int32_t> rbeg, rend, rcap;
+    std::vector<uint2> rarc;
+    int64_t tail = 0, rtail = 0;  // first unused slot
+    std::vector<int64_t> dirty_arc, dirty_rarc;
+    std::vector<int32_t> dirty_row, dirty_rrow;
+    bool full = true;  // next upload sends everything
+};
+
+namespace ddp {
+namespace {
+
+// Lays rows out with slack: capacity = used + max(2, used / 4); reserves
+// room for relocations at the end.
+void mirror_layout(const std::vector<int32_t> &used_b, const std::vector<int32_t> &used_e,
+                   const std::vector<uint2> &src, std::vector<int32_t> &beg, std::vector<int32_t> &end,
+                   std::vector<int32_t> &cap, std::vector<uint2> &dst, int64_t &tail) {
+    const size_t n = used_b.size();
+    std::vector<int32_t> nb(n), ne(n), nc(n);
+    int64_t total = 0;
+    for (size_t u = 0; u < n; u++) {
+        int32_t live = 0;
+        for (int32_t j = used_b[u]; j < used_e[u]; j++)
+            if ((int32_t)src[(size_t)j].x >= 0) live++;
+        nc[u] = live + std::max(2, live / 4);
+        total += nc[u];
+    }
+    const int64_t reserve = std::max<int64_t>(1 << 16, total / 4);
+    std::vector<uint2> out((size_t)(total + reserve), make_uint2(0xFFFFFFFFu, 0u));
+    int64_t k = 0;
+    for (size_t u = 0; u < n; u++) {
+        nb[u] = (int32_t)k;
+        int64_t p = k;
+        for (int32_t j = used_b[u]; j < used_e[u]; j++)
+            if ((int32_t)src[(size_t)j].x >= 0) out[(size_t)p++] = src[(size_t)j];
+        ne[u] = (int32_t)p;
+        k += nc[u];
+    }
+    beg.swap(nb);
+    end.swap(ne);
+    cap.swap(nc);
+    dst.swap(out);
+    tail = k;
+}
+
+// Appends an arc to row u; moves the row to the end when it is full.
+// Returns false when the arc array has no room left (caller re-lays out).
+bool mirror_append(std::vector<int32_t> &beg, std::vector<int32_t> &end, std::vector<int32_t> &cap,
+                   std::vector<uint2> &arc, int64_t &tail, int32_t u, uint2 a,
+                   std::vector<int64_t> &dirty, std::vector<int32_t> &drow) {
+    if (end[(size_t)u] - beg[(size_t)u] >= cap[(size_t)u]) {
+        const int32_t used = end[(size_t)u] - beg[(size_t)u];
+        const int32_t ncap = std::max(4, 2 * cap[(size_t)u]);
+        if (tail + ncap > (int64_t)arc.size() || tail + ncap > INT32_MAX) return false;
+        for (int32_t j = 0; j < used; j++) {
+            arc[(size_t)(tail + j)] = arc[(size_t)(beg[(size_t)u] + j)];
+            dirty.push_back(tail + j);
+        }
+        beg[(size_t)u] = (int32_t)tail;
+        end[(size_t)u] = (int32_t)(tail + used);
+        cap[(size_t)u] = ncap;
+        tail += ncap;
+    }
+    const int32_t j = end[(size_t)u]++;
+    arc[(size_t)j] = a;
+    dirty.push_back(j);
+    drow.push_back(u);
+    return true;
+}
+
+__global__ void k_scatter_arcs(uint2 *arc, const long long *slot, const uint2 *val, int m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) arc[slot[i]] = val[i];
+}
+
+__global__ void k_scatter_rows(int32_t *beg, int32_t *end, const int4 *rows, int m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) {
+        int4 r = rows[i];
+        beg[r.x] = r.y;
+        end[r.x] = r.z;
+    }
+}
+
+struct DynArgs {
+    const int4 *upd;  // {kind, u, v, w}
+    int nupd;
+    int32_t *inv;     // invalidated nodes (n)
+    int32_t *out;     // cost, path len, status, phases, invalidated, reseeded, relaxed, hops lowered
+    int32_t *path;
+    int32_t path_cap;
+    int heur;         // 0: h = 0, 1: hops
+    int initial;      // 1: first search from the source (no repair steps)
+};
+
+// Shared counter block for the repair steps (inside SearchCtl's pad space is
+// not enough, so the dynamic kernel keeps its own).
+struct DynCtl {
+    int cnt[4];
+    int inv_n;
+    int far_add;
+    int hops_lowered;
+    int relaxed;
+    int reseeded;
+    int pad[7];
+};
+
+__device__ __forceinline__ SlotBufs slot_of_dyn(const SlotArrays &sa) {
+    SlotBufs b;
+    b.state = sa.state;
+    b.touched = sa.touched;
+    b.hops = sa.hops;
+    b.q0 = sa.q;
+    b.q1 = sa.q + sa.cap_q;
+    b.f0 = sa.f;
+    b.f1 = sa.f + sa.cap_f;
+    b.ctl = sa.ctl;
+    b.cap_q = sa.cap_q;
+    b.cap_f = sa.cap_f;
+    return b;
+}
+
+template <class Grp>
+__device__ void dyn_level_end(const Grp &grp, DynCtl *dc, int it, int &nf) {
+    const int PH = (it + 1) & 3, RS = (it + 3) & 3;
+    grp.sync();
+    if (grp.rank() == 0) dc->cnt[RS] = 0;
+    nf = *(volatile int *)&dc->cnt[PH];
+}
+
+__global__ void __launch_bounds__(512, 2)
+    k_dyn(DevGraph G, SlotArrays sa, uint32_t *hops, SearchParams P, DynArgs A, DynCtl *dc) {
+    __shared__ WarpRows wrows[16];
+    SlotBufs B = slot_of_dyn(sa);
+    GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
+    const int rank = grp.rank(), size = grp.size();
+    const uint32_t scale = G.wmin;
+    int32_t *fa = reinterpret_cast<int32_t *>(B.q0);
+    int32_t *fb = reinterpret_cast<int32_t *>(B.q1);
+    uint2 *far_buf = (*(volatile int *)&B.ctl->far_sel) ? B.f1 : B.f0;
+    const int64_t far_base = *(volatile int *)&B.ctl->far_n;
+
+    if (!A.initial) {
+        int it = 0, nf = 0;
+        // ---- A. heuristic repair: lower hops over inserted arcs ----------
+        if (A.heur == 1) {
+            for (int i = rank; i < A.nupd; i += size) {
+                const int4 up = A.upd[i];
+                if (up.x != UPD_INS) continue;
+                const uint32_t hv = __ldcg(hops + up.z);
+                if (hv == HOPS_INF) continue;
+                const uint32_t old = atomicMin(hops + up.y, hv + 1);
+                if (hv + 1 < old) {
+                    const int s = atomicAdd(&dc->cnt[(it + 1) & 3], 1);
+                    fb[s] = up.y;  // each lowering pushes once; bounded by 2 cap_q
+                    atomicAdd(&dc->hops_lowered, 1);
+                }
+            }
+            dyn_level_end(grp, dc, it, nf);
+            it++;
+            while (nf > 0) {
+                int32_t *t = fa;
+                fa = fb;
+                fb = t;
+                const int PH = (it + 1) & 3;
+                for (int i = rank; i < nf; i += size) {
+                    const int u = __ldcg(fa + i);
+                    const uint32_t hu = __ldcg(hops + u);
+                    const int b = row_begin(G.roff, G.roend, u), e = row_end(G.roff, G.roend, u);
+                    for (int j = b; j < e; j++) {
+                        const int p = (int)__ldcg(G.rarc + j).x;
+                        if (p < 0) continue;
+                        if (hu + 1 < __ldcg(hops + p)) {
+                            const uint32_t old = atomicMin(hops + p, hu + 1);
+                            if (hu + 1 < old) {
+                                const int s = atomicAdd(&dc->cnt[PH], 1);
+                                if (s < 2 * B.cap_q) fb[s] = p;
+                                else atomicOr(&B.ctl->status, ST_OVERFLOW);
+                                atomicAdd(&dc->hops_lowered, 1);
+                            }
+                        }
+                    }
+                }
+                dyn_level_end(grp, dc, it, nf);
+                it++;
+                if (*(volatile int *)&B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) break;
+            }
+        }
+        // ---- B. invalidate subtrees hanging off removed / heavier tree arcs
+        {
+            const int PH = (it + 1) & 3;
+            for (int i = rank; i < A.nupd; i += size) {
+                const int4 up = A.upd[i];
+                if (up.x != UPD_TREE) continue;
+                const uint64_t sv = __ldcg(B.state + up.z);
+                if (st_g(sv) < INF_G && st_parent(sv) == up.y &&
+                    atomicCAS(B.state + up.z, sv, ~0ull) == sv) {
+                    fb[atomicAdd(&dc->cnt[PH], 1)] = up.z;
+                    A.inv[atomicAdd(&dc->inv_n, 1)] = up.z;
+                }
+            }
+            dyn_level_end(grp, dc, it, nf);
+            it++;
+            while (nf > 0) {
+                int32_t *t = fa;
+                fa = fb;
+                fb = t;
+                const int PH2 = (it + 1) & 3;
+                for (int i = rank; i < nf; i += size) {
+                    const int x = __ldcg(fa + i);
+                    const int b = row_begin(G.off, G.oend, x), e = row_end(G.off, G.oend, x);
+                    for (int j = b; j < e; j++) {
+                        const int y = (int)__ldcg(G.arc + j).x;
+                        if (y < 0) continue;
+                        const uint64_t sy = __ldcg(B.state + y);
+                        if (st_g(sy) < INF_G && st_parent(sy) == x && atomicCAS(B.state + y, sy, ~0ull) == sy) {
+                            fb[atomicAdd(&dc->cnt[PH2], 1)] = y;  // each node invalidated once
+                            A.inv[atomicAdd(&dc->inv_n, 1)] = y;
+                        }
+                    }
+                }
+                dyn_level_end(grp, dc, it, nf);
+                it++;
+            }
+        }
+        // ---- C. re-seed invalidated nodes from valid in-neighbours --------
+        const int ninv = *(volatile int *)&dc->inv_n;
+        uint2 *best = B.q1;  // one {g, parent} per invalidated node
+        for (int i = rank; i < ninv; i += size) {
+            const int x = A.inv[i];
+            uint32_t bg = INF_G;
+            int bp = -1;
+            const int b = row_begin(G.roff, G.roend, x), e = row_end(G.roff, G.roend, x);
+            for (int j = b; j < e; j++) {
+                const uint2 a = __ldcg(G.rarc + j);
+                const int p = (int)a.x;
+                if (p < 0) continue;
+                const uint32_t gp = st_g(__ldcg(B.state + p));
+                if (gp >= INF_G) continue;
+                const uint64_t c = (uint64_t)gp + a.y;
+                if (c < bg) {
+                    bg = (uint32_t)c;
+                    bp = p;
+                }
+            }
+            best[i] = make_uint2(bg, (uint32_t)bp);
+        }
+        grp.sync();
+        for (int i = rank; i < ninv; i += size) {
+            const uint2 bv = best[i];
+            if (bv.x >= INF_G) continue;
+            const int x = A.inv[i];
+            B.state[x] = st_make(bv.x, (int32_t)bv.y);
+            const int s = atomicAdd(&dc->far_add, 1);
+            if (far_base + s < B.cap_f) far_buf[far_base + s] = make_uint2((uint32_t)x, bv.x);
+            else atomicOr(&B.ctl->status, ST_OVERFLOW);
+            atomicAdd(&dc->reseeded, 1);
+        }
+        grp.sync();
+        // ---- D. relax heads of inserted / lighter arcs --------------------
+        for (int i = rank; i < A.nupd; i += size) {
+            const int4 up = A.upd[i];
+            if (up.x != UPD_INS && up.x != UPD_LIGHTER) continue;
+            const uint32_t gu = st_g(__ldcg(B.state + up.y));
+            if (gu >= INF_G) continue;
+            const uint64_t ng64 = (uint64_t)gu + (uint32_t)up.w;
+            if (ng64 >= INF_G) continue;
+            const uint32_t ng = (uint32_t)ng64;
+            uint64_t cur = __ldcg(B.state + up.z);
+            while (ng < st_g(cur)) {
+                const uint64_t got = atomicCAS(B.state + up.z, cur, st_make(ng, up.y));
+                if (got == cur) {
+                    const int s = atomicAdd(&dc->far_add, 1);
+                    if (far_base + s < B.cap_f) far_buf[far_base + s] = make_uint2((uint32_t)up.z, ng);
+                    else atomicOr(&B.ctl->status, ST_OVERFLOW);
+                    atomicAdd(&dc->relaxed, 1);
+                    break;
+                }
+                cur = got;
+            }
+        }
+        grp.sync();
+        if (rank == 0) B.ctl->far_n = (int)min((int64_t)B.cap_f, far_base + *(volatile int *)&dc->far_add);
+        grp.sync();
+    }
+    // ---- E. (resume) the A* search ---------------------------------------
+    SearchResult r;
+    if (A.heur == 1) r = run_search(grp, G, B, HeurHops{hops, scale, HOPS_INF, 0u}, P, wrows);
+    else r = run_search(grp, G, B, HeurZero{}, P, wrows);
+    if (rank == 0) {
+        const int st = B.ctl->status;
+        A.out[0] = (st & (ST_OVERFLOW | ST_TIMEOUT)) ? -1 : (r.cost >= INF_G ? DDP_INF : (int32_t)r.cost);
+        A.out[1] = (st & (ST_OVERFLOW | ST_TIMEOUT)) ? 0 : write_path(B, P.s, P.t, A.path, A.path_cap, G.n, &B.ctl->status);
+        A.out[2] = B.ctl->status;
+        A.out[3] = r.iters;
+        A.out[4] = *(volatile int *)&dc->inv_n;
+        A.out[5] = *(volatile int *)&dc->reseeded;
+        A.out[6] = *(volatile int *)&dc->relaxed;
+        A.out[7] = *(volatile int *)&dc->hops_lowered;
+        A.out[8] = (int32_t)min((unsigned long long)INT32_MAX, (unsigned long long)B.ctl->expanded);
+        A.out[9] = (int32_t)min((unsigned long long)INT32_MAX, (unsigned long long)B.ctl->scanned);
+    }
+}
+
+}  // namespace
+}  // namespace ddp
+
+using namespace ddp;
+
+struct ddp_dyn {
+    ddp_graph *g = nullptr;
+    int32_t s = 0, t = 0;
+    int hkind = DDP_H_ZERO;
+    ddp_opts o{};
+    SlotArrays sa;
+    uint32_t *d_hops = nullptr;
+    int32_t *d_inv = nullptr;
+    int32_t *d_out = nullptr;
+    int32_t *d_path = nullptr;
+    DynCtl *d_dc = nullptr;
+    int4 *d_upd = nullptr;
+    int32_t upd_cap = 0;
+    long long *d_slot = nullptr;
+    uint2 *d_val = nullptr;
+    int4 *d_rows = nullptr;
+    int64_t scat_cap = 0, rows_cap = 0;
+    int64_t arc_cap = 0, rarc_cap = 0;  // device capacities
+    int32_t cost = DDP_INF;
+    int32_t path_len = 0;
+    int64_t stats[10] = {0};
+    int grid = 0;
+};
+
+namespace ddp {
+
+static int dyn_upload(ddp_dyn *d) {
+    ddp_graph *g = d->g;
+    DynMirror *m = g->dyn;
+    const int32_t n = g->n;
+    if (m->full) {
+        if ((int64_t)m->arc.size() > d->arc_cap) {
+            cudaFree(g->d_arc);
+            g->d_arc = nullptr;
+            DDP_CUDA(cudaMalloc(&g->d_arc, sizeof(uint2) * m->arc.size()));
+            d->arc_cap = (int64_t)m->arc.size();
+        }
+        if ((int64_t)m->rarc.size() > d->rarc_cap) {
+            cudaFree(g->d_rarc);
+            g->d_rarc = nullptr;
+            DDP_CUDA(cudaMalloc(&g->d_rarc, sizeof(uint2) * m->rarc.size()));
+            d->rarc_cap = (int64_t)m->rarc.size();
+        }
+        DDP_CUDA(cudaMemcpy(g->d_arc, m->arc.data(), sizeof(uint2) * m->arc.size(), cudaMemcpyHostToDevice));
+        DDP_CUDA(cudaMemcpy(g->d_rarc, m->rarc.data(), sizeof(uint2) * m->rarc.size(), cudaMemcpyHostToDevice));
+        DDP_CUDA(cudaMemcpy(g->d_off, m->beg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        DDP_CUDA(cudaMemcpy(g->d_oend, m->end.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        DDP_CUDA(cudaMemcpy(g->d_roff, m->rbeg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        DDP_CUDA(cudaMemcpy(g->d_roend, m->rend.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+        m->full = false;
+        m->dirty_arc.clear();
+        m->dirty_rarc.clear();
+        m->dirty_row.clear();
+        m->dirty_rrow.clear();
+        return DDP_OK;
+    }
+    // scatter the touched slots and row bounds
+    auto scatter = [&](std::vector<int64_t> &dirty, std::vector<uint2> &src, uint2 *dst) -> int {
+        if (dirty.empty()) return DDP_OK;
+        std::sort(dirty.begin(), dirty.end());
+        dirty.erase(std::unique(dirty.begin(), dirty.end()), dirty.end());
+        const int64_t k = (int64_t)dirty.size();
+        if (k > d->scat_cap) {
+            cudaFree(d->d_slot);
+            cudaFree(d->d_val);
+            d->d_slot = nullptr;
+            d->d_val = nullptr;
+            DDP_CUDA(cudaMalloc(&d->d_slot, sizeof(long long) * k));
+            DDP_CUDA(cudaMalloc(&d->d_val, sizeof(uint2) * k));
+            d->scat_cap = k;
+        }
+        std::vector<long long> sl(dirty.begin(), dirty.end());
+        std::vector<uint2> val((size_t)k);
+        for (int64_t i = 0; i < k; i++) val[(size_t)i] = src[(size_t)dirty[(size_t)i]];
+        DDP_CUDA(cudaMemcpyAsync(d->d_slot, sl.data(), sizeof(long long) * k, cudaMemcpyHostToDevice, g->stream));
+        DDP_CUDA(cudaMemcpyAsync(d->d_val, val.data(), sizeof(uint2) * k, cudaMemcpyHostToDevice, g->stream));
+        k_scatter_arcs<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(dst, d->d_slot, d->d_val, (int)k);
+        DDP_CUDA(cudaGetLastError());
+        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        dirty.clear();
+        return DDP_OK;
+    };
+    auto rows = [&](std::vector<int32_t> &drow, std::vector<int32_t> &b, std::vector<int32_t> &e, int32_t *db,
+                    int32_t *de) -> int {
+        if (drow.empty()) return DDP_OK;
+        std::sort(drow.begin(), drow.end());
+        drow.erase(std::unique(drow.begin(), drow.end()), drow.end());
+        const int64_t k = (int64_t)drow.size();
+        if (k > d->rows_cap) {
+            cudaFree(d->d_rows);
+            d->d_rows = nullptr;
+            DDP_CUDA(cudaMalloc(&d->d_rows, sizeof(int4) * k));
+            d->rows_cap = k;
+        }
+        std::vector<int4> r((size_t)k);
+        for (int64_t i = 0; i < k; i++) {
+            const int32_t u = drow[(size_t)i];
+            r[(size_t)i] = make_int4(u, b[(size_t)u], e[(size_t)u], 0);
+        }
+        DDP_CUDA(cudaMemcpyAsync(d->d_rows, r.data(), sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
+        k_scatter_rows<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(db, de, d->d_rows, (int)k);
+        DDP_CUDA(cudaGetLastError());
+        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        drow.clear();
+        return DDP_OK;
+    };
+    int rc = scatter(m->dirty_arc, m->arc, g->d_arc);
+    if (!rc) rc = scatter(m->dirty_rarc, m->rarc, g->d_rarc);
+    if (!rc) rc = rows(m->dirty_row, m->beg, m->end, g->d_off, g->d_oend);
+    if (!rc) rc = rows(m->dirty_rrow, m->rbeg, m->rend, g->d_roff, g->d_roend);
+    return rc;
+}
+
+static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
+    ddp_graph *g = d->g;
+    DevGraph G = graph_view(g);
+    SearchParams P{d->s, d->t, d->o.delta > 0 ? (uint32_t)d->o.delta : std::max(1u, (g->wmin + g->wmax) / 4),
+                   d->o.K, 1, initial ? 0 : 1, 1};
+    DynArgs A;
+    A.upd = d->d_upd;
+    A.nupd = nupd;
+    A.inv = d->d_inv;
+    A.out = d->d_out;
+    A.path = d->d_path;
+    A.path_cap = g->n;
+    A.heur = d->hkind == DDP_H_BFS_HOPS ? 1 : 0;
+    A.initial = initial;
+    // fresh barrier / counters; the far pile position survives in ctl
+    DDP_CUDA(cudaMemsetAsync(d->d_dc, 0, sizeof(DynCtl), g->stream));
+    DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->bar_count, 0, 2 * sizeof(unsigned int), g->stream));
+    DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->status, 0, sizeof(int), g->stream));
+    void *args[] = {&G, &d->sa, &d->d_hops, &P, &A, &d->d_dc};
+    DDP_CUDA(cudaLaunchCooperativeKernel((const void *)k_dyn, dim3(d->grid), dim3(512), args, 0, g->stream));
+    int32_t out[10];
+    DDP_CUDA(cudaMemcpyAsync(out, d->d_out, sizeof(out), cudaMemcpyDeviceToHost, g->stream));
+    DDP_CUDA(cudaStreamSynchronize(g->stream));
+    if (out[2] & ST_TIMEOUT) return fail(DDP_ERR_TIMEOUT, "dynamic search: barrier wait timed out");
+    if (out[2] & ST_OVERFLOW) return fail(DDP_ERR_QUEUE_OVERFLOW, "dynamic search: queue overflow");
+    d->cost = out[0];
+    d->path_len = out[1];
+    for (int i = 0; i < 10; i++) d->stats[i] = out[i];
+    return DDP_OK;
+}
+
+}  // namespace ddp
+
+extern "C" {
+
+int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, const ddp_opts *opts,
+                   ddp_dyn **out) {
+    if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (source < 0 || source >= g->n || target < 0 || target >= g->n)
+        return fail(DDP_ERR_INVALID, "source/target out of range");
+    if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS)
+        return fail(DDP_ERR_INVALID, "dynamic search heuristic must be ZERO or BFS_HOPS");
+    std::lock_guard<std::mutex> lk(g->mu);
+    if (g->dyn_active) return fail(DDP_ERR_INVALID, "graph already has a dynamic search");
+    const int32_t n = g->n;
+    ddp_dyn *d = new ddp_dyn();
+    d->g = g;
+    d->s = source;
+    d->t = target;
+    d->hkind = hkind;
+    if (opts) d->o = *opts;
+    auto bail = [&](int rc) {
+        ddp_dyn_free(d);
+        return rc;
+    };
+    if (g->dyn) {
+        // the graph is already in the dynamic layout (an earlier search)
+        d->arc_cap = g->e;
+        d->rarc_cap = g->e_rev;
+    } else {
+    // host mirror from the device CSR
+    std::vector<int32_t> off((size_t)n + 1), roff((size_t)n + 1);
+    std::vector<uint2> arc((size_t)std::max<int64_t>(g->e, 1)), rarc((size_t)std::max<int64_t>(g->e_rev, 1));
+    DDP_CUDA(cudaMemcpy(off.data(), g->d_off, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(roff.data(), g->d_roff, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost));
+    if (g->e) DDP_CUDA(cudaMemcpy(arc.data(), g->d_arc, sizeof(uint2) * g->e, cudaMemcpyDeviceToHost));
+    if (g->e_rev) DDP_CUDA(cudaMemcpy(rarc.data(), g->d_rarc, sizeof(uint2) * g->e_rev, cudaMemcpyDeviceToHost));
+    DynMirror *m = new DynMirror();
+    m->n = n;
+    std::vector<int32_t> ob(off.begin(), off.end() - 1), oe(off.begin() + 1, off.end());
+    std::vector<int32_t> rb(roff.begin(), roff.end() - 1), re(roff.begin() + 1, roff.end());
+    mirror_layout(ob, oe, arc, m->beg, m->end, m->cap, m->arc, m->tail);
+    mirror_layout(rb, re, rarc, m->rbeg, m->rend, m->rcap, m->rarc, m->rtail);
+    g->dyn = m;
+    g->e = (int64_t)m->arc.size();
+    g->e_rev = (int64_t)m->rarc.size();
+    d->arc_cap = 0;
+    d->rarc_cap = 0;
+    workspace_release(g);  // the single-query workspace was sized for the old arrays
+    cudaError_t e0 = cudaMalloc(&g->d_oend, sizeof(int32_t) * n);
+    if (e0 == cudaSuccess) e0 = cudaMalloc(&g->d_roend, sizeof(int32_t) * n);
+    if (e0 != cudaSuccess) return bail(cuda_fail(e0, "cudaMalloc(row ends)"));
+    int rc0 = dyn_upload(d);
+    if (rc0) return bail(rc0);
+    }
+    g->dyn_active = true;
+    cudaError_t e1;
+    int rc;
+    // one search slot with generous queues (keep mode retains the open list)
+    const int64_t capq = (int64_t)n + 4096, capf = 2 * (int64_t)n + 4096;
+    rc = slots_alloc(d->sa, n, 1, capq, capf, false, g->stream);
+    if (rc) return bail(rc);
+    e1 = cudaMalloc(&d->d_inv, sizeof(int32_t) * n);
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_out, sizeof(int32_t) * 16);
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_path, sizeof(int32_t) * n);
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_dc, sizeof(DynCtl));
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_hops, sizeof(uint32_t) * n);
+    if (e1 != cudaSuccess) return bail(cuda_fail(e1, "cudaMalloc(dynamic state)"));
+    DDP_CUDA(cudaMemsetAsync(d->sa.ctl, 0, sizeof(SearchCtl), g->stream));
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dyn, 512, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    d->grid = std::max(1, per_sm) * std::max(1, sms);
+    if (d->o.grid > 0 && d->o.grid < d->grid) d->grid = d->o.grid;
+    if (hkind == DDP_H_BFS_HOPS) {
+        // exact reverse BFS from the target into the dynamic hop array
+        ddp_heuristic *h = nullptr;
+        g->mu.unlock();
+        rc = ddp_heuristic_build(g, target, DDP_H_BFS_HOPS, nullptr, nullptr, &h);
+        g->mu.lock();
+        if (rc) return bail(rc);
+        cudaError_t ce = cudaMemcpy(d->d_hops, heuristic_hops_ptr(h), sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice);
+        ddp_heuristic_free(h);
+        if (ce != cudaSuccess) return bail(cuda_fail(ce, "hops copy"));
+    }
+    rc = dyn_launch(d, 1, 0);
+    if (rc) return bail(rc);
+    *out = d;
+    return DDP_OK;
+}
+
+int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
+                   const uint32_t *w, int32_t *out_cost) {
+    if (!d || nupd < 0 || (nupd > 0 && (!flag || !u || !v || !w)))
+        return fail(DDP_ERR_INVALID, "bad update arguments");
+    ddp_graph *g = d->g;
+    std::lock_guard<std::mutex> lk(g->mu);
+    DynMirror *m = g->dyn;
+    const int32_t n = g->n;
+    std::vector<int4> ups;
+    ups.reserve((size_t)nupd);
+    // deletes and weight changes resolve against the pre-batch graph
+    // (removeDelEdges runs before mergeDiff, DA_dyn_cpu.cu:1473-1484)
+    for (int32_t i = 0; i < nupd; i++) {
+        if (flag[i] != 0 && flag[i] != 2) continue;
+        const int32_t a = u[i], b = v[i];
+        if (a < 0 || a >= n || b < 0 || b >= n) continue;
+        int32_t jf = -1;
+        for (int32_t j = m->beg[(size_t)a]; j < m->end[(size_t)a]; j++)
+            if ((int32_t)m->arc[(size_t)j].x == b) {
+                jf = j;
+                break;
+            }
+        if (jf < 0) continue;  // no such arc: nothing to do
+        int32_t jr = -1;
+        for (int32_t j = m->rbeg[(size_t)b]; j < m->rend[(size_t)b]; j++)
+            if ((int32_t)m->rarc[(size_t)j].x == a && m->rarc[(size_t)j].y == m->arc[(size_t)jf].y) {
+                jr = j;
+                break;
+            }
+        const uint32_t wold = m->arc[(size_t)jf].y;
+        if (flag[i] == 0) {
+            m->arc[(size_t)jf].x = 0xFFFFFFFFu;
+            if (jr >= 0) m->rarc[(size_t)jr].x = 0xFFFFFFFFu;
+            ups.push_back(make_int4(UPD_TREE, a, b, 0));
+        } else {
+            m->arc[(size_t)jf].y = w[i];
+            if (jr >= 0) m->rarc[(size_t)jr].y = w[i];
+            if (w[i] < wold) ups.push_back(make_int4(UPD_LIGHTER, a, b, (int)w[i]));
+            else if (w[i] > wold) ups.push_back(make_int4(UPD_TREE, a, b, 0));
+            if (w[i] < g->wmin) g->wmin = w[i];
+            if (w[i] > g->wmax) g->wmax = w[i];
+        }
+        m->dirty_arc.push_back(jf);
+        if (jr >= 0) m->dirty_rarc.push_back(jr);
+    }
+    // inserts, appended to their rows in batch order (createDiffGraph)
+    bool relayout = false;
+    for (int32_t i = 0; i < nupd && !relayout; i++) {
+        if (flag[i] != 1) continue;
+        const int32_t a = u[i], b = v[i];
+        if (a < 0 || a >= n || b < 0 || b >= n) continue;
+        if (!mirror_append(m->beg, m->end, m->cap, m->arc, m->tail, a, make_uint2((uint32_t)b, w[i]), m->dirty_arc,
+                           m->dirty_row) ||
+            !mirror_append(m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, b, make_uint2((uint32_t)a, w[i]),
+                           m->dirty_rarc, m->dirty_rrow)) {
+            relayout = true;
+            break;
+        }
+        ups.push_back(make_int4(UPD_INS, a, b, (int)w[i]));
+        if (w[i] < g->wmin) g->wmin = w[i];
+        if (w[i] > g->wmax) g->wmax = w[i];
+    }
+    if (relayout) {
+        // the arc arrays are full: lay everything out again with fresh slack,
+        // then append the remaining inserts
+        std::vector<int32_t> b0 = m->beg, e0 = m->end, rb0 = m->rbeg, re0 = m->rend;
+        std::vector<uint2> a0 = m->arc, ra0 = m->rarc;
+        mirror_layout(b0, e0, a0, m->beg, m->end, m->cap, m->arc, m->tail);
+        mirror_layout(rb0, re0, ra0, m->rbeg, m->rend, m->rcap, m->rarc, m->rtail);
+        m->full = true;
+        size_t done = 0;
+        for (const int4 &x : ups)
+            if (x.x == UPD_INS) done++;
+        size_t seen = 0;
+        for (int32_t i = 0; i < nupd; i++) {
+            if (flag[i] != 1) continue;
+            const int32_t a = u[i], b = v[i];
+            if (a < 0 || a >= n || b < 0 || b >= n) continue;
+            if (seen++ < done) continue;
+            if (!mirror_append(m->beg, m->end, m->cap, m->arc, m->tail, a, make_uint2((uint32_t)b, w[i]),
+                               m->dirty_arc, m->dirty_row) ||
+                !mirror_append(m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, b, make_uint2((uint32_t)a, w[i]),
+                               m->dirty_rarc, m->dirty_rrow))
+                return fail(DDP_ERR_OOM, "dynamic graph: insert batch larger than the arc reserve");
+            ups.push_back(make_int4(UPD_INS, a, b, (int)w[i]));
+            if (w[i] < g->wmin) g->wmin = w[i];
+            if (w[i] > g->wmax) g->wmax = w[i];
+        }
+        g->e = (int64_t)m->arc.size();
+        g->e_rev = (int64_t)m->rarc.size();
+    }
+    int rc = dyn_upload(d);
+    if (rc) return rc;
+    const int32_t k = (int32_t)ups.size();
+    if (k > d->upd_cap) {
+        cudaFree(d->d_upd);
+        d->d_upd = nullptr;
+        DDP_CUDA(cudaMalloc(&d->d_upd, sizeof(int4) * std::max(k, 1)));
+        d->upd_cap = k;
+    }
+    if (k) DDP_CUDA(cudaMemcpy(d->d_upd, ups.data(), sizeof(int4) * k, cudaMemcpyHostToDevice));
+    rc = dyn_launch(d, 0, k);
+    if (rc) return rc;
+    if (out_cost) *out_cost = d->cost;
+    return DDP_OK;
+}
+
+int ddp_dyn_cost(const ddp_dyn *d, int32_t *cost) {
+    if (!d || !cost) return fail(DDP_ERR_INVALID, "null argument");
+    *cost = d->cost;
+    return DDP_OK;
+}
+
+int ddp_dyn_path(ddp_dyn *d, int32_t *buf, int32_t cap, int32_t *len) {
+    if (!d || !len) return fail(DDP_ERR_INVALID, "null argument");
+    *len = d->path_len;
+    if (buf && cap > 0 && d->path_len > 0)
+        DDP_CUDA(cudaMemcpy(buf, d->d_path, sizeof(int32_t) * std::min(cap, d->path_len), cudaMemcpyDeviceToHost));
+    return DDP_OK;
+}
+
+int ddp_dyn_stats(const ddp_dyn *d, int64_t *stats) {
+    if (!d || !stats) return fail(DDP_ERR_INVALID, "null argument");
+    for (int i = 0; i < 10; i++) stats[i] = d->stats[i];
+    return DDP_OK;
+}
+
+int ddp_dyn_free(ddp_dyn *d) {
+    if (!d) return DDP_OK;
+    slots_free(d->sa);
+    cudaFree(d->d_hops);
+    cudaFree(d->d_inv);
+    cudaFree(d->d_out);
+    cudaFree(d->d_path);
+    cudaFree(d->d_dc);
+    cudaFree(d->d_upd);
+    cudaFree(d->d_slot);
+    cudaFree(d->d_val);
+    cudaFree(d->d_rows);
+    // the graph keeps its dynamic layout and mirror (other searches and
+    // ddp_graph_read_csr see the updated graph)
+    if (d->g) d->g->dyn_active = false;
+    delete d;
+    return DDP_OK;
+}
+
+}  // extern "C"
+
+namespace ddp {
+void dyn_mirror_free(DynMirror *m) { delete m; }
+
+// Compacted CSR of a dynamic graph (live arcs in row order), n+1 offsets.
+int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights) {
+    const DynMirror *m = g->dyn;
+    int64_t k = 0;
+    for (int32_t u = 0; u < g->n; u++) {
+        if (offsets) offsets[u] = (int32_t)k;
+        for (int32_t j = m->beg[(size_t)u]; j < m->end[(size_t)u]; j++) {
+            const uint2 a = m->arc[(size_t)j];
+            if ((int32_t)a.x < 0) continue;
+            if (cols) cols[k] = (int32_t)a.x;
+            if (weights) weights[k] = a.y;
+            k++;
+        }
+    }
+    if (offsets) offsets[g->n] = (int32_t)k;
+    return DDP_OK;
+}
+
+int64_t dyn_live_arcs(const ddp_graph *g) {
+    const DynMirror *m = g->dyn;
+    int64_t k = 0;
+    for (int32_t u = 0; u < g->n; u++)
+        for (int32_t j = m->beg[(size_t)u]; j < m->end[(size_t)u]; j++)
+            if ((int32_t)m->arc[(size_t)j].x >= 0) k++;
+    return k;
+}
+}  // namespace ddp

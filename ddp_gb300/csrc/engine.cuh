@@ -57,6 +57,7 @@ struct SearchCtl {
     unsigned int tag;     // hop-array tag of the current query (batch)
     unsigned int hcap;    // hop cap of the last BFS
     int cur_q;            // query the slot is working on (batch)
+    int far_n, far_sel;   // far pile left by the last run (dynamic resume)
     unsigned int bar_count, bar_gen;  // grid barrier (single-query form)
 };
 
@@ -249,7 +250,10 @@ __device__ __forceinline__ int row_owner(const WarpRows &wr, int k) {
 __device__ __forceinline__ uint2 row_arc(const DevGraph &G, const WarpRows &wr, int o, int k,
                                          bool fwd) {
     int j = k - wr.excl[o];
-    if (j < wr.bdeg[o]) return fwd ? __ldg(G.arc + wr.rb[o] + j) : __ldg(G.rarc + wr.rb[o] + j);
+    if (j < wr.bdeg[o]) {
+        if (G.oend) return fwd ? __ldcg(G.arc + wr.rb[o] + j) : __ldcg(G.rarc + wr.rb[o] + j);
+        return fwd ? __ldg(G.arc + wr.rb[o] + j) : __ldg(G.rarc + wr.rb[o] + j);
+    }
     j -= wr.bdeg[o];
     return fwd ? __ldcg(G.darc + wr.drb[o] + j) : __ldcg(G.drarc + wr.drb[o] + j);
 }
@@ -258,7 +262,11 @@ __device__ __forceinline__ uint2 row_arc(const DevGraph &G, const WarpRows &wr, 
 struct SearchParams {
     int32_t s, t;
     uint32_t delta;
-    int32_t K;  // 0 = whole near bucket per iteration
+    int32_t K;     // 0 = whole near bucket per iteration
+    int keep;      // keep every generated node open (no f(t) pruning): the
+                   // state stays resumable after graph updates
+    int resume;    // continue from the slot's far pile instead of starting at s
+    int no_touch_log;  // do not log first touches (slots that are never reset)
 };
 
 struct SearchResult {
@@ -284,23 +292,31 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             ctl->err[i] = 0;
             ctl->ck[i] = 0;
         }
-        ctl->touched = 1;
         ctl->iters = 0;
         ctl->expanded = ctl->scanned = ctl->relaxed = 0;
         ctl->far_scanned = 0;
-        B.state[P.s] = st_make(0, -1);
-        B.touched[0] = P.s;
-        B.q0[0] = make_uint2((uint32_t)P.s, 0u);
+        if (!P.resume) {
+            ctl->touched = 1;
+            B.state[P.s] = st_make(0, -1);
+            B.touched[0] = P.s;
+            B.q0[0] = make_uint2((uint32_t)P.s, 0u);
+        }
     }
+    const int64_t far_resume = P.resume ? (int64_t)(*(volatile int *)&ctl->far_n) : 0;
+    const bool far_in_f1 = P.resume && (*(volatile int *)&ctl->far_sel) != 0;
     grp.sync();
 
     uint2 *qcur = B.q0, *qnxt = B.q1;
-    uint2 *fcur = B.f0, *falt = B.f1;
-    int64_t nnear = 1, head = 0, nnext = 0, nfar = 0;
+    uint2 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
+    int64_t nnear = P.resume ? 0 : 1, head = 0, nnext = 0, nfar = far_resume;
     const uint32_t hs = H(P.s);
     uint32_t T = sat_add(hs, P.delta);
     uint32_t Tsplit = T;
-    bool splitting = false;
+    bool splitting = P.resume != 0;
+    if (P.resume) {
+        T = 0;
+        Tsplit = 0;  // the first split only measures the far pile's minimum f
+    }
     // compaction: a split pass at the current T that only drops stale and
     // pruned far entries, run when the far pile fills up between splits
     bool compacting = false;
@@ -328,6 +344,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                 const int64_t idx = base + lane;
                 int u = -1, rb = 0, bdeg = 0, drb = 0, deg = 0;
                 uint32_t gu = 0;
+                bool requeue = false;
                 if (idx < end) {
                     const uint2 en = __ldcg(qcur + idx);
                     u = (int)en.x;
@@ -336,20 +353,26 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     // entries that turn out stale)
                     const uint64_t su = __ldcg(B.state + u);
                     const uint32_t hu = H(u);
-                    const int r0 = __ldg(G.off + u), r1 = __ldg(G.off + u + 1);
+                    const int r0 = row_begin(G.off, G.oend, u), r1 = row_end(G.off, G.oend, u);
                     int d0 = 0, d1 = 0;
                     if (has_diff) {
                         d0 = __ldcg(G.doff + u);
                         d1 = __ldcg(G.doff + u + 1);
                     }
-                    if (st_g(su) == gu && u != P.t && (uint64_t)gu + hu < ft) {
-                        rb = r0;
-                        bdeg = r1 - r0;
-                        drb = d0;
-                        deg = bdeg + (d1 - d0);
-                        n_exp++;
+                    if (st_g(su) == gu && u != P.t) {
+                        if ((uint64_t)gu + hu < ft) {
+                            rb = r0;
+                            bdeg = r1 - r0;
+                            drb = d0;
+                            deg = bdeg + (d1 - d0);
+                            n_exp++;
+                        } else if (P.keep) {
+                            requeue = true;  // stays open beyond f(t)
+                        }
                     }
                 }
+                stage_push(requeue, make_uint2((uint32_t)u, gu), wr.sf, c_f, &ctl->fq[PH], fcur, nfar,
+                           B.cap_f, ctl, PH);
                 int total;
                 int ex = warp_excl_scan(deg, &total);
                 wr.excl[lane] = ex;
@@ -396,7 +419,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     }
 #pragma unroll
                     for (int r = 0; r < ARCS; r++) {
-                        go[r] = live[r] && (uint64_t)ng[r] + hv[r] < ft;
+                        go[r] = live[r] && (P.keep ? hv[r] < INF_G : (uint64_t)ng[r] + hv[r] < ft);
                         prev[r] = go[r] ? atomicCAS(B.state + v[r], sv[r], st_make(ng[r], wr.u[o[r]])) : sv[r];
                     }
 #pragma unroll
@@ -412,7 +435,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                                 got = atomicCAS(B.state + v[r], cur, st_make(ng[r], wr.u[o[r]]));
                             }
                             if (got == cur) {
-                                first = st_g(cur) >= INF_G;
+                                first = !P.no_touch_log && st_g(cur) >= INF_G;
                                 const uint64_t fv = (uint64_t)ng[r] + hv[r];
                                 if (fv < T) to_near = true;
                                 else to_far = true;
@@ -449,13 +472,11 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     uint64_t sv = __ldcg(B.state + en.x);
                     if (st_g(sv) == en.y) {
                         uint64_t f = (uint64_t)en.y + H((int)en.x);
-                        if (f < ft) {
-                            if (f < thr) {
-                                to_near = true;
-                            } else {
-                                keep = true;
-                                local_min = min(local_min, (uint32_t)f);
-                            }
+                        if (f < ft && f < thr) {
+                            to_near = true;
+                        } else if (f < ft || (P.keep && f < INF_G)) {
+                            keep = true;
+                            local_min = min(local_min, (uint32_t)f);
                         }
                     }
                 }
@@ -530,8 +551,8 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             if (nnear > 0) {
                 T = Tsplit;
                 splitting = false;
-            } else if (nfar == 0) {
-                break;  // open list empty below f(t): done
+            } else if (nfar == 0 || m >= ft) {
+                break;  // no open node with f < f(t): done
             } else {
                 Tsplit = sat_add(m, P.delta);
             }
@@ -552,6 +573,10 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     if (lane == 0) {
         if (n_exp) atomicAdd(&ctl->expanded, n_exp);
         if (n_rel) atomicAdd(&ctl->relaxed, n_rel);
+    }
+    if (grp.rank() == 0) {
+        ctl->far_n = (int)nfar;
+        ctl->far_sel = fcur == B.f1 ? 1 : 0;
     }
     grp.sync();
     SearchResult r;
@@ -624,8 +649,8 @@ __device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBu
             int rb = 0, bdeg = 0, drb = 0, deg = 0;
             if (idx < nf) {
                 int u = __ldcg(fa + idx);
-                rb = __ldg(G.roff + u);
-                bdeg = __ldg(G.roff + u + 1) - rb;
+                rb = row_begin(G.roff, G.roend, u);
+                bdeg = row_end(G.roff, G.roend, u) - rb;
                 deg = bdeg;
                 if (has_diff) {
                     drb = __ldcg(G.droff + u);

@@ -43,6 +43,8 @@ DevGraph graph_view(const ddp_graph *g) {
     d.darc = g->d_darc;
     d.droff = g->d_droff;
     d.drarc = g->d_drarc;
+    d.oend = g->d_oend;
+    d.roend = g->d_roend;
     return d;
 }
 
@@ -115,6 +117,9 @@ void graph_release(ddp_graph *g) {
     cudaFree(g->d_darc);
     cudaFree(g->d_droff);
     cudaFree(g->d_drarc);
+    cudaFree(g->d_oend);
+    cudaFree(g->d_roend);
+    dyn_mirror_free(g->dyn);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
 }
@@ -203,8 +208,9 @@ int ddp_graph_set_coords(ddp_graph *g, const int32_t *xy) {
 
 int ddp_graph_info(const ddp_graph *g, int32_t *n, int64_t *e, uint32_t *wmin, uint32_t *wmax) {
     if (!g) return fail(DDP_ERR_INVALID, "null graph");
+    std::lock_guard<std::mutex> lk(const_cast<ddp_graph *>(g)->mu);
     if (n) *n = g->n;
-    if (e) *e = g->e;
+    if (e) *e = g->dyn ? dyn_live_arcs(g) : g->e;
     if (wmin) *wmin = g->wmin;
     if (wmax) *wmax = g->wmax;
     return DDP_OK;
@@ -213,6 +219,7 @@ int ddp_graph_info(const ddp_graph *g, int32_t *n, int64_t *e, uint32_t *wmin, u
 int ddp_graph_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights) {
     if (!g) return fail(DDP_ERR_INVALID, "null graph");
     std::lock_guard<std::mutex> lk(const_cast<ddp_graph *>(g)->mu);
+    if (g->dyn) return dyn_read_csr(g, offsets, cols, weights);
     if (offsets)
         DDP_CUDA(cudaMemcpy(offsets, g->d_off, sizeof(int32_t) * ((size_t)g->n + 1),
                             cudaMemcpyDeviceToHost));

@@ -6,6 +6,8 @@
 
 #include "common.cuh"
 
+struct DynMirror;
+
 struct ddp_graph {
     std::mutex mu;
     int device = 0;
@@ -25,6 +27,11 @@ struct ddp_graph {
     uint2 *d_darc = nullptr;
     int32_t *d_droff = nullptr;
     uint2 *d_drarc = nullptr;
+    // dynamic layout (rows with explicit ends), set by ddp_dyn_create
+    int32_t *d_oend = nullptr;
+    int32_t *d_roend = nullptr;
+    DynMirror *dyn = nullptr;  // host mirror of a dynamic graph
+    bool dyn_active = false;          // a ddp_dyn search owns the graph's updates
     // single-query workspace, allocated on first use
     struct Workspace *ws = nullptr;
 };
@@ -33,4 +40,7 @@ namespace ddp {
 DevGraph graph_view(const ddp_graph *g);
 int ensure_device();
 void workspace_release(ddp_graph *g);
+void dyn_mirror_free(DynMirror *m);
+int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights);
+int64_t dyn_live_arcs(const ddp_graph *g);
 }  // namespace ddp

@@ -161,7 +161,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
             grp.sync();
             continue;
         }
-        SearchParams P{s, t, A.delta, A.K};
+        SearchParams P{s, t, A.delta, A.K, 0, 0, 0};
         SearchResult r;
         if (HK == 1) {
             const uint32_t tag = *(volatile uint32_t *)&ctl->tag;
@@ -314,6 +314,10 @@ struct ddp_query {
     int64_t stats[DDP_STATS] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
+namespace ddp {
+uint32_t *heuristic_hops_ptr(const ddp_heuristic *h) { return h ? h->d_hops : nullptr; }
+}  // namespace ddp
+
 extern "C" {
 
 int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_t *user_h,
@@ -442,7 +446,7 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
     int64_t cap = o.queue_cap > 0 ? o.queue_cap : (int64_t)g->n + 1024;
     const uint32_t delta = o.delta > 0 ? (uint32_t)o.delta : auto_delta(g);
     DevGraph G = graph_view(g);
-    SearchParams P{source, target, delta, o.K};
+    SearchParams P{source, target, delta, o.K, 0, 0, 0};
     for (int attempt = 0; attempt < 4; attempt++) {
         int rc = workspace_ensure(g, cap);
         if (rc) return rc;

@@ -39,5 +39,6 @@ size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops);
 int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, bool hops,
                 cudaStream_t st);
 void slots_free(SlotArrays &sa);
+uint32_t *heuristic_hops_ptr(const ddp_heuristic *h);
 
 }  // namespace ddp

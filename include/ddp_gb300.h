@@ -158,6 +158,32 @@ int ddp_batch_group(const ddp_batch *b, int32_t *group);
 int ddp_batch_launches(const ddp_batch *b, int32_t *launches);
 int ddp_batch_free(ddp_batch *b);
 
+/* ---- dynamic A*: DA_star/DA_dyn_cpu.cu (program), LIB d_a_star.cuh:9-86
+ *      (GPU_D_A_Star, declared there but not compiling) ------------------- */
+typedef struct ddp_dyn ddp_dyn;
+/* Runs the initial A* from source to target on g (hkind DDP_H_ZERO or
+ * DDP_H_BFS_HOPS) and keeps the search resident.  The graph switches to a
+ * layout with growable rows; it stays usable by every other call and
+ * ddp_graph_read_csr returns its current arcs.  One dynamic search per graph
+ * at a time. */
+int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind,
+                   const ddp_opts *opts, ddp_dyn **out);
+/* Applies one update batch (DA_dyn_cpu.cu:1295-1326 Updates.txt lines):
+ * flag 1 = insert u->v with weight w (appended to row u), flag 0 = delete the
+ * first live u->v arc of the pre-batch graph, flag 2 = set the weight of
+ * that arc to w (no reference counterpart; a delete plus an insert gives the
+ * same arc set).  Repairs the search incrementally and returns the new cost
+ * (DDP_INF when the target became unreachable). */
+int ddp_dyn_update(ddp_dyn *d, int32_t n, const int32_t *flag, const int32_t *u, const int32_t *v,
+                   const uint32_t *w, int32_t *out_cost);
+int ddp_dyn_cost(const ddp_dyn *d, int32_t *cost);
+int ddp_dyn_path(ddp_dyn *d, int32_t *buf, int32_t cap, int32_t *len);
+/* Counters of the last create/update: cost, path length, status, search
+ * phases, invalidated nodes, re-seeded nodes, relaxed arc heads, lowered hop
+ * counts, expanded nodes, scanned arcs (10 values). */
+int ddp_dyn_stats(const ddp_dyn *d, int64_t *stats);
+int ddp_dyn_free(ddp_dyn *d);
+
 /* ---- reverse-BFS hop counts without device allocation ------------------
  * No counterpart in the reference.  For callers that cannot let a library
  * call cudaMalloc (for example a service that gives all device memory to its

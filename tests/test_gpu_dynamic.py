@@ -1,0 +1,162 @@
+"""Dynamic A* (ddp_dyn) against the oracle: after every update batch the
+cost equals a from-scratch A* on the updated graph (the reference's own
+check, DA_star/genCSRwholegraph.cpp + GA_v2.cu on graph_cg.txt), the path is
+valid on that graph, and the device graph equals the oracle's merged CSR
+(DA_dyn_cpu.cu removeDelEdges + mergeDiff semantics) row by row."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _scratch_cost(O, off_ref, col, w, s, t, heuristic=True):
+    n = len(off_ref)
+    h = np.maximum(O.bfs_heuristic(n, off_ref, col, w, t), 0) if heuristic else np.zeros(n, np.int32)
+    found, cost, _, _, _ = O.astar(n, off_ref, col, w, h, s, t)
+    return cost if found else 2147483647
+
+
+def _run(d, O, g, batches, s, t, hkind=None, check_csr_every=1):
+    """g: CSR with a sentinel last node; batches: list of (flag,u,v,w)."""
+    hkind = d.H_BFS_HOPS if hkind is None else hkind
+    dg = d.DeviceGraph.from_csr(g)
+    dyn = d.DynamicSearch(dg, s, t, hkind)
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    assert dyn.cost == _scratch_cost(O, off, col, w, s, t)
+    for bi, (fl, uu, vv, ww) in enumerate(batches):
+        cost = dyn.update(fl, uu, vv, ww)
+        off, col, w, _ = O.apply_batch(len(off), off, col, w, fl, uu, vv, ww)
+        want = _scratch_cost(O, off, col, w, s, t)
+        assert cost == want, f"batch {bi}: {cost} != {want} ({dyn.stats()})"
+        full_off = np.concatenate([off, [len(col)]]).astype(np.int32)
+        if want != d.INF:
+            ok, why = O.check_path(full_off, col, w, dyn.path(), s, t, cost)
+            assert ok, f"batch {bi}: {why}"
+        if bi % check_csr_every == 0:
+            r = dg.read_csr()
+            assert np.array_equal(r.off, full_off) and np.array_equal(r.col, col) and np.array_equal(r.w, w), bi
+    dyn.close()
+    return dg
+
+
+def _split(fl, u, v, w, per):
+    return [(fl[i:i + per], u[i:i + per], v[i:i + per], w[i:i + per]) for i in range(0, len(fl), per)]
+
+
+def test_dynamic_random_batches(gpu, oracle):
+    """BASELINE config 3 shape at 1/50 scale: inserts of new arcs and
+    deletes of existing non-chain arcs, weights in [1,1000]."""
+    d = gpu
+    base = d.gen_random_chain(20000, 10, 1, 1000, 303)
+    fl, u, v, w = d.gen_updates(base, 25, 200, 100, 1, 1000, 304)
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    _run(d, oracle, g, _split(fl, u, v, w, 200), s, t)
+
+
+def test_dynamic_deletes_on_the_path(gpu, oracle):
+    """Deleting arcs of the current shortest path exercises subtree
+    invalidation and re-seeding; re-inserting them restores the cost."""
+    d = gpu
+    base = d.gen_random_chain(5000, 6, 1, 100, 11)
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    dg = d.DeviceGraph.from_csr(g)
+    dyn = d.DynamicSearch(dg, s, t)
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    removed = []
+    for rnd in range(6):
+        p = dyn.path()
+        assert len(p) >= 2
+        a, b = int(p[len(p) // 2 - 1]), int(p[len(p) // 2])
+        row = slice(off[a], off[a + 1] if a + 1 < len(off) else len(col))
+        ws = w[row][col[row] == b]
+        removed.append((a, b, int(ws[0])))
+        fl, uu, vv, ww = [0], [a], [b], [0]
+        cost = dyn.update(fl, uu, vv, ww)
+        off, col, w, nd = oracle.apply_batch(len(off), off, col, w, fl, uu, vv, ww)
+        assert nd == 1
+        assert cost == _scratch_cost(oracle, off, col, w, s, t), rnd
+        assert dyn.stats()["invalidated"] >= 1
+    fl = [1] * len(removed)
+    uu = [x[0] for x in removed]
+    vv = [x[1] for x in removed]
+    ww = [x[2] for x in removed]
+    cost = dyn.update(fl, uu, vv, ww)
+    off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, uu, vv, ww)
+    assert cost == _scratch_cost(oracle, off, col, w, s, t)
+    dyn.close()
+
+
+def test_dynamic_weight_changes_and_unreachable(gpu, oracle):
+    d = gpu
+    base = d.gen_random_chain(3000, 4, 1, 50, 21)
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    dg = d.DeviceGraph.from_csr(g)
+    dyn = d.DynamicSearch(dg, s, t)
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    rng = np.random.default_rng(2)
+    for rnd in range(8):
+        p = dyn.path()
+        k = int(rng.integers(0, len(p) - 1))
+        a, b = int(p[k]), int(p[k + 1])
+        nw = int(rng.integers(1, 200))
+        fl, uu, vv, ww = [2, 2], [a, int(p[0])], [b, int(p[1])], [nw, 1]
+        cost = dyn.update(fl, uu, vv, ww)
+        off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, uu, vv, ww)
+        assert cost == _scratch_cost(oracle, off, col, w, s, t), rnd
+    # cut every arc into t: unreachable, then one arc back
+    n = len(off)
+    ends = np.append(off[1:], len(col))
+    src = np.repeat(np.arange(n), ends - off)
+    into = np.flatnonzero((col == t))
+    fl = [0] * len(into)
+    uu = src[into].tolist()
+    vv = [t] * len(into)
+    cost = dyn.update(fl, uu, vv, [0] * len(into))
+    off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, uu, vv, [0] * len(into))
+    assert cost == d.INF == _scratch_cost(oracle, off, col, w, s, t)
+    assert len(dyn.path()) == 0
+    cost = dyn.update([1], [s], [t], [777])
+    off, col, w, _ = oracle.apply_batch(len(off), off, col, w, [1], [s], [t], [777])
+    assert cost == _scratch_cost(oracle, off, col, w, s, t) <= 777
+    dyn.close()
+
+
+def test_dynamic_row_growth_and_relayout(gpu, oracle):
+    """Many inserts into a few rows: rows move to the end of the arc array
+    and the array is laid out again when it fills; the CSR stays exact."""
+    d = gpu
+    base = d.gen_random_chain(2000, 3, 1, 30, 5)
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    rng = np.random.default_rng(9)
+    batches = []
+    for b in range(6):
+        m = 3000
+        uu = rng.choice([s, int(base.perm[5]), int(base.perm[9])], m).astype(np.int32)
+        vv = rng.integers(0, base.n, m).astype(np.int32)
+        keep = uu != vv
+        uu, vv = uu[keep], vv[keep]
+        batches.append((np.ones(len(uu), np.int32), uu, vv, rng.integers(5, 60, len(uu)).astype(np.uint32)))
+    _run(d, oracle, g, batches, s, t)
+
+
+def test_dynamic_zero_heuristic_and_recreate(gpu, oracle):
+    d = gpu
+    base = d.gen_random_chain(8000, 8, 1, 1000, 77)
+    fl, u, v, w = d.gen_updates(base, 6, 100, 50, 1, 1000, 78)
+    g = base.with_sentinel()
+    s, t = int(base.perm[3]), int(base.perm[-2])
+    dg = _run(d, oracle, g, _split(fl, u, v, w, 100), s, t, hkind=d.H_ZERO, check_csr_every=3)
+    # a second dynamic search on the same (already updated) graph
+    r = dg.read_csr()
+    dyn = d.DynamicSearch(dg, t, s)
+    h = np.maximum(oracle.bfs_heuristic(r.n, r.off[:-1], r.col, r.w, s), 0)
+    f, c, _, _, _ = oracle.astar(r.n, r.off[:-1], r.col, r.w, h, t, s)
+    assert dyn.cost == (c if f else d.INF)
+    # the static single-query engine sees the updated graph too
+    hh = dg.heuristic(s, d.H_BFS_HOPS)
+    assert dg.solve(t, s, hh).cost == dyn.cost
+    dyn.close()
