@@ -36,6 +36,14 @@ CONFIGS = {
     # name: (nodes, avg out-degree, wmin, wmax, pairs, hop_lo, hop_hi, graph seed, pair seed)
     "c4": dict(n=4_000_000, deg=8, wmin=1, wmax=100, pairs=4096, hop_lo=4, hop_hi=400, gseed=4004,
                pseed=4400),
+    "c1": dict(n=100_000, deg=8, wmin=1, wmax=100, gseed=1001, K=1024),
+    "c2": dict(rows=2048, cols=2048, wall=0.30, gseed=2002),
+    "c3": dict(n=1_000_000, deg=10, wmin=1, wmax=1000, gseed=3003, useed=3303, batches=100, per_batch=1000,
+               inserts=500),
+    "c5": dict(n=8_000_000, k=6, side=1 << 20, wscale=1000, gseed=5005, rates=[5000, 20000, 50000, 100000, 200000],
+               seconds=1.0, update_ms=10, wchanges=500, deletes=100, inserts=100),
+    "c5-small": dict(n=500_000, k=6, side=1 << 20, wscale=1000, gseed=5005, rates=[5000, 20000, 50000],
+                     seconds=0.5, update_ms=10, wchanges=500, deletes=100, inserts=100),
     "c4-small": dict(n=400_000, deg=8, wmin=1, wmax=100, pairs=1024, hop_lo=4, hop_hi=400, gseed=4004,
                      pseed=4400),
 }
@@ -204,10 +212,247 @@ def run_reference(a, c, world, rank):
     print(json.dumps(out), flush=True)
 
 
+def _pct(x, q):
+    return float(np.percentile(np.asarray(x, np.float64), q)) if len(x) else None
+
+
+def bench_single(a, c):
+    """Configs 1 and 2: one query, plain single-query GA* (cooperative grid),
+    K swept; exact against the oracle."""
+    import torch  # noqa: F401  (device init on the same path as the main bench)
+
+    from ddp_gb300 import build as B
+    B.build()
+    import ddp_gb300 as d
+    from oracle import oracle as O
+    if a.config == "c1":
+        g = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
+        s, t = int(g.perm[0]), int(g.perm[-1])
+        hk = d.H_BFS_HOPS
+        Ks = [c["K"]]
+        workload = (f"single-query GA*: {c['n']:,}-node random digraph (chain + uniform arcs), avg out-degree "
+                    f"{c['deg']}, w U[{c['wmin']},{c['wmax']}], h = reverse-BFS hops x min w, K={c['K']}")
+    else:
+        g = d.gen_maze(c["rows"], c["cols"], c["wall"], c["gseed"])
+        s, t = 0, g.n - 1
+        hk = d.H_MANHATTAN
+        Ks = [256, 512, 1024, 2048, 4096, 8192, 0]
+        workload = (f"single-query GA*: {c['rows']}x{c['cols']} 4-connected maze, {int(100 * c['wall'])}% walls, "
+                    f"carved corridor (0,0)->(end), unit w, Manhattan h, K swept")
+    dg = d.DeviceGraph.from_csr(g)
+    h = dg.heuristic(t, hk, want_values=True)
+    res = {}
+    cost = None
+    for K in Ks:
+        for _ in range(max(3, a.warmup)):
+            r = dg.solve(s, t, h, K=K)
+        times = []
+        for _ in range(a.steps):
+            t0 = time.perf_counter()
+            r = dg.solve(s, t, h, K=K)
+            times.append(time.perf_counter() - t0)
+        res[K] = (float(np.median(times)), r)
+        cost = r.cost
+    bestK = min(res, key=lambda k: res[k][0])
+    best_t, r = res[bestK]
+    gs = g.with_sentinel()
+    hh = np.concatenate([np.maximum(h.values, 0), [0]]).astype(np.int32)
+    f, oc, _, _, osec = O.astar(gs.n, gs.off[:-1], gs.col, gs.w, hh, s, t, mode=O.HEAP_POSMAP)
+    ok, why = O.check_path(g.off, g.col, g.w, r.path, s, t, r.cost)
+    out = {"metric": "single-query GA* latency (exact)", "value": 1000 * best_t, "unit": "ms/query",
+           "higher_is_better": False, "n_gpus": 1, "steps": a.steps, "warmup": max(3, a.warmup),
+           "dtype": "int32", "data": "synthetic (seeded generators)",
+           "config": {"workload": workload, "n": g.n, "e": g.e, "best_K": bestK,
+                      "K_sweep_ms": {str(k): 1000 * v[0] for k, v in res.items()}},
+           "cost": cost, "exact_vs_oracle": bool(f and oc == cost), "path_valid": ok,
+           "work": {"expanded": int(r.stats[0]), "scanned": int(r.stats[1]), "phases": int(r.stats[3])},
+           "cpu_baseline": {"value": 1000 * osec, "unit": "ms/query", "cores": 1, "kind": "port",
+                            "sample": "the same query, search loop only, position-map heap"}}
+    print(json.dumps(out), flush=True)
+
+
+def bench_dynamic(a, c):
+    """Config 3: update batches applied incrementally, against a from-scratch
+    GA* per batch on the same GPU (the reference's GA_merge method), exact
+    against the CPU oracle on sampled batches."""
+    import torch  # noqa: F401
+
+    from ddp_gb300 import build as B
+    B.build()
+    import ddp_gb300 as d
+    from oracle import oracle as O
+    base = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
+    fl, u, v, w = d.gen_updates(base, c["batches"], c["per_batch"], c["inserts"], c["wmin"], c["wmax"], c["useed"])
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    dg = d.DeviceGraph.from_csr(g)
+    t0 = time.perf_counter()
+    dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS)
+    t_init = time.perf_counter() - t0
+    per = c["per_batch"]
+    nb = c["batches"]
+    sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}
+    off, col, ww = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    dyn_t, scratch_t, cpu_t, exact, costs, inval = [], [], [], True, [], []
+    for b in range(nb):
+        sl = slice(b * per, (b + 1) * per)
+        t0 = time.perf_counter()
+        cost = dyn.update(fl[sl], u[sl], v[sl], w[sl])
+        dyn_t.append(time.perf_counter() - t0)
+        costs.append(cost)
+        inval.append(dyn.stats()["invalidated"])
+        off, col, ww, _ = O.apply_batch(len(off), off, col, ww, fl[sl], u[sl], v[sl], w[sl])
+        if b in sample:
+            # GPU from-scratch GA* on the updated graph (heuristic + search)
+            t1 = time.perf_counter()
+            hh = dg.heuristic(t, d.H_BFS_HOPS)
+            r = dg.solve(s, t, hh)
+            hh.close()
+            scratch_t.append(time.perf_counter() - t1)
+            hcpu = np.maximum(O.bfs_heuristic(len(off), off, col, ww, t), 0)
+            f, oc, _, _, osec = O.astar(len(off), off, col, ww, hcpu, s, t, mode=O.HEAP_POSMAP)
+            cpu_t.append(osec)
+            want = oc if f else d.INF
+            exact = exact and cost == want and r.cost == want
+    out = {"metric": "dynamic A* update batch latency (exact)", "value": 1000 * float(np.mean(dyn_t)),
+           "unit": "ms/batch", "higher_is_better": False, "n_gpus": 1, "steps": nb, "warmup": 0,
+           "dtype": "int32", "data": "synthetic (seeded generators)",
+           "config": {"workload": f"dynamic A*: {c['n']:,}-node random digraph, avg out-degree {c['deg']}, "
+                                  f"w U[{c['wmin']},{c['wmax']}], BFS-hops x min w heuristic, {nb} batches x "
+                                  f"{per} updates ({c['inserts']} inserts of new arcs, {per - c['inserts']} "
+                                  f"deletes of existing non-chain arcs)", "n": g.n, "e": g.e},
+           "batch_ms": {"p50": 1000 * _pct(dyn_t, 50), "p99": 1000 * _pct(dyn_t, 99),
+                        "initial_search_ms": 1000 * t_init},
+           "gpu_from_scratch_ms_per_batch": 1000 * float(np.mean(scratch_t)),
+           "cpu_from_scratch_ms_per_batch": {"value": 1000 * float(np.mean(cpu_t)), "cores": 1, "kind": "port",
+                                             "sample": f"{len(cpu_t)} sampled batches, search loop only"},
+           "exact_on_sampled_batches": exact, "sampled_batches": sorted(sample),
+           "invalidated_nodes_mean": float(np.mean(inval)), "costs_first_last": [costs[0], costs[-1]]}
+    print(json.dumps(out), flush=True)
+    dyn.close()
+
+
+def bench_serving(a, c):
+    """Config 5: Poisson arrivals served by continuous batching on an 8M-node
+    geometric graph, with an update batch every 10 ms."""
+    import torch  # noqa: F401
+
+    from ddp_gb300 import build as B
+    B.build()
+    import ddp_gb300 as d
+    from oracle import oracle as O
+    g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
+    dg = d.DeviceGraph.from_csr(g)
+    dg.set_euclid(d.euclid_rho_fp(g))
+    srv = d.Server(dg, d.H_EUCLID, max_requests=1 << 22, grid=a.slots)
+    rng = np.random.default_rng(c["gseed"] + 1)
+    src = np.repeat(np.arange(g.n, dtype=np.int32), np.diff(g.off))
+    deleted = []
+
+    def update_batch():
+        j = rng.integers(0, g.e, c["wchanges"] + c["deletes"])
+        wc = j[:c["wchanges"]]
+        dl = j[c["wchanges"]:]
+        neww = np.maximum(1, np.rint(g.w[wc] * rng.uniform(0.5, 2.0, len(wc)))).astype(np.uint32)
+        fl = [np.full(len(wc), 2, np.int32), np.zeros(len(dl), np.int32)]
+        uu = [src[wc], src[dl]]
+        vv = [g.col[wc], g.col[dl]]
+        ww = [neww, np.zeros(len(dl), np.uint32)]
+        if deleted:  # inserts between neighbours: arcs deleted earlier come back
+            back = deleted[:c["inserts"]]
+            del deleted[:c["inserts"]]
+            bj = np.array(back, np.int64)
+            fl.append(np.ones(len(bj), np.int32))
+            uu.append(src[bj])
+            vv.append(g.col[bj])
+            ww.append(g.w[bj])
+        deleted.extend(dl.tolist())
+        srv.update(np.concatenate(fl), np.concatenate(uu), np.concatenate(vv), np.concatenate(ww))
+
+    # warm up: first update builds the dynamic mirror; a few queries
+    update_batch()
+    srv.submit(rng.integers(0, g.n, 64).astype(np.int32), rng.integers(0, g.n, 64).astype(np.int32))
+    srv.drain()
+    rows = []
+    for rate in c["rates"]:
+        nreq = int(rate * c["seconds"])
+        arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        S = rng.integers(0, g.n, nreq).astype(np.int32)
+        T = rng.integers(0, g.n, nreq).astype(np.int32)
+        lat, got, i, n_upd = [], 0, 0, 0
+        t0 = time.perf_counter()
+        next_upd = c["update_ms"] / 1000.0
+        last = t0
+        while got < nreq:
+            now = time.perf_counter() - t0
+            j = int(np.searchsorted(arr, now, side="right"))
+            if j > i:
+                srv.submit(S[i:j], T[i:j])
+                i = j
+            if now >= next_upd and i < nreq:
+                update_batch()
+                n_upd += 1
+                next_upd += c["update_ms"] / 1000.0
+            ids, costs, l, v = srv.poll()
+            if len(ids):
+                got += len(ids)
+                lat.append(l)
+                last = time.perf_counter()
+            elif j == i and i >= nreq:
+                time.sleep(0.0001)
+            if time.perf_counter() - t0 > 60 * c["seconds"] + 60:
+                break
+        lat = np.concatenate(lat) / 1e6 if lat else np.zeros(0)
+        wall = last - t0
+        rows.append({"offered_qps": rate, "served_qps": got / wall if wall > 0 else 0.0, "requests": nreq,
+                     "completed": got, "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "updates": n_upd})
+    # exactness on a sample (against the current graph version: no updates now)
+    Sx = rng.integers(0, g.n, 8).astype(np.int32)
+    Tx = rng.integers(0, g.n, 8).astype(np.int32)
+    srv.submit(Sx, Tx)
+    ids, costs, _, _ = srv.drain()
+    costs = costs[np.argsort(ids)]
+    r = dg.read_csr()
+    exact = True
+    cpu_ms = []
+    for k in range(len(Sx)):
+        gs = r.with_sentinel()
+        f, oc, _, _, osec = O.astar(gs.n, gs.off[:-1], gs.col, gs.w, np.zeros(gs.n, np.int32), int(Sx[k]), int(Tx[k]))
+        cpu_ms.append(1000 * osec)
+        exact = exact and costs[k] == (oc if f else d.INF)
+    st = srv.stats()
+    best = max(rows, key=lambda x: x["served_qps"])
+    out = {"metric": "A* serving queries/sec + p50/p99 latency (exact)", "value": best["served_qps"],
+           "unit": "queries/s", "higher_is_better": True, "n_gpus": 1, "dtype": "int32",
+           "data": "synthetic (seeded generators)",
+           "config": {"workload": f"serving: {c['n']:,} points uniform on a {c['side']}^2 grid, symmetric "
+                                  f"{c['k']}-NN arcs, w = max(1, round({c['wscale']} x length / mean spacing)), "
+                                  f"h = floor(rho x floor(distance)), Poisson arrivals, every {c['update_ms']} ms "
+                                  f"{c['wchanges']} weight changes x U[0.5,2] + {c['deletes']} deletes + up to "
+                                  f"{c['inserts']} re-inserts", "n": g.n, "e": g.e, "slots": st["slots"]},
+           "rates": rows, "exact_on_sample": bool(exact), "server": st,
+           "cpu_baseline": {"value": float(np.mean(cpu_ms)), "unit": "ms/query (Dijkstra order, h = 0)",
+                            "cores": 1, "kind": "port", "sample": f"{len(cpu_ms)} queries"}}
+    print(json.dumps(out), flush=True)
+    srv.close()
+
+
 def main():
     a = args_parse()
     world, rank, local = dist_env()
     c = dict(CONFIGS[a.config])
+    if a.config in ("c1", "c2"):
+        if rank == 0:
+            bench_single(a, c)
+        return
+    if a.config == "c3":
+        if rank == 0:
+            bench_dynamic(a, c)
+        return
+    if a.config in ("c5", "c5-small"):
+        if rank == 0:
+            bench_serving(a, c)
+        return
     if a.impl == "reference":
         run_reference(a, c, world, rank)
         return

@@ -24,7 +24,7 @@ import numpy as np
 
 from ._lib import DdpError, Opts, check, lib, ptr  # noqa: F401
 
-H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED = 0, 1, 2, 3, 4
+H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED, H_EUCLID = 0, 1, 2, 3, 4, 5
 INF = 2147483647
 # per-query counters: expanded, scanned, relaxed, phases, bfs_reached,
 # bfs_scanned, far_scanned, touched
@@ -32,10 +32,11 @@ STATS = 8
 
 __all__ = [
     "CSR", "DeviceGraph", "Heuristic", "SolveResult", "BatchEngine", "DdpError", "INF",
-    "H_ZERO", "H_BFS_HOPS", "H_MANHATTAN", "H_USER", "H_BFS_CAPPED", "gen_random_chain", "gen_maze",
+    "H_ZERO", "H_BFS_HOPS", "H_MANHATTAN", "H_USER", "H_BFS_CAPPED", "H_EUCLID", "gen_geometric",
+    "euclid_rho_fp", "gen_random_chain", "gen_maze",
     "gen_updates", "gen_pairs", "read_graph_text", "write_graph_text", "read_ints_text",
     "write_ints_text", "read_updates_text", "write_updates_text", "Graph", "GPU_Graph",
-    "Dynamic_Graph", "GPU_Dynamic_Graph", "A_Star", "GPU_A_Star", "DynamicSearch",
+    "Dynamic_Graph", "GPU_Dynamic_Graph", "A_Star", "GPU_A_Star", "DynamicSearch", "Server",
 ]
 
 
@@ -154,6 +155,38 @@ def gen_updates(g: CSR, nbatches: int, per_batch: int, inserts_per_batch: int, w
     if rc:
         raise DdpError(rc, "ddp_gen_updates failed")
     return flag, u, v, w
+
+
+def gen_geometric(n: int, k: int = 6, side: int = 1 << 20, wscale: int = 1000, seed: int = 5005,
+                  threads: int = 0) -> CSR:
+    """Points uniform on an integer grid [0, side)^2, each joined both ways to
+    its k nearest neighbours; w = max(1, round(wscale * length / spacing)),
+    spacing = side / sqrt(n).  Returns a CSR with xy set."""
+    xy = np.empty(2 * n, np.int32)
+    off = np.empty(n + 1, np.int32)
+    col = np.empty(2 * k * n, np.int32)
+    w = np.empty(2 * k * n, np.uint32)
+    m = C.c_int64()
+    threads = threads or min(16, os.cpu_count() or 1)
+    rc = lib().ddp_gen_geometric(n, k, side, wscale, seed, threads, ptr(xy), ptr(off), ptr(col),
+                                 ptr(w, C.c_uint32), C.byref(m))
+    if rc:
+        raise DdpError(rc, "ddp_gen_geometric failed")
+    e = m.value
+    return CSR(n, off, col[:e].copy(), w[:e].copy(), xy=xy.reshape(n, 2))
+
+
+def euclid_rho_fp(g: CSR) -> int:
+    """Largest 16.16 fixed-point rho with rho <= w / length on every live arc
+    (minus one unit of slack), the scale of the Euclidean heuristic."""
+    live = g.col >= 0
+    src = np.repeat(np.arange(g.n), np.diff(g.off))[live]
+    dst = g.col[live]
+    d = g.xy[dst].astype(np.float64) - g.xy[src].astype(np.float64)
+    ln = np.sqrt((d * d).sum(1))
+    ok = ln > 0
+    rho = float((g.w[live][ok].astype(np.float64) / ln[ok]).min()) if ok.any() else 0.0
+    return max(0, int(np.floor(rho * 65536.0)) - 1)
 
 
 def gen_pairs(g: CSR, npairs: int, hop_lo: int, hop_hi: int, seed: int, bfs_cap_level: int = 6,
@@ -308,6 +341,9 @@ class DeviceGraph:
     def set_coords(self, xy) -> None:
         a = _i32(np.asarray(xy).reshape(-1))
         check(lib().ddp_graph_set_coords(self.handle, ptr(a)))
+
+    def set_euclid(self, rho_fp: int) -> None:
+        check(lib().ddp_graph_set_euclid(self.handle, int(rho_fp)))
 
     def info(self):
         n, e, lo, hi = C.c_int32(), C.c_int64(), C.c_uint32(), C.c_uint32()
@@ -470,6 +506,72 @@ class DynamicSearch:
     def close(self):
         if self.handle:
             lib().ddp_dyn_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching A* service on a resident graph (ddp_server)."""
+
+    def __init__(self, graph: DeviceGraph, hkind: int = H_EUCLID, max_requests: int = 1 << 20, **opts):
+        self.graph = graph
+        o = _opts(**opts)
+        h = C.c_void_p()
+        check(lib().ddp_serve_create(graph.handle, int(hkind), C.byref(o), int(max_requests), C.byref(h)))
+        self.handle = h
+
+    def submit(self, S, T) -> int:
+        S, T = _i32(S), _i32(T)
+        first = C.c_int64()
+        check(lib().ddp_serve_submit(self.handle, len(S), ptr(S), ptr(T), C.byref(first)))
+        return first.value
+
+    def poll(self, max_results: int = 1 << 16):
+        ids = np.empty(max_results, np.int64)
+        costs = np.empty(max_results, np.int32)
+        lat = np.empty(max_results, np.int64)
+        ver = np.empty(max_results, np.int32)
+        k = C.c_int32()
+        P = C.POINTER(C.c_int64)
+        check(lib().ddp_serve_poll(self.handle, max_results, ids.ctypes.data_as(P), ptr(costs),
+                                   lat.ctypes.data_as(P), ptr(ver), C.byref(k)))
+        n = k.value
+        return ids[:n], costs[:n], lat[:n], ver[:n]
+
+    def update(self, flag, u, v, w) -> None:
+        flag, u, v, w = _i32(flag), _i32(u), _i32(v), _u32(w)
+        check(lib().ddp_serve_update(self.handle, len(flag), ptr(flag), ptr(u), ptr(v), ptr(w, C.c_uint32)))
+
+    def stats(self) -> dict:
+        st = np.empty(6, np.int64)
+        check(lib().ddp_serve_stats(self.handle, st.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(zip(["submitted", "completed", "slots", "launches", "version", "reruns"], st.tolist()))
+
+    def drain(self, timeout_s: float = 60.0):
+        """Polls until every submitted request is back; returns them."""
+        import time as _t
+        out = [[], [], [], []]
+        t0 = _t.monotonic()
+        while True:
+            r = self.poll()
+            for i in range(4):
+                out[i].append(r[i])
+            st = self.stats()
+            if st["completed"] >= st["submitted"]:
+                break
+            if _t.monotonic() - t0 > timeout_s:
+                raise TimeoutError("serving drain timed out")
+            _t.sleep(0.0002)
+        return tuple(np.concatenate(x) for x in out)
+
+    def close(self):
+        if self.handle:
+            lib().ddp_serve_free(self.handle)
             self.handle = None
 
     def __del__(self):

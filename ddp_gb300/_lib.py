@@ -28,6 +28,7 @@ SIGNATURES = {
     "ddp_graph_from_csr": (C.c_int, [C.c_int32, C.c_int64, i32p, C.c_int32, i32p, u32p, C.POINTER(vp)]),
     "ddp_graph_load_text": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
     "ddp_graph_set_coords": (C.c_int, [vp, i32p]),
+    "ddp_graph_set_euclid": (C.c_int, [vp, C.c_uint32]),
     "ddp_graph_info": (C.c_int, [vp, i32p, i64p, u32p, u32p]),
     "ddp_graph_read_csr": (C.c_int, [vp, i32p, i32p, u32p]),
     "ddp_graph_free": (C.c_int, [vp]),
@@ -54,6 +55,12 @@ SIGNATURES = {
     "ddp_dyn_path": (C.c_int, [vp, i32p, C.c_int32, i32p]),
     "ddp_dyn_stats": (C.c_int, [vp, i64p]),
     "ddp_dyn_free": (C.c_int, [vp]),
+    "ddp_serve_create": (C.c_int, [vp, C.c_int32, C.POINTER(Opts), C.c_int64, C.POINTER(vp)]),
+    "ddp_serve_submit": (C.c_int, [vp, C.c_int32, i32p, i32p, i64p]),
+    "ddp_serve_poll": (C.c_int, [vp, C.c_int32, i64p, i32p, i64p, i32p, i32p]),
+    "ddp_serve_update": (C.c_int, [vp, C.c_int32, i32p, i32p, i32p, u32p]),
+    "ddp_serve_stats": (C.c_int, [vp, i64p]),
+    "ddp_serve_free": (C.c_int, [vp]),
     "ddp_bfs_hops_noalloc": (C.c_int, [C.c_int32, vp, vp, C.c_int32, vp, vp]),
     "ddp_io_read_graph_text": (C.c_int, [C.c_char_p, i32p, i64p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(u32p)]),
     "ddp_io_write_graph_text": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, i32p, i32p, u32p]),
@@ -69,6 +76,8 @@ SIGNATURES = {
                                u32p, i32p]),
     "ddp_gen_updates": (C.c_int, [C.c_int32, C.c_int64, i32p, i32p, u32p, i32p, C.c_int32, C.c_int32, C.c_int32,
                                   C.c_uint32, C.c_uint32, C.c_uint64, i32p, i32p, i32p, u32p]),
+    "ddp_gen_geometric": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_uint32, C.c_uint64, C.c_int32, i32p, i32p,
+                                    i32p, u32p, i64p]),
     "ddp_gen_pairs": (C.c_int, [C.c_int32, i32p, i32p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                 C.c_int32, i32p, i32p, i32p]),
 }

@@ -54,6 +54,7 @@ struct DevGraph {
     const uint2 *rarc;    // e   {tail, w}
     const int32_t *xy;    // 2n coordinates (may be null)
     uint32_t wmin;
+    uint32_t rho_fp;      // Euclidean heuristic scale, 16.16 fixed point
     // Arcs inserted by dynamic updates live in a second CSR (doff/darc)
     // until they are folded into the main one; null when absent.
     const int32_t *doff;  // n+1

@@ -56,6 +56,17 @@ struct DynMirror {
     std::vector<int64_t> dirty_arc, dirty_rarc;
     std::vector<int32_t> dirty_row, dirty_rrow;
     bool full = true;  // next upload sends everything
+    // device side: capacities of the arc arrays and scatter staging buffers
+    int64_t arc_cap = 0, rarc_cap = 0;
+    long long *d_slot = nullptr;
+    uint2 *d_val = nullptr;
+    int4 *d_rows = nullptr;
+    int64_t scat_cap = 0, rows_cap = 0;
+    ~DynMirror() {
+        cudaFree(d_slot);
+        cudaFree(d_val);
+        cudaFree(d_rows);
+    }
 };
 
 namespace ddp {
@@ -371,11 +382,6 @@ struct ddp_dyn {
     DynCtl *d_dc = nullptr;
     int4 *d_upd = nullptr;
     int32_t upd_cap = 0;
-    long long *d_slot = nullptr;
-    uint2 *d_val = nullptr;
-    int4 *d_rows = nullptr;
-    int64_t scat_cap = 0, rows_cap = 0;
-    int64_t arc_cap = 0, rarc_cap = 0;  // device capacities
     int32_t cost = DDP_INF;
     int32_t path_len = 0;
     int64_t stats[10] = {0};
@@ -384,22 +390,22 @@ struct ddp_dyn {
 
 namespace ddp {
 
-static int dyn_upload(ddp_dyn *d) {
-    ddp_graph *g = d->g;
+int dyn_upload(ddp_graph *g) {
     DynMirror *m = g->dyn;
+    DynMirror *d = m;  // device bookkeeping lives in the mirror
     const int32_t n = g->n;
     if (m->full) {
-        if ((int64_t)m->arc.size() > d->arc_cap) {
+        if ((int64_t)m->arc.size() > m->arc_cap) {
             cudaFree(g->d_arc);
             g->d_arc = nullptr;
             DDP_CUDA(cudaMalloc(&g->d_arc, sizeof(uint2) * m->arc.size()));
-            d->arc_cap = (int64_t)m->arc.size();
+            m->arc_cap = (int64_t)m->arc.size();
         }
-        if ((int64_t)m->rarc.size() > d->rarc_cap) {
+        if ((int64_t)m->rarc.size() > m->rarc_cap) {
             cudaFree(g->d_rarc);
             g->d_rarc = nullptr;
             DDP_CUDA(cudaMalloc(&g->d_rarc, sizeof(uint2) * m->rarc.size()));
-            d->rarc_cap = (int64_t)m->rarc.size();
+            m->rarc_cap = (int64_t)m->rarc.size();
         }
         DDP_CUDA(cudaMemcpy(g->d_arc, m->arc.data(), sizeof(uint2) * m->arc.size(), cudaMemcpyHostToDevice));
         DDP_CUDA(cudaMemcpy(g->d_rarc, m->rarc.data(), sizeof(uint2) * m->rarc.size(), cudaMemcpyHostToDevice));
@@ -504,35 +510,14 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
 
 }  // namespace ddp
 
-extern "C" {
 
-int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, const ddp_opts *opts,
-                   ddp_dyn **out) {
-    if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
-    *out = nullptr;
-    if (source < 0 || source >= g->n || target < 0 || target >= g->n)
-        return fail(DDP_ERR_INVALID, "source/target out of range");
-    if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS)
-        return fail(DDP_ERR_INVALID, "dynamic search heuristic must be ZERO or BFS_HOPS");
-    std::lock_guard<std::mutex> lk(g->mu);
-    if (g->dyn_active) return fail(DDP_ERR_INVALID, "graph already has a dynamic search");
+namespace ddp {
+
+// Switches g to the dynamic layout (rows with slack and explicit ends) and
+// builds its host mirror, once.
+int dyn_graph_prepare(ddp_graph *g) {
+    if (g->dyn) return DDP_OK;
     const int32_t n = g->n;
-    ddp_dyn *d = new ddp_dyn();
-    d->g = g;
-    d->s = source;
-    d->t = target;
-    d->hkind = hkind;
-    if (opts) d->o = *opts;
-    auto bail = [&](int rc) {
-        ddp_dyn_free(d);
-        return rc;
-    };
-    if (g->dyn) {
-        // the graph is already in the dynamic layout (an earlier search)
-        d->arc_cap = g->e;
-        d->rarc_cap = g->e_rev;
-    } else {
-    // host mirror from the device CSR
     std::vector<int32_t> off((size_t)n + 1), roff((size_t)n + 1);
     std::vector<uint2> arc((size_t)std::max<int64_t>(g->e, 1)), rarc((size_t)std::max<int64_t>(g->e_rev, 1));
     DDP_CUDA(cudaMemcpy(off.data(), g->d_off, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost));
@@ -548,61 +533,21 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     g->dyn = m;
     g->e = (int64_t)m->arc.size();
     g->e_rev = (int64_t)m->rarc.size();
-    d->arc_cap = 0;
-    d->rarc_cap = 0;
     workspace_release(g);  // the single-query workspace was sized for the old arrays
-    cudaError_t e0 = cudaMalloc(&g->d_oend, sizeof(int32_t) * n);
-    if (e0 == cudaSuccess) e0 = cudaMalloc(&g->d_roend, sizeof(int32_t) * n);
-    if (e0 != cudaSuccess) return bail(cuda_fail(e0, "cudaMalloc(row ends)"));
-    int rc0 = dyn_upload(d);
-    if (rc0) return bail(rc0);
-    }
-    g->dyn_active = true;
-    cudaError_t e1;
-    int rc;
-    // one search slot with generous queues (keep mode retains the open list)
-    const int64_t capq = (int64_t)n + 4096, capf = 2 * (int64_t)n + 4096;
-    rc = slots_alloc(d->sa, n, 1, capq, capf, false, g->stream);
-    if (rc) return bail(rc);
-    e1 = cudaMalloc(&d->d_inv, sizeof(int32_t) * n);
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_out, sizeof(int32_t) * 16);
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_path, sizeof(int32_t) * n);
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_dc, sizeof(DynCtl));
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_hops, sizeof(uint32_t) * n);
-    if (e1 != cudaSuccess) return bail(cuda_fail(e1, "cudaMalloc(dynamic state)"));
-    DDP_CUDA(cudaMemsetAsync(d->sa.ctl, 0, sizeof(SearchCtl), g->stream));
-    int per_sm = 0, sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dyn, 512, 0);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    d->grid = std::max(1, per_sm) * std::max(1, sms);
-    if (d->o.grid > 0 && d->o.grid < d->grid) d->grid = d->o.grid;
-    if (hkind == DDP_H_BFS_HOPS) {
-        // exact reverse BFS from the target into the dynamic hop array
-        ddp_heuristic *h = nullptr;
-        g->mu.unlock();
-        rc = ddp_heuristic_build(g, target, DDP_H_BFS_HOPS, nullptr, nullptr, &h);
-        g->mu.lock();
-        if (rc) return bail(rc);
-        cudaError_t ce = cudaMemcpy(d->d_hops, heuristic_hops_ptr(h), sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice);
-        ddp_heuristic_free(h);
-        if (ce != cudaSuccess) return bail(cuda_fail(ce, "hops copy"));
-    }
-    rc = dyn_launch(d, 1, 0);
-    if (rc) return bail(rc);
-    *out = d;
-    return DDP_OK;
+    if (!g->d_oend) DDP_CUDA(cudaMalloc(&g->d_oend, sizeof(int32_t) * n));
+    if (!g->d_roend) DDP_CUDA(cudaMalloc(&g->d_roend, sizeof(int32_t) * n));
+    return dyn_upload(g);
 }
 
-int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
-                   const uint32_t *w, int32_t *out_cost) {
-    if (!d || nupd < 0 || (nupd > 0 && (!flag || !u || !v || !w)))
-        return fail(DDP_ERR_INVALID, "bad update arguments");
-    ddp_graph *g = d->g;
-    std::lock_guard<std::mutex> lk(g->mu);
+// Applies one update batch to the mirror with the reference's semantics and
+// uploads the touched slots.  ups receives the search-relevant updates.
+int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
+                    const uint32_t *w, std::vector<int4> &ups) {
+    int rcp = dyn_graph_prepare(g);
+    if (rcp) return rcp;
     DynMirror *m = g->dyn;
     const int32_t n = g->n;
-    std::vector<int4> ups;
+    ups.clear();
     ups.reserve((size_t)nupd);
     // deletes and weight changes resolve against the pre-batch graph
     // (removeDelEdges runs before mergeDiff, DA_dyn_cpu.cu:1473-1484)
@@ -685,7 +630,81 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
         g->e = (int64_t)m->arc.size();
         g->e_rev = (int64_t)m->rarc.size();
     }
-    int rc = dyn_upload(d);
+    return dyn_upload(g);
+}
+
+}  // namespace ddp
+
+extern "C" {
+
+int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, const ddp_opts *opts,
+                   ddp_dyn **out) {
+    if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (source < 0 || source >= g->n || target < 0 || target >= g->n)
+        return fail(DDP_ERR_INVALID, "source/target out of range");
+    if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS)
+        return fail(DDP_ERR_INVALID, "dynamic search heuristic must be ZERO or BFS_HOPS");
+    std::lock_guard<std::mutex> lk(g->mu);
+    if (g->dyn_active) return fail(DDP_ERR_INVALID, "graph already has a dynamic search");
+    const int32_t n = g->n;
+    ddp_dyn *d = new ddp_dyn();
+    d->g = g;
+    d->s = source;
+    d->t = target;
+    d->hkind = hkind;
+    if (opts) d->o = *opts;
+    auto bail = [&](int rc) {
+        ddp_dyn_free(d);
+        return rc;
+    };
+    int rc0 = dyn_graph_prepare(g);
+    if (rc0) return bail(rc0);
+    g->dyn_active = true;
+    cudaError_t e1;
+    int rc;
+    // one search slot with generous queues (keep mode retains the open list)
+    const int64_t capq = (int64_t)n + 4096, capf = 2 * (int64_t)n + 4096;
+    rc = slots_alloc(d->sa, n, 1, capq, capf, false, g->stream);
+    if (rc) return bail(rc);
+    e1 = cudaMalloc(&d->d_inv, sizeof(int32_t) * n);
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_out, sizeof(int32_t) * 16);
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_path, sizeof(int32_t) * n);
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_dc, sizeof(DynCtl));
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_hops, sizeof(uint32_t) * n);
+    if (e1 != cudaSuccess) return bail(cuda_fail(e1, "cudaMalloc(dynamic state)"));
+    DDP_CUDA(cudaMemsetAsync(d->sa.ctl, 0, sizeof(SearchCtl), g->stream));
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dyn, 512, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    d->grid = std::max(1, per_sm) * std::max(1, sms);
+    if (d->o.grid > 0 && d->o.grid < d->grid) d->grid = d->o.grid;
+    if (hkind == DDP_H_BFS_HOPS) {
+        // exact reverse BFS from the target into the dynamic hop array
+        ddp_heuristic *h = nullptr;
+        g->mu.unlock();
+        rc = ddp_heuristic_build(g, target, DDP_H_BFS_HOPS, nullptr, nullptr, &h);
+        g->mu.lock();
+        if (rc) return bail(rc);
+        cudaError_t ce = cudaMemcpy(d->d_hops, heuristic_hops_ptr(h), sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice);
+        ddp_heuristic_free(h);
+        if (ce != cudaSuccess) return bail(cuda_fail(ce, "hops copy"));
+    }
+    rc = dyn_launch(d, 1, 0);
+    if (rc) return bail(rc);
+    *out = d;
+    return DDP_OK;
+}
+
+int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
+                   const uint32_t *w, int32_t *out_cost) {
+    if (!d || nupd < 0 || (nupd > 0 && (!flag || !u || !v || !w)))
+        return fail(DDP_ERR_INVALID, "bad update arguments");
+    ddp_graph *g = d->g;
+    std::lock_guard<std::mutex> lk(g->mu);
+    std::vector<int4> ups;
+    int rc = dyn_graph_apply(g, nupd, flag, u, v, w, ups);
     if (rc) return rc;
     const int32_t k = (int32_t)ups.size();
     if (k > d->upd_cap) {
@@ -730,9 +749,6 @@ int ddp_dyn_free(ddp_dyn *d) {
     cudaFree(d->d_path);
     cudaFree(d->d_dc);
     cudaFree(d->d_upd);
-    cudaFree(d->d_slot);
-    cudaFree(d->d_val);
-    cudaFree(d->d_rows);
     // the graph keeps its dynamic layout and mirror (other searches and
     // ddp_graph_read_csr see the updated graph)
     if (d->g) d->g->dyn_active = false;

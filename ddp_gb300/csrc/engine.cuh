@@ -145,6 +145,27 @@ struct HeurManhattan {
     }
 };
 
+// floor(sqrt(x)) for x < 2^62, exact: a float estimate, then integer fix-up
+__host__ __device__ __forceinline__ uint64_t isqrt_floor(uint64_t x) {
+    uint64_t r = (uint64_t)sqrt((double)x);
+    while (r * r > x) r--;
+    while ((r + 1) * (r + 1) <= x) r++;
+    return r;
+}
+
+struct HeurEuclid {  // floor(rho * floor(dist)), rho <= w / length on every arc
+    const int32_t *xy;
+    int32_t tx, ty;
+    uint32_t rho_fp;  // 16.16
+    __device__ uint32_t operator()(int32_t v) const {
+        int2 p = __ldg(reinterpret_cast<const int2 *>(xy) + v);
+        const int64_t dx = (int64_t)p.x - tx, dy = (int64_t)p.y - ty;
+        const uint64_t r = isqrt_floor((uint64_t)(dx * dx + dy * dy));
+        const uint64_t h = (r * rho_fp) >> 16;
+        return h >= INF_G ? INF_G - 1 : (uint32_t)h;
+    }
+};
+
 // ---- warp helpers ----------------------------------------------------------
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 

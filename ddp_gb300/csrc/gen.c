@@ -428,3 +428,188 @@ int ddp_gen_pairs(int32_t n, const int32_t *off, const int32_t *col, int32_t npa
     pthread_mutex_destroy(&c.mu);
     return 0;
 }
+
+/* ---------------- 2D geometric k-NN graph -------------------------------- */
+/* Points uniform on an integer grid [0, side)^2, each joined in both
+ * directions to its k nearest neighbours (ties by index), duplicates
+ * removed; w = max(1, round(wscale * length / spacing)) with
+ * spacing = side / sqrt(n), i.e. wscale per mean point spacing. */
+typedef struct {
+    int32_t n, k, side, gcells;
+    const int32_t *xy;
+    const int32_t *cell_start, *cell_pts;
+    int32_t *knn;
+    int32_t next;
+    pthread_mutex_t mu;
+} knn_ctx;
+
+static void *knn_worker(void *arg) {
+    knn_ctx *c = (knn_ctx *)arg;
+    const int32_t k = c->k, G = c->gcells;
+    int64_t *bd = (int64_t *)malloc(sizeof(int64_t) * (size_t)k);
+    int32_t *bi = (int32_t *)malloc(sizeof(int32_t) * (size_t)k);
+    const double csz = (double)c->side / G;
+    for (;;) {
+        pthread_mutex_lock(&c->mu);
+        int32_t start = c->next;
+        c->next += 4096;
+        pthread_mutex_unlock(&c->mu);
+        if (start >= c->n) break;
+        int32_t stop = start + 4096 < c->n ? start + 4096 : c->n;
+        for (int32_t p = start; p < stop; p++) {
+            const int64_t px = c->xy[2 * p], py = c->xy[2 * p + 1];
+            int32_t cx = (int32_t)(px / csz), cy = (int32_t)(py / csz);
+            if (cx >= G) cx = G - 1;
+            if (cy >= G) cy = G - 1;
+            int cnt = 0;
+            for (int r = 1;; r++) {
+                cnt = 0;
+                for (int32_t yy = cy - r; yy <= cy + r; yy++) {
+                    if (yy < 0 || yy >= G) continue;
+                    for (int32_t xx = cx - r; xx <= cx + r; xx++) {
+                        if (xx < 0 || xx >= G) continue;
+                        const int32_t cell = yy * G + xx;
+                        for (int32_t j = c->cell_start[cell]; j < c->cell_start[cell + 1]; j++) {
+                            const int32_t q = c->cell_pts[j];
+                            if (q == p) continue;
+                            const int64_t dx = c->xy[2 * q] - px, dy = c->xy[2 * q + 1] - py;
+                            const int64_t d = dx * dx + dy * dy;
+                            /* insertion into the sorted top-k (distance, index) */
+                            if (cnt < k || d < bd[cnt - 1] || (d == bd[cnt - 1] && q < bi[cnt - 1])) {
+                                int pos = cnt < k ? cnt++ : k - 1;
+                                while (pos > 0 && (bd[pos - 1] > d || (bd[pos - 1] == d && bi[pos - 1] > q))) {
+                                    bd[pos] = bd[pos - 1];
+                                    bi[pos] = bi[pos - 1];
+                                    pos--;
+                                }
+                                bd[pos] = d;
+                                bi[pos] = q;
+                            }
+                        }
+                    }
+                }
+                /* the ring of radius r covers every point within r*csz */
+                const double reach = r * csz;
+                if (cnt == k && (double)bd[k - 1] < reach * reach) break;
+                if (r > G) break;
+            }
+            for (int i = 0; i < k; i++) c->knn[(size_t)p * k + i] = i < cnt ? bi[i] : -1;
+        }
+    }
+    free(bd);
+    free(bi);
+    return NULL;
+}
+
+int ddp_gen_geometric(int32_t n, int32_t k, int32_t side, uint32_t wscale, uint64_t seed, int32_t threads,
+                      int32_t *xy, int32_t *off, int32_t *col, uint32_t *w, int64_t *n_arcs) {
+    if (n < 2 || k < 1 || k >= n || side < 2) return -1;
+    rng_t r;
+    rng_seed(&r, seed, 5);
+    for (int32_t i = 0; i < n; i++) {
+        xy[2 * i] = (int32_t)rng_below(&r, (uint64_t)side);
+        xy[2 * i + 1] = (int32_t)rng_below(&r, (uint64_t)side);
+    }
+    /* grid buckets, about 2 points per cell */
+    int32_t G = (int32_t)sqrt((double)n / 2.0);
+    if (G < 1) G = 1;
+    const double csz = (double)side / G;
+    int32_t *cs = (int32_t *)calloc((size_t)G * G + 1, sizeof(int32_t));
+    int32_t *cp = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t *cellof = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t *knn = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * k);
+    if (!cs || !cp || !cellof || !knn) {
+        free(cs);
+        free(cp);
+        free(cellof);
+        free(knn);
+        return -2;
+    }
+    for (int32_t i = 0; i < n; i++) {
+        int32_t cx = (int32_t)(xy[2 * i] / csz), cy = (int32_t)(xy[2 * i + 1] / csz);
+        if (cx >= G) cx = G - 1;
+        if (cy >= G) cy = G - 1;
+        cellof[i] = cy * G + cx;
+        cs[cellof[i] + 1]++;
+    }
+    for (int64_t c2 = 0; c2 < (int64_t)G * G; c2++) cs[c2 + 1] += cs[c2];
+    {
+        int32_t *fill = (int32_t *)malloc(sizeof(int32_t) * (size_t)G * G);
+        memcpy(fill, cs, sizeof(int32_t) * (size_t)G * G);
+        for (int32_t i = 0; i < n; i++) cp[fill[cellof[i]]++] = i;
+        free(fill);
+    }
+    knn_ctx c;
+    c.n = n;
+    c.k = k;
+    c.side = side;
+    c.gcells = G;
+    c.xy = xy;
+    c.cell_start = cs;
+    c.cell_pts = cp;
+    c.knn = knn;
+    c.next = 0;
+    pthread_mutex_init(&c.mu, NULL);
+    if (threads < 1) threads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, knn_worker, &c);
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&c.mu);
+    /* symmetric rows: kNN(u) plus every v with u in kNN(v), sorted, unique */
+    int32_t *deg = (int32_t *)calloc((size_t)n + 1, sizeof(int32_t));
+    for (int64_t i = 0; i < (int64_t)n * k; i++)
+        if (knn[i] >= 0) deg[knn[i] + 1]++;
+    for (int32_t i = 0; i < n; i++) deg[i + 1] += deg[i];
+    int32_t *rev = (int32_t *)malloc(sizeof(int32_t) * (size_t)(deg[n] > 0 ? deg[n] : 1));
+    {
+        int32_t *fill = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+        memcpy(fill, deg, sizeof(int32_t) * (size_t)n);
+        for (int32_t u = 0; u < n; u++)
+            for (int j = 0; j < k; j++) {
+                int32_t v = knn[(size_t)u * k + j];
+                if (v >= 0) rev[fill[v]++] = u;
+            }
+        free(fill);
+    }
+    const double spacing = (double)side / sqrt((double)n);
+    int64_t m = 0;
+    int32_t tmp[256];
+    for (int32_t u = 0; u < n; u++) {
+        off[u] = (int32_t)m;
+        int t = 0;
+        for (int j = 0; j < k; j++)
+            if (knn[(size_t)u * k + j] >= 0 && t < 256) tmp[t++] = knn[(size_t)u * k + j];
+        for (int32_t j = deg[u]; j < deg[u + 1] && t < 256; j++) tmp[t++] = rev[j];
+        /* sort + unique (rows are short) */
+        for (int a = 1; a < t; a++) {
+            int32_t x = tmp[a];
+            int b = a - 1;
+            while (b >= 0 && tmp[b] > x) {
+                tmp[b + 1] = tmp[b];
+                b--;
+            }
+            tmp[b + 1] = x;
+        }
+        for (int a = 0; a < t; a++) {
+            if (a > 0 && tmp[a] == tmp[a - 1]) continue;
+            const int32_t v = tmp[a];
+            const double dx = (double)xy[2 * v] - xy[2 * u], dy = (double)xy[2 * v + 1] - xy[2 * u + 1];
+            const double len = sqrt(dx * dx + dy * dy);
+            double ww = floor(wscale * len / spacing + 0.5);
+            if (ww < 1) ww = 1;
+            col[m] = v;
+            w[m] = (uint32_t)ww;
+            m++;
+        }
+    }
+    off[n] = (int32_t)m;
+    *n_arcs = m;
+    free(cs);
+    free(cp);
+    free(cellof);
+    free(knn);
+    free(deg);
+    free(rev);
+    return 0;
+}

@@ -39,6 +39,7 @@ DevGraph graph_view(const ddp_graph *g) {
     d.rarc = g->d_rarc;
     d.xy = g->d_xy;
     d.wmin = g->wmin;
+    d.rho_fp = g->rho_fp;
     d.doff = g->d_doff;
     d.darc = g->d_darc;
     d.droff = g->d_droff;
@@ -203,6 +204,13 @@ int ddp_graph_set_coords(ddp_graph *g, const int32_t *xy) {
     if (!g->d_xy) DDP_CUDA(cudaMalloc(&g->d_xy, sizeof(int32_t) * 2 * (size_t)g->n));
     DDP_CUDA(cudaMemcpy(g->d_xy, xy, sizeof(int32_t) * 2 * (size_t)g->n, cudaMemcpyHostToDevice));
     g->h_xy.assign(xy, xy + 2 * (size_t)g->n);
+    return DDP_OK;
+}
+
+int ddp_graph_set_euclid(ddp_graph *g, uint32_t rho_fp) {
+    if (!g) return fail(DDP_ERR_INVALID, "null graph");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->rho_fp = rho_fp;
     return DDP_OK;
 }
 

@@ -16,6 +16,7 @@ struct ddp_graph {
     int64_t e = 0;      // arcs in the main CSR (dead ones included)
     int64_t e_rev = 0;  // arcs in the reverse CSR
     uint32_t wmin = 0, wmax = 0;
+    uint32_t rho_fp = 0;  // Euclidean heuristic scale (16.16)
     int32_t *d_off = nullptr;
     uint2 *d_arc = nullptr;
     int32_t *d_roff = nullptr;
@@ -43,4 +44,6 @@ void workspace_release(ddp_graph *g);
 void dyn_mirror_free(DynMirror *m);
 int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights);
 int64_t dyn_live_arcs(const ddp_graph *g);
+int dyn_upload(ddp_graph *g);
+int dyn_graph_prepare(ddp_graph *g);
 }  // namespace ddp

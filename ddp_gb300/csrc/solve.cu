@@ -134,7 +134,30 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
     long long t0 = 0;
     for (;;) {
         if (grp.rank() == 0) {
-            const int q = atomicAdd(A.work, 1);
+            int q;
+            if (A.serve) {
+                // claim the next published request; leave when paused or
+                // after idle_limit empty polls
+                q = -1;
+                for (int idle = 0; idle <= A.idle_limit;) {
+                    if (*A.pause) break;
+                    const int p = *A.pub;
+                    const int c = *(volatile int *)A.work;
+                    if (c < p) {
+                        if (atomicCAS(A.work, c, c + 1) == c) {
+                            q = c;
+                            break;
+                        }
+                        continue;
+                    }
+                    idle++;
+                    __nanosleep(1000);
+                }
+                __threadfence_system();  // requests were written before pub
+                if (q < 0) q = A.nq;     // exit marker
+            } else {
+                q = atomicAdd(A.work, 1);
+            }
             ctl->cur_q = q;
             ctl->status = 0;
             ctl->bfs_reached = 0;
@@ -151,12 +174,20 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
         grp.sync();
         const int q = *(volatile int *)&ctl->cur_q;
         if (q >= A.nq) break;
-        const int32_t s = __ldg(A.S + q), t = __ldg(A.T + q);
+        // serving requests live in host memory written while the kernel
+        // runs: read them uncached
+        const int32_t s = A.serve ? *(const volatile int32_t *)(A.S + q) : __ldg(A.S + q);
+        const int32_t t = A.serve ? *(const volatile int32_t *)(A.T + q) : __ldg(A.T + q);
         if (s < 0 || s >= G.n || t < 0 || t >= G.n) {
             if (grp.rank() == 0) {
                 A.cost[q] = DDP_INF;
                 if (A.plen) A.plen[q] = -1;
                 if (A.qstatus) A.qstatus[q] = -1;
+                if (A.serve) {
+                    A.ver[q] = A.version;
+                    __threadfence_system();
+                    A.done[q] = 1;
+                }
             }
             grp.sync();
             continue;
@@ -170,6 +201,9 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
         } else if (HK == 2) {
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
             r = run_search(grp, G, B, HeurManhattan{G.xy, tp.x, tp.y, G.wmin}, P, wrows);
+        } else if (HK == 3) {
+            int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
+            r = run_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows);
         } else {
             r = run_search(grp, G, B, HeurZero{}, P, wrows);
         }
@@ -184,6 +218,11 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
                                                            : (int32_t)r.cost;
             if (A.plen) A.plen[q] = len;
             if (A.qstatus) A.qstatus[q] = ctl->status;
+            if (A.serve) {
+                A.ver[q] = A.version;
+                __threadfence_system();
+                A.done[q] = 1;
+            }
             if (A.stats) {
                 long long *st6 = A.stats + DDP_STATS * (size_t)q;
                 st6[0] = (long long)ctl->expanded;
@@ -251,6 +290,30 @@ static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CA
 // Nodes a capped heuristic BFS reaches before it stops (at the end of the
 // level that crosses this count).
 int64_t bfs_budget(int32_t n) { return std::max<int64_t>(4096, (int64_t)n / 32); }
+
+// Launches the persistent slot kernel for heuristic kind `hkind`.
+cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
+                         cudaStream_t st) {
+    void *args[] = {&G, &sa, &A};
+    const void *fn = is_bfs_kind(hkind)           ? (const void *)k_batch<1>
+                     : (hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
+                     : (hkind == DDP_H_EUCLID)    ? (const void *)k_batch<3>
+                                                  : (const void *)k_batch<0>;
+    if (coop) return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, st);
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st);
+}
+
+int slots_per_sm(int hkind, int block) {
+    int per_sm = 0;
+    const void *fn = is_bfs_kind(hkind)           ? (const void *)k_batch<1>
+                     : (hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
+                     : (hkind == DDP_H_EUCLID)    ? (const void *)k_batch<3>
+                                                  : (const void *)k_batch<0>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
+    return per_sm;
+}
+
+int device_sms() { return sm_count(); }
 
 uint32_t auto_delta(const ddp_graph *g) {
     // bucket width ~ a typical arc weight: wide enough for parallel buckets,
@@ -399,6 +462,22 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
             }
         break;
     }
+    case DDP_H_EUCLID: {
+        if (!g->d_xy) {
+            delete h;
+            return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
+        }
+        h->tx = g->h_xy[2 * (size_t)target];
+        h->ty = g->h_xy[2 * (size_t)target + 1];
+        if (out_h)
+            for (int32_t i = 0; i < g->n; i++) {
+                const int64_t dx = (int64_t)g->h_xy[2 * (size_t)i] - h->tx;
+                const int64_t dy = (int64_t)g->h_xy[2 * (size_t)i + 1] - h->ty;
+                const uint64_t r = isqrt_floor((uint64_t)(dx * dx + dy * dy));
+                out_h[i] = (int32_t)std::min<uint64_t>((r * g->rho_fp) >> 16, INT32_MAX - 1);
+            }
+        break;
+    }
     case DDP_H_USER: {
         if (!user_h) {
             delete h;
@@ -464,6 +543,11 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             int grid = coop_grid(k_solve_single<HeurManhattan>, block, o.grid);
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurManhattan>, grid, block, args, st);
+        } else if (kind == DDP_H_EUCLID) {
+            HeurEuclid H{g->d_xy, h->tx, h->ty, g->rho_fp};
+            int grid = coop_grid(k_solve_single<HeurEuclid>, block, o.grid);
+            void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
+            e = coop_launch(k_solve_single<HeurEuclid>, grid, block, args, st);
         } else if (kind == DDP_H_USER) {
             HeurArray H{h->d_h};
             int grid = coop_grid(k_solve_single<HeurArray>, block, o.grid);
@@ -613,6 +697,13 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     A.status = b->d_status;
     A.delta = b->o.delta > 0 ? (uint32_t)b->o.delta : auto_delta(b->g);
     A.bfs_budget = b->hkind == DDP_H_BFS_CAPPED ? bfs_budget(b->g->n) : 0;
+    A.serve = 0;
+    A.pub = nullptr;
+    A.pause = nullptr;
+    A.idle_limit = 0;
+    A.done = nullptr;
+    A.ver = nullptr;
+    A.version = 0;
     A.K = b->o.K;
     A.group = b->group;
     DevGraph G = graph_view(b->g);
@@ -626,6 +717,7 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     void *args[] = {&G, &sa, &A};
     const void *fn = is_bfs_kind(b->hkind)           ? (const void *)k_batch<1>
                      : (b->hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
+                     : (b->hkind == DDP_H_EUCLID)    ? (const void *)k_batch<3>
                                                      : (const void *)k_batch<0>;
     if (b->group > 1)
         return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
@@ -639,9 +731,9 @@ extern "C" {
 int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out) {
     if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN)
-        return fail(DDP_ERR_INVALID, "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED or MANHATTAN");
-    if (hkind == DDP_H_MANHATTAN && !g->d_xy)
+    if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN && hkind != DDP_H_EUCLID)
+        return fail(DDP_ERR_INVALID, "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED, MANHATTAN or EUCLID");
+    if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID) && !g->d_xy)
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_batch *b = new ddp_batch();
     b->g = g;
@@ -661,6 +753,8 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, b->block, 0);
     else if (hkind == DDP_H_MANHATTAN)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, b->block, 0);
+    else if (hkind == DDP_H_EUCLID)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<3>, b->block, 0);
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<0>, b->block, 0);
     b->group = std::max(1, b->o.group);

@@ -33,6 +33,15 @@ struct BatchArgs {
     int32_t K;
     int64_t bfs_budget;  // capped heuristic BFS (0 = run to completion)
     int group;           // CTAs per query slot
+    // serving mode (continuous batching): requests are published in host
+    // memory mapped into the device; slots wait for them
+    int serve;
+    const volatile int *pub;    // published request count
+    const volatile int *pause;  // non-zero: stop claiming, exit
+    int idle_limit;             // polls (~1 us each) before an idle slot exits
+    volatile int *done;         // per request: 1 once cost/ver are written
+    int32_t *ver;               // per request: graph version it ran on
+    int version;
 };
 
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops);
@@ -40,5 +49,11 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
                 cudaStream_t st);
 void slots_free(SlotArrays &sa);
 uint32_t *heuristic_hops_ptr(const ddp_heuristic *h);
+cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
+                         cudaStream_t st);
+int slots_per_sm(int hkind, int block);
+int device_sms();
+uint32_t auto_delta(const ddp_graph *g);
+int64_t bfs_budget(int32_t n);
 
 }  // namespace ddp

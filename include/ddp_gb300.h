@@ -54,6 +54,9 @@ enum ddp_heuristic_kind {
                             DA_star/genOpCSR.cpp); unreachable -> pruned      */
     DDP_H_MANHATTAN = 2, /* |dx| + |dy| on node coordinates x min arc weight   */
     DDP_H_USER = 3,      /* caller-supplied array (a_star.h:34 set_huiristics) */
+    DDP_H_EUCLID = 5,    /* floor(rho * floor(|xy(v) - xy(t)|)), rho a 16.16
+                            fixed-point lower bound of w / length over the arcs
+                            (ddp_graph_set_euclid); integer arithmetic only    */
     DDP_H_BFS_CAPPED = 4 /* DDP_H_BFS_HOPS with the BFS stopped after the level
                             where it has reached max(4096, n/32) nodes; nodes
                             not reached get (last level + 1) x min weight,
@@ -95,6 +98,9 @@ int ddp_graph_from_csr(int32_t n, int64_t e, const int32_t *offsets, int32_t off
 int ddp_graph_load_text(const char *path, ddp_graph **out);
 /* Node coordinates (x,y interleaved, 2n int32) for the Manhattan heuristic. */
 int ddp_graph_set_coords(ddp_graph *g, const int32_t *xy);
+/* 16.16 fixed-point scale of the Euclidean heuristic: rho_fp / 65536 must not
+ * exceed w / length for any arc (length measured in coordinate units). */
+int ddp_graph_set_euclid(ddp_graph *g, uint32_t rho_fp);
 int ddp_graph_info(const ddp_graph *g, int32_t *n, int64_t *e, uint32_t *wmin, uint32_t *wmax);
 /* Copies the current forward CSR back (offsets n+1, cols/weights e). */
 int ddp_graph_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights);
@@ -184,6 +190,30 @@ int ddp_dyn_path(ddp_dyn *d, int32_t *buf, int32_t cap, int32_t *len);
 int ddp_dyn_stats(const ddp_dyn *d, int64_t *stats);
 int ddp_dyn_free(ddp_dyn *d);
 
+/* ---- serving: continuous batching with interleaved updates (no reference
+ *      counterpart: the reference answers one (s,t) per process) --------- */
+typedef struct ddp_server ddp_server;
+/* Slots (one CTA each, fixed queue/state footprint; as many as fit in half of
+ * free device memory) serve requests published in a ring of max_requests
+ * entries in pinned host memory mapped into the device. */
+int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t max_requests,
+                     ddp_server **out);
+/* Publishes n requests; *first_id = id of the first.  Non-blocking. */
+int ddp_serve_submit(ddp_server *s, int32_t n, const int32_t *sources, const int32_t *targets,
+                     int64_t *first_id);
+/* Collects up to max finished requests: id, cost (DDP_INF = unreachable),
+ * host-observed latency (submit to this poll) and graph version.  Any array
+ * may be NULL.  Non-blocking except for rare re-runs of oversized searches. */
+int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int64_t *latency_ns,
+                   int32_t *versions, int32_t *nout);
+/* Applies an update batch (ddp_dyn_update flags) between requests: claiming
+ * pauses, running searches finish, the graph changes, the version bumps. */
+int ddp_serve_update(ddp_server *s, int32_t n, const int32_t *flag, const int32_t *u, const int32_t *v,
+                     const uint32_t *w);
+/* submitted, completed, slots, kernel launches, graph version, re-runs */
+int ddp_serve_stats(const ddp_server *s, int64_t *stats6);
+int ddp_serve_free(ddp_server *s);
+
 /* ---- reverse-BFS hop counts without device allocation ------------------
  * No counterpart in the reference.  For callers that cannot let a library
  * call cudaMalloc (for example a service that gives all device memory to its
@@ -234,6 +264,11 @@ int ddp_gen_updates(int32_t n, int64_t e, const int32_t *off, const int32_t *col
                     const int32_t *protect_next, int32_t nbatches, int32_t per_batch,
                     int32_t inserts_per_batch, uint32_t wmin, uint32_t wmax, uint64_t seed,
                     int32_t *flag, int32_t *uu, int32_t *vv, uint32_t *ww);
+/* Points uniform on [0, side)^2 (xy, 2n int32), each joined both ways to its
+ * k nearest neighbours, w = max(1, round(wscale * length / spacing)) with
+ * spacing = side / sqrt(n).  off has n+1 entries; col/w hold at most 2kn arcs. */
+int ddp_gen_geometric(int32_t n, int32_t k, int32_t side, uint32_t wscale, uint64_t seed, int32_t threads,
+                      int32_t *xy, int32_t *off, int32_t *col, uint32_t *w, int64_t *n_arcs);
 int ddp_gen_pairs(int32_t n, const int32_t *off, const int32_t *col, int32_t npairs, int32_t hop_lo,
                   int32_t hop_hi, int32_t bfs_cap_level, uint64_t seed, int32_t threads, int32_t *S,
                   int32_t *T, int32_t *want_hops);

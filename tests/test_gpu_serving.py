@@ -1,0 +1,103 @@
+"""Serving (continuous batching with interleaved updates): every answer is
+exact for the graph version it ran on, each request gives the same answer
+alone and in the mix, and updates between requests are applied."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _geo(d, n, seed):
+    g = d.gen_geometric(n, 6, 1 << 20, 1000, seed, 4)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.set_euclid(d.euclid_rho_fp(g))
+    return g, dg
+
+
+def _oracle(O, g, s, t, rho_fp):
+    n = g.n
+    dx = g.xy[:, 0].astype(np.int64) - g.xy[t, 0]
+    dy = g.xy[:, 1].astype(np.int64) - g.xy[t, 1]
+    r = np.floor(np.sqrt((dx * dx + dy * dy).astype(np.float64))).astype(np.int64)
+    # exact floor sqrt
+    r -= (r * r > dx * dx + dy * dy)
+    r += ((r + 1) * (r + 1) <= dx * dx + dy * dy)
+    h = ((r * rho_fp) >> 16).astype(np.int32)
+    gs = g.with_sentinel()
+    hh = np.concatenate([h, [0]]).astype(np.int32)
+    f, c, _, _, _ = O.astar(gs.n, gs.off[:-1], gs.col, gs.w, hh, s, t)
+    return c if f else 2147483647
+
+
+def test_serving_mix_equals_alone_and_oracle(gpu, oracle):
+    d = gpu
+    g, dg = _geo(d, 50_000, 31)
+    rho = d.euclid_rho_fp(g)
+    srv = d.Server(dg, d.H_EUCLID, max_requests=4096, grid=64)
+    rng = np.random.default_rng(1)
+    S = rng.integers(0, g.n, 300).astype(np.int32)
+    T = rng.integers(0, g.n, 300).astype(np.int32)
+    # arrivals in waves while earlier requests are still running
+    for i in range(0, 300, 50):
+        srv.submit(S[i:i + 50], T[i:i + 50])
+        time.sleep(0.001)
+    ids, costs, lat, ver = srv.drain()
+    order = np.argsort(ids)
+    ids, costs = ids[order], costs[order]
+    assert ids.tolist() == list(range(300))
+    for i in range(0, 300, 23):
+        h = dg.heuristic(int(T[i]), d.H_EUCLID)
+        alone = dg.solve(int(S[i]), int(T[i]), h).cost
+        h.close()
+        assert costs[i] == alone == _oracle(oracle, g, int(S[i]), int(T[i]), rho), i
+    st = srv.stats()
+    assert st["completed"] == 300 and st["slots"] >= 1
+    srv.close()
+
+
+def test_serving_with_updates(gpu, oracle):
+    """Weight changes, deletes and inserts between requests: each answer
+    equals the oracle on the graph version it reports."""
+    d = gpu
+    g, dg = _geo(d, 20_000, 41)
+    srv = d.Server(dg, d.H_EUCLID, max_requests=4096, grid=32)
+    rng = np.random.default_rng(5)
+    versions = [(g.off.copy(), g.col.copy(), g.w.copy(), d.euclid_rho_fp(g))]
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    submitted = []
+    for rnd in range(4):
+        S = rng.integers(0, g.n, 40).astype(np.int32)
+        T = rng.integers(0, g.n, 40).astype(np.int32)
+        srv.submit(S, T)
+        submitted += list(zip(S.tolist(), T.tolist()))
+        # an update batch: 30 weight changes x[0.5,2], 5 deletes, 5 inserts between neighbours
+        src = np.repeat(np.arange(len(off)), np.diff(np.append(off, len(col))))
+        live = np.flatnonzero(col >= 0)
+        pick = rng.choice(live, 40, replace=False)
+        fl, uu, vv, ww = [], [], [], []
+        for j in pick[:30]:
+            fl.append(2); uu.append(int(src[j])); vv.append(int(col[j]))
+            ww.append(max(1, int(round(w[j] * rng.uniform(0.5, 2.0)))))
+        for j in pick[30:35]:
+            fl.append(0); uu.append(int(src[j])); vv.append(int(col[j])); ww.append(0)
+        for j in pick[35:40]:
+            a, b = int(col[j]), int(src[j])
+            fl.append(1); uu.append(a); vv.append(b); ww.append(int(w[j]))
+        srv.update(fl, uu, vv, ww)
+        off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, uu, vv, ww)
+        gg = d.CSR(g.n, np.append(off, len(col)).astype(np.int32), col, w, xy=g.xy)
+        versions.append((gg.off, gg.col, gg.w, d.euclid_rho_fp(gg)))
+    ids, costs, lat, ver = srv.drain()
+    assert len(ids) == len(submitted)
+    for k in range(0, len(ids), 7):
+        i = int(ids[k])
+        s_, t_ = submitted[i]
+        vo, vc, vw, vrho = versions[int(ver[k])]
+        # the server's scale is a lower bound of every version's own rho
+        gv = d.CSR(g.n, vo, vc, vw, xy=g.xy)
+        want = _oracle(oracle, gv, s_, t_, 0)  # h = 0: the cost does not depend on h
+        assert costs[k] == want, (i, int(ver[k]))
+    assert srv.stats()["version"] == 4
+    srv.close()
