@@ -274,10 +274,13 @@ def write_updates_text(path: str, batches) -> None:
 
 # ---------------------------------------------------------------------------
 # device objects
-def _opts(K=0, delta=0, block=0, grid=0, queue_cap=0, stream=None, group=0) -> Opts:
+OPT_SYNC, OPT_ONE_CTA = 1, 2
+
+
+def _opts(K=0, delta=0, block=0, grid=0, queue_cap=0, stream=None, group=0, flags=0) -> Opts:
     """stream: a cudaStream_t as an int (e.g. torch's stream.cuda_stream);
-    group: CTAs per query slot in the batch engine."""
-    return Opts(int(K), int(delta), int(block), int(grid), int(queue_cap), stream or None, int(group), 0)
+    group: CTAs per query slot in the batch engine; flags: OPT_* bits."""
+    return Opts(int(K), int(delta), int(block), int(grid), int(queue_cap), stream or None, int(group), int(flags))
 
 
 @dataclass

@@ -17,7 +17,7 @@ vp = C.c_void_p
 
 class Opts(C.Structure):
     _fields_ = [("K", C.c_int32), ("delta", C.c_int32), ("block", C.c_int32), ("grid", C.c_int32),
-                ("queue_cap", C.c_int64), ("stream", C.c_void_p), ("group", C.c_int32), ("reserved", C.c_int32)]
+                ("queue_cap", C.c_int64), ("stream", C.c_void_p), ("group", C.c_int32), ("flags", C.c_int32)]
 
 
 # name -> (restype, argtypes)

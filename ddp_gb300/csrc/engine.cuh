@@ -625,14 +625,16 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
 //   L+1 hops away), so min(hops, cap) x wmin stays admissible and consistent.
 template <class Grp>
 __device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBufs &B, int32_t t,
-                                 WarpRows *wrows, uint32_t tag, int64_t budget) {
+                                 WarpRows *wrows, uint32_t tag, int64_t budget, bool spare_q0 = false) {
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     WarpRows &wr = wrows[threadIdx.x >> 5];
     const bool has_diff = G.doff != nullptr;
-    int *fa = reinterpret_cast<int *>(B.q0);
+    // frontier ping-pong: the two near queues, or (when q0 is the
+    // asynchronous ring that must stay clean) q1 and the second far pile
+    int *fa = reinterpret_cast<int *>(spare_q0 ? B.f1 : B.q0);
     int *fb = reinterpret_cast<int *>(B.q1);
-    const int64_t capf = B.cap_q * 2;  // uint2 slots reused as ints
+    const int64_t capf = 2 * (spare_q0 ? min(B.cap_q, B.cap_f) : B.cap_q);  // uint2 slots reused as ints
     const uint32_t max_lvl = tag ? 254u : 0xFFFFFFF0u;
 
     if (!tag)

@@ -1,0 +1,378 @@
+// Asynchronous single-CTA A*: the search of one query by one CTA without a
+// barrier per expansion wave.
+//
+// The phase-synchronous engine (engine.cuh, run_search) advances the search
+// frontier by one arc per barrier; a narrow search with a good heuristic
+// (grid mazes, geometric graphs) then costs one barrier round per hop of the
+// path.  Here the current bucket (entries with f < T) is a work pool that
+// warps drain and refill concurrently:
+//   * a warp first continues on its own children (up to 64 entries staged in
+//     shared memory: depth-first chasing of the frontier with no queue round
+//     trip), and spills to a ring in global memory that any warp may claim
+//     from;
+//   * a `pending` counter in shared memory counts entries pushed and not yet
+//     retired; children are counted before their parent retires, so
+//     pending == 0 means the bucket is empty and no warp is working on it;
+//   * ring slots hold {node, g} with node = 0xFFFFFFFF meaning "not written
+//     yet"; a claimer waits (bounded) for a reserved slot to be written and
+//     clears it after reading, so the ring is clean for the next bucket.
+// Between buckets the CTA synchronises once and splits the far pile at the
+// next threshold exactly as run_search does.  Stale entries (g changed since
+// the push) and entries with f >= f(t) are dropped; keep mode retains them in
+// the far pile, as in run_search.
+#pragma once
+
+#include "engine.cuh"
+
+namespace ddp {
+
+constexpr uint32_t RING_EMPTY = 0xFFFFFFFFu;
+
+struct CtaQ {
+    int head, tail;      // ring positions of the current bucket
+    int pending;         // entries pushed to the bucket and not yet retired
+    int far_cnt;         // far pushes appended this bucket
+    int alt_cnt;         // split: far entries kept
+    unsigned int minf;   // split: min f kept
+    int status;
+    int pad;
+};
+
+// Reserves k ring slots (lane 0 only); returns the first position or -1 when
+// the ring would overflow (the caller then sends the entries to far).
+__device__ __forceinline__ int ring_reserve(CtaQ *sq, int k, int cap) {
+    for (;;) {
+        const int t = *(volatile int *)&sq->tail;
+        if (t + k > cap) return -1;
+        if (atomicCAS(&sq->tail, t, t + k) == t) return t;
+    }
+}
+
+template <class Heur>
+__device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, const Heur &H, const SearchParams &P,
+                                       WarpRows *wrows, CtaQ *sq) {
+    SearchCtl *ctl = B.ctl;
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    WarpRows &wr = wrows[warp];
+    uint2 *ring = B.q0;
+    const int cap = (int)min(B.cap_q, (int64_t)0x3FFFFFFF);
+
+    if (threadIdx.x == 0) {
+        ctl->iters = 0;
+        ctl->expanded = ctl->scanned = ctl->relaxed = 0;
+        ctl->far_scanned = 0;
+        sq->head = 0;
+        sq->tail = 0;
+        sq->pending = 0;
+        sq->far_cnt = 0;
+        sq->alt_cnt = 0;
+        sq->minf = 0xFFFFFFFFu;
+        sq->status = 0;
+        if (!P.resume) {
+            ctl->touched = 1;
+            B.state[P.s] = st_make(0, -1);
+            B.touched[0] = P.s;
+            ring[0] = make_uint2((uint32_t)P.s, 0u);
+            sq->tail = 1;
+            sq->pending = 1;
+        }
+    }
+    const int64_t far_resume = P.resume ? (int64_t)(*(volatile int *)&ctl->far_n) : 0;
+    const bool far_in_f1 = P.resume && (*(volatile int *)&ctl->far_sel) != 0;
+    __syncthreads();
+
+    uint2 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
+    int64_t nfar = far_resume;
+    uint32_t T = sat_add(H(P.s), P.delta);
+    uint32_t Tsplit = T;
+    bool do_expand = !P.resume;
+    if (P.resume) T = Tsplit = 0;
+    unsigned long long n_exp = 0, n_scan = 0, n_rel = 0;
+    int phases = 0;
+    const int64_t max_phases = 4 * (int64_t)G.n + (1 << 22);
+
+    for (;;) {
+        if (do_expand) {
+            // ---- drain the bucket asynchronously -----------------------
+            int c_f = 0, c_t = 0, c_loc = 0;  // staged far pushes, touches, own children
+            for (;;) {
+                const uint64_t st_t = __ldcg(B.state + P.t);
+                const uint64_t ft64 = (uint64_t)st_g(st_t) + H(P.t);
+                const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
+                // 1. take work: own children first, else claim from the ring
+                int n = 0;
+                uint2 en = make_uint2(RING_EMPTY, 0u);
+                if (c_loc > 0) {
+                    n = min(32, c_loc);
+                    if (lane < n) en = wr.sn[c_loc - n + lane];
+                    c_loc -= n;
+                    __syncwarp();
+                } else {
+                    int h0 = 0;
+                    if (lane == 0) {
+                        n = -1;
+                        for (uint32_t spins = 0;; spins++) {
+                            const int h = *(volatile int *)&sq->head, t = *(volatile int *)&sq->tail;
+                            if (h < t) {
+                                const int k = min(32, t - h);
+                                if (atomicCAS(&sq->head, h, h + k) == h) {
+                                    n = k;
+                                    h0 = h;
+                                    break;
+                                }
+                                continue;
+                            }
+                            if (*(volatile int *)&sq->pending == 0) break;  // bucket done
+                            if (spins > SPIN_LIMIT) {
+                                atomicOr(&sq->status, ST_TIMEOUT);
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
+                    }
+                    n = __shfl_sync(FULL, n, 0);
+                    h0 = __shfl_sync(FULL, h0, 0);
+                    if (n < 0) break;
+                    if (lane < n) {
+                        volatile uint2 *slot = reinterpret_cast<volatile uint2 *>(ring + h0 + lane);
+                        uint2 x = make_uint2(slot->x, slot->y);
+                        for (uint32_t spins = 0; x.x == RING_EMPTY; spins++) {
+                            // reserved by a producer that has not written yet
+                            if (spins > SPIN_LIMIT) {
+                                atomicOr(&sq->status, ST_TIMEOUT);
+                                break;
+                            }
+                            __nanosleep(32);
+                            x = make_uint2(slot->x, slot->y);
+                        }
+                        en = x;
+                        slot->x = RING_EMPTY;  // clean for the next bucket
+                    }
+                }
+                // 2. entry stage (as run_search)
+                int u = -1, rb = 0, deg = 0;
+                uint32_t gu = 0;
+                bool requeue = false;
+                if (lane < n && en.x != RING_EMPTY) {
+                    u = (int)en.x;
+                    gu = en.y;
+                    const uint64_t su = __ldcg(B.state + u);
+                    const uint32_t hu = H(u);
+                    const int r0 = row_begin(G.off, G.oend, u), r1 = row_end(G.off, G.oend, u);
+                    if (st_g(su) == gu && u != P.t) {
+                        if ((uint64_t)gu + hu < ft) {
+                            rb = r0;
+                            deg = r1 - r0;
+                            n_exp++;
+                        } else if (P.keep) {
+                            requeue = true;
+                        }
+                    }
+                }
+                stage_push(requeue, make_uint2((uint32_t)u, gu), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
+                           ctl, 0);
+                int total;
+                const int ex = warp_excl_scan(deg, &total);
+                wr.excl[lane] = ex;
+                wr.rb[lane] = rb;
+                wr.bdeg[lane] = deg;
+                wr.drb[lane] = 0;
+                wr.g[lane] = gu;
+                wr.u[lane] = u;
+                __syncwarp();
+                n_scan += (lane == 0) ? (unsigned long long)total : 0ull;
+                for (int kb = 0; kb < total; kb += 32) {
+                    const int k = kb + lane;
+                    bool to_near = false, to_far = false, first = false;
+                    int v = 0;
+                    uint32_t ng = 0;
+                    if (k < total) {
+                        const int o = row_owner(wr, k);
+                        const uint2 a = row_arc(G, wr, o, k, true);
+                        v = (int)a.x;
+                        const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
+                        if (v >= 0 && ng64 < INF_G) {
+                            ng = (uint32_t)ng64;
+                            uint64_t cur = __ldcg(B.state + v);
+                            if (ng < st_g(cur)) {
+                                const uint32_t hv = H(v);
+                                const uint64_t fv = (uint64_t)ng + hv;
+                                if (P.keep ? hv < INF_G : fv < ft) {
+                                    const uint64_t nv = st_make(ng, wr.u[o]);
+                                    for (;;) {
+                                        const uint64_t got = atomicCAS(B.state + v, cur, nv);
+                                        if (got == cur) {
+                                            first = !P.no_touch_log && st_g(cur) >= INF_G;
+                                            if (fv < T) to_near = true;
+                                            else to_far = true;
+                                            break;
+                                        }
+                                        cur = got;
+                                        if (ng >= st_g(cur)) break;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    if (to_near || to_far) n_rel++;
+                    // near pushes: counted in `pending` first, then kept as
+                    // this warp's own work, or spilled to the ring when full
+                    const unsigned mn = __ballot_sync(FULL, to_near);
+                    if (mn) {
+                        const int kn = __popc(mn);
+                        const int rank_in = __popc(mn & ((1u << lane) - 1u));
+                        if (lane == 0) atomicAdd(&sq->pending, kn);
+                        __syncwarp();
+                        if (c_loc + kn <= 64) {
+                            if (to_near) wr.sn[c_loc + rank_in] = make_uint2((uint32_t)v, ng);
+                            c_loc += kn;
+                        } else {
+                            int p0 = 0;
+                            if (lane == 0) p0 = ring_reserve(sq, kn, cap);
+                            p0 = __shfl_sync(FULL, p0, 0);
+                            if (p0 >= 0) {
+                                if (to_near) {
+                                    volatile uint2 *slot = reinterpret_cast<volatile uint2 *>(ring + p0 + rank_in);
+                                    // one 8-byte store: readers see the old
+                                    // empty marker or the whole entry
+                                    *reinterpret_cast<volatile unsigned long long *>(slot) =
+                                        ((unsigned long long)ng << 32) | (uint32_t)v;
+                                }
+                            } else {
+                                // ring full: the entries go to far (the next
+                                // split brings them back) and leave the bucket
+                                if (lane == 0) atomicSub(&sq->pending, kn);
+                                to_far = to_far || to_near;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                    stage_push(to_far, make_uint2((uint32_t)v, ng), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
+                               ctl, 0);
+                    stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, 0);
+                }
+                __syncwarp();
+                // 3. retire the chunk (its children are already counted)
+                if (lane == 0 && n > 0) atomicSub(&sq->pending, n);
+                if (*(volatile int *)&sq->status & ST_TIMEOUT) break;
+            }
+            stage_flush(wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
+            stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, 0);
+            __syncthreads();
+            phases++;
+            nfar += *(volatile int *)&sq->far_cnt;
+            const int st = *(volatile int *)&sq->status | *(volatile int *)&ctl->status;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                sq->far_cnt = 0;
+                sq->head = 0;
+                sq->tail = 0;
+                sq->pending = 0;
+            }
+            if (st & (ST_OVERFLOW | ST_TIMEOUT)) {
+                if (threadIdx.x == 0) atomicOr(&ctl->status, st & (ST_OVERFLOW | ST_TIMEOUT));
+                break;
+            }
+            if (nfar > B.cap_f) {
+                if (threadIdx.x == 0) atomicOr(&ctl->status, ST_OVERFLOW);
+                break;
+            }
+            Tsplit = sat_add(T, P.delta);
+            __syncthreads();
+        }
+        // ---- split the far pile at Tsplit ---------------------------------
+        {
+            const uint64_t st_t = __ldcg(B.state + P.t);
+            const uint64_t ft64 = (uint64_t)st_g(st_t) + H(P.t);
+            const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
+            unsigned int local_min = 0xFFFFFFFFu;
+            int c_n = 0, c_f = 0;
+            if (threadIdx.x == 0) ctl->far_scanned += (unsigned long long)nfar;
+            for (int64_t base = (int64_t)warp * 32; base < nfar; base += (int64_t)(blockDim.x >> 5) * 32) {
+                const int64_t idx = base + lane;
+                bool to_near = false, keep = false;
+                uint2 en = make_uint2(0u, 0u);
+                if (idx < nfar) {
+                    en = __ldcg(fcur + idx);
+                    const uint64_t sv = __ldcg(B.state + en.x);
+                    if (st_g(sv) == en.y) {
+                        const uint64_t f = (uint64_t)en.y + H((int)en.x);
+                        if (f < ft && f < Tsplit) {
+                            to_near = true;
+                        } else if (f < ft || (P.keep && f < INF_G)) {
+                            keep = true;
+                            local_min = min(local_min, (uint32_t)f);
+                        }
+                    }
+                }
+                // split output goes to ring positions [0, m): the ring is
+                // clean and nobody reads it until the split is over
+                stage_push(to_near, en, wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
+                stage_push(keep, en, wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
+            }
+            stage_flush(wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
+            stage_flush(wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) local_min = min(local_min, __shfl_xor_sync(FULL, local_min, o));
+            if (lane == 0 && local_min != 0xFFFFFFFFu) atomicMin(&sq->minf, local_min);
+            __syncthreads();
+            const int m = min(*(volatile int *)&sq->tail, cap);
+            const int kept = *(volatile int *)&sq->alt_cnt;
+            const unsigned int mf = *(volatile unsigned int *)&sq->minf;
+            const int st = *(volatile int *)&ctl->status;
+            phases++;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                sq->alt_cnt = 0;
+                sq->minf = 0xFFFFFFFFu;
+                sq->head = 0;
+                sq->pending = m;
+            }
+            uint2 *t2 = fcur;
+            fcur = falt;
+            falt = t2;
+            nfar = kept;
+            if (st & (ST_OVERFLOW | ST_TIMEOUT)) break;
+            if (phases > max_phases) {
+                if (threadIdx.x == 0) atomicOr(&ctl->status, ST_TIMEOUT);
+                break;
+            }
+            if (m > 0) {
+                T = Tsplit;
+                do_expand = true;
+            } else if (nfar == 0 || mf >= ft) {
+                break;  // no open node with f < f(t)
+            } else {
+                Tsplit = sat_add(mf, P.delta);
+                do_expand = false;
+            }
+            __syncthreads();
+        }
+    }
+
+    if (lane == 0 && n_scan) atomicAdd(&ctl->scanned, n_scan);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_exp += __shfl_xor_sync(FULL, n_exp, o);
+        n_rel += __shfl_xor_sync(FULL, n_rel, o);
+    }
+    if (lane == 0) {
+        if (n_exp) atomicAdd(&ctl->expanded, n_exp);
+        if (n_rel) atomicAdd(&ctl->relaxed, n_rel);
+    }
+    if (threadIdx.x == 0) {
+        ctl->far_n = (int)nfar;
+        ctl->far_sel = fcur == B.f1 ? 1 : 0;
+        ctl->iters = phases;
+    }
+    __syncthreads();
+    SearchResult r;
+    const uint64_t st_t = __ldcg(B.state + P.t);
+    const uint64_t c = (uint64_t)st_g(st_t) + H(P.t);
+    r.cost = (st_g(st_t) >= INF_G || c >= INF_G) ? 0xFFFFFFFFu : (uint32_t)c;
+    r.iters = phases;
+    return r;
+}
+
+}  // namespace ddp

@@ -100,6 +100,7 @@ int launch(ddp_server *s) {
     A.K = s->o.K;
     A.bfs_budget = s->hkind == DDP_H_BFS_CAPPED ? bfs_budget(s->g->n) : 0;
     A.group = 1;
+    A.sync_engine = (s->o.flags & DDP_OPT_SYNC) != 0;
     A.serve = 1;
     A.pub = s->d_ctl;
     A.pause = s->d_ctl + 1;

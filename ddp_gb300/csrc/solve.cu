@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "engine_async.cuh"
 #include "graph.cuh"
 #include "solve.cuh"
 
@@ -48,6 +49,8 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
     DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * S, st));
     if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
+    // queue slots start as "empty" (the asynchronous engine's ring marker)
+    DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * 2 * S, st));
     DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl) * S, st));
     return DDP_OK;
 }
@@ -101,7 +104,8 @@ __global__ void __launch_bounds__(512) k_bfs_single(DevGraph G, SlotArrays sa, u
     SlotBufs B = slot_of(sa, 0);
     B.hops = hops;
     GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
-    const uint32_t cap = run_bfs_hops(grp, G, B, t, wrows, 0u, (int64_t)budget);
+    // q0 is the ring of the asynchronous engine: keep it clean
+    const uint32_t cap = run_bfs_hops(grp, G, B, t, wrows, 0u, (int64_t)budget, true);
     if (grp.rank() == 0) B.ctl->hcap = cap;
 }
 
@@ -127,9 +131,19 @@ __global__ void __launch_bounds__(512, 2)
 // finishing short searches take the next query (dynamic load balance over
 // uneven depths).  Fewer, wider groups keep fewer per-query state arrays live
 // at once, which lets them stay resident in L2.
+// One search of the slot: the asynchronous single-CTA engine when the slot is
+// one CTA (and the caller did not ask for the phase-synchronous one), else
+// the phase-synchronous group engine.
+template <class Grp, class Heur>
+__device__ SearchResult slot_search(const Grp &grp, const DevGraph &G, const SlotBufs &B, const Heur &H,
+                                    const SearchParams &P, WarpRows *wrows, CtaQ *sq, bool async) {
+    if (async) return run_search_cta(G, B, H, P, wrows, sq);
+    return run_search(grp, G, B, H, P, wrows);
+}
+
 template <int HK, class Grp>
 __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B, const BatchArgs &A,
-                           uint32_t *epoch, WarpRows *wrows) {
+                           uint32_t *epoch, WarpRows *wrows, CtaQ *sq, bool async) {
     SearchCtl *ctl = B.ctl;
     long long t0 = 0;
     for (;;) {
@@ -196,16 +210,22 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
         SearchResult r;
         if (HK == 1) {
             const uint32_t tag = *(volatile uint32_t *)&ctl->tag;
-            const uint32_t cap = run_bfs_hops(grp, G, B, t, wrows, tag, A.bfs_budget);
-            r = run_search(grp, G, B, HeurHops{B.hops, G.wmin, cap, tag}, P, wrows);
+            const uint32_t cap = run_bfs_hops(grp, G, B, t, wrows, tag, A.bfs_budget, async);
+            r = slot_search(grp, G, B, HeurHops{B.hops, G.wmin, cap, tag}, P, wrows, sq, async);
         } else if (HK == 2) {
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
-            r = run_search(grp, G, B, HeurManhattan{G.xy, tp.x, tp.y, G.wmin}, P, wrows);
+            r = slot_search(grp, G, B, HeurManhattan{G.xy, tp.x, tp.y, G.wmin}, P, wrows, sq, async);
         } else if (HK == 3) {
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
-            r = run_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows);
+            r = slot_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows, sq, async);
         } else {
-            r = run_search(grp, G, B, HeurZero{}, P, wrows);
+            r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
+        }
+        if (async && (*(volatile int *)&ctl->status & (ST_OVERFLOW | ST_TIMEOUT))) {
+            // an aborted asynchronous search may leave ring slots written:
+            // clear the ring so the slot's next search starts clean
+            for (int64_t i = grp.rank(); i < B.cap_q; i += grp.size()) B.q0[i].x = RING_EMPTY;
+            grp.sync();
         }
         if (grp.rank() == 0) {
             const int st = ctl->status;
@@ -250,15 +270,36 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
 template <int HK>
 __global__ void __launch_bounds__(512, 2) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
     __shared__ WarpRows wrows[MAX_WARPS];
+    __shared__ CtaQ sq;
     if (A.group <= 1) {
         SlotBufs B = slot_of(sa, blockIdx.x);
         CtaGroup grp{&B.ctl->status};
-        batch_loop<HK>(grp, G, B, A, sa.epoch + blockIdx.x, wrows);
+        batch_loop<HK>(grp, G, B, A, sa.epoch + blockIdx.x, wrows, &sq, !A.sync_engine);
     } else {
         const int slot = blockIdx.x / A.group;
         SlotBufs B = slot_of(sa, slot);
         SubGridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status, A.group};
-        batch_loop<HK>(grp, G, B, A, sa.epoch + slot, wrows);
+        batch_loop<HK>(grp, G, B, A, sa.epoch + slot, wrows, &sq, false);
+    }
+}
+
+// Single query on one CTA with the asynchronous engine (narrow searches).
+template <class Heur>
+__global__ void __launch_bounds__(512, 2)
+    k_solve_cta(DevGraph G, SlotArrays sa, Heur H, SearchParams P, int32_t *out, int32_t *path, int32_t path_cap) {
+    __shared__ WarpRows wrows[MAX_WARPS];
+    __shared__ CtaQ sq;
+    SlotBufs B = slot_of(sa, 0);
+    SearchResult r = run_search_cta(G, B, H, P, wrows, &sq);
+    if (threadIdx.x == 0) {
+        out[0] = r.cost >= INF_G ? DDP_INF : (int32_t)r.cost;
+        out[1] = (B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) ? 0 : write_path(B, P.s, P.t, path, path_cap, G.n, &B.ctl->status);
+        out[2] = B.ctl->status;
+        out[3] = r.iters;
+    }
+    if (B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) {
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < B.cap_q; i += blockDim.x) B.q0[i].x = RING_EMPTY;
     }
 }
 
@@ -533,7 +574,23 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
         DDP_CUDA(cudaMemsetAsync(w->sa.ctl, 0, sizeof(SearchCtl), st));
         cudaError_t e;
         const int kind = h ? h->kind : DDP_H_ZERO;
-        if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) {
+        const bool one_cta = (o.flags & DDP_OPT_ONE_CTA) != 0;
+        if (one_cta) {
+            void *hp = nullptr;
+            HeurHops Hh{h ? h->d_hops : nullptr, g->wmin, h ? h->cap : HOPS_INF, 0u};
+            HeurManhattan Hm{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->wmin};
+            HeurEuclid He{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->rho_fp};
+            HeurArray Ha{h ? h->d_h : nullptr};
+            HeurZero Hz{};
+            const void *fn;
+            if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) { fn = (const void *)k_solve_cta<HeurHops>; hp = &Hh; }
+            else if (kind == DDP_H_MANHATTAN) { fn = (const void *)k_solve_cta<HeurManhattan>; hp = &Hm; }
+            else if (kind == DDP_H_EUCLID) { fn = (const void *)k_solve_cta<HeurEuclid>; hp = &He; }
+            else if (kind == DDP_H_USER) { fn = (const void *)k_solve_cta<HeurArray>; hp = &Ha; }
+            else { fn = (const void *)k_solve_cta<HeurZero>; hp = &Hz; }
+            void *args[] = {&G, &w->sa, hp, &P, &w->d_out, &w->d_path, &g->n};
+            e = cudaLaunchKernel(fn, dim3(1), dim3(block), args, 0, st);
+        } else if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) {
             HeurHops H{h->d_hops, g->wmin, h->cap, 0u};
             int grid = coop_grid(k_solve_single<HeurHops>, block, o.grid);
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
@@ -560,6 +617,8 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             e = coop_launch(k_solve_single<HeurZero>, grid, block, args, st);
         }
         if (e != cudaSuccess) return cuda_fail(e, "k_solve_single launch");
+        if (!one_cta)  // the phase-synchronous engine leaves entries in q0/q1
+            DDP_CUDA(cudaMemsetAsync(w->sa.q, 0xFF, sizeof(uint2) * (size_t)w->sa.cap_q * 2, st));
         k_reset_touched<<<dim3(256, 1), 256, 0, st>>>(w->sa);
         DDP_CUDA(cudaGetLastError());
         int32_t res[4];
@@ -706,6 +765,7 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     A.version = 0;
     A.K = b->o.K;
     A.group = b->group;
+    A.sync_engine = (b->o.flags & DDP_OPT_SYNC) != 0;
     DevGraph G = graph_view(b->g);
     cudaError_t e = cudaMemsetAsync(b->d_work, 0, sizeof(int) * 2, b->stream);
     if (e != cudaSuccess) return e;

@@ -33,6 +33,7 @@ struct BatchArgs {
     int32_t K;
     int64_t bfs_budget;  // capped heuristic BFS (0 = run to completion)
     int group;           // CTAs per query slot
+    int sync_engine;     // 1: phase-synchronous engine even for one-CTA slots
     // serving mode (continuous batching): requests are published in host
     // memory mapped into the device; slots wait for them
     int serve;

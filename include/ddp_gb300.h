@@ -78,8 +78,12 @@ typedef struct ddp_opts {
     int64_t queue_cap; /* entries per search queue                               */
     void *stream;      /* cudaStream_t; NULL = the handle's own stream           */
     int32_t group;     /* batch: CTAs working on one query (1 = one CTA)          */
-    int32_t reserved;
+    int32_t flags;     /* DDP_OPT_* bits                                          */
 } ddp_opts;
+
+/* ddp_opts.flags */
+#define DDP_OPT_SYNC 1    /* one-CTA slots use the phase-synchronous engine      */
+#define DDP_OPT_ONE_CTA 2 /* ddp_solve: one CTA with the asynchronous engine      */
 
 /* ---- library ----------------------------------------------------------- */
 const char *ddp_last_error(void);

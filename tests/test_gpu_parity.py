@@ -272,3 +272,39 @@ def test_batch_multi_cta_groups(gpu, oracle, group):
         ok, why = oracle.check_path(g.off, g.col, g.w, be.path(i), int(S[i]), int(T[i]), int(cost[i]))
         assert ok, why
     be.close()
+
+
+def test_async_one_cta_engine(gpu, oracle):
+    """The asynchronous single-CTA engine (ddp_solve with OPT_ONE_CTA, and
+    one-CTA batch slots) matches the oracle, also when it alternates with the
+    phase-synchronous engine on the same workspace."""
+    d = gpu
+    m = d.gen_maze(160, 200, 0.3, 12)
+    dm = d.DeviceGraph.from_csr(m)
+    t = m.n - 1
+    h = dm.heuristic(t, d.H_MANHATTAN, want_values=True)
+    mg = m.with_sentinel()
+    hh = np.concatenate([h.values, [0]]).astype(np.int32)
+    want = _oracle_cost(oracle, mg, hh, 0, t)
+    for flags in (d.OPT_ONE_CTA, 0, d.OPT_ONE_CTA):
+        r = dm.solve(0, t, h, flags=flags)
+        assert r.cost == want
+        ok, why = oracle.check_path(m.off, m.col, m.w, r.path, 0, t, r.cost)
+        assert ok, why
+    g = d.gen_random_chain(20000, 8, 1, 100, 404).with_sentinel()
+    dg = d.DeviceGraph.from_csr(g)
+    S, T, _ = d.gen_pairs(d.CSR(g.n, g.off, g.col, g.w), 48, 4, 400, 9)
+    for hk in (d.H_BFS_CAPPED, d.H_ZERO):
+        be = d.BatchEngine(dg, hk, group=1)
+        cost, _ = be.solve(S, T)
+        for i in range(len(S)):
+            href = oracle.bfs_heuristic(g.n, g.off[:-1], g.col, g.w, int(T[i]))
+            assert cost[i] == _oracle_cost(oracle, g, href, int(S[i]), int(T[i])), i
+            ok, why = oracle.check_path(g.off, g.col, g.w, be.path(i), int(S[i]), int(T[i]), int(cost[i]))
+            assert ok, why
+        be.close()
+    for s_, t_ in [(3, 15000), (19000, 7)]:
+        hq = dg.heuristic(t_, d.H_BFS_HOPS)
+        a = dg.solve(s_, t_, hq, flags=d.OPT_ONE_CTA)
+        b = dg.solve(s_, t_, hq)
+        assert a.cost == b.cost == _oracle_cost(oracle, g, oracle.bfs_heuristic(g.n, g.off[:-1], g.col, g.w, t_), s_, t_)
