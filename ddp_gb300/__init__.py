@@ -521,11 +521,13 @@ class DynamicSearch:
 class Server:
     """Continuous-batching A* service on a resident graph (ddp_server)."""
 
-    def __init__(self, graph: DeviceGraph, hkind: int = H_EUCLID, max_requests: int = 1 << 20, **opts):
+    def __init__(self, graph: DeviceGraph, hkind: int = H_EUCLID, max_requests: int = 1 << 20, versions: int = 8,
+                 **opts):
         self.graph = graph
         o = _opts(**opts)
         h = C.c_void_p()
-        check(lib().ddp_serve_create(graph.handle, int(hkind), C.byref(o), int(max_requests), C.byref(h)))
+        check(lib().ddp_serve_create(graph.handle, int(hkind), C.byref(o), int(max_requests), int(versions),
+                                     C.byref(h)))
         self.handle = h
 
     def submit(self, S, T) -> int:

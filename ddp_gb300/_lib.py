@@ -55,7 +55,7 @@ SIGNATURES = {
     "ddp_dyn_path": (C.c_int, [vp, i32p, C.c_int32, i32p]),
     "ddp_dyn_stats": (C.c_int, [vp, i64p]),
     "ddp_dyn_free": (C.c_int, [vp]),
-    "ddp_serve_create": (C.c_int, [vp, C.c_int32, C.POINTER(Opts), C.c_int64, C.POINTER(vp)]),
+    "ddp_serve_create": (C.c_int, [vp, C.c_int32, C.POINTER(Opts), C.c_int64, C.c_int32, C.POINTER(vp)]),
     "ddp_serve_submit": (C.c_int, [vp, C.c_int32, i32p, i32p, i64p]),
     "ddp_serve_poll": (C.c_int, [vp, C.c_int32, i64p, i32p, i64p, i32p, i32p]),
     "ddp_serve_update": (C.c_int, [vp, C.c_int32, i32p, i32p, i32p, u32p]),

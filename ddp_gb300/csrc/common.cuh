@@ -16,6 +16,9 @@ namespace ddp {
 void set_error(const std::string &msg);
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
+// Event trace to stderr, on when the environment sets DDP_TRACE=1.
+bool trace_on();
+void trace(const char *fmt, ...) __attribute__((format(printf, 1, 2)));
 
 #define DDP_CUDA(call)                                              \
     do {                                                            \

@@ -396,13 +396,13 @@ int dyn_upload(ddp_graph *g) {
     const int32_t n = g->n;
     if (m->full) {
         if ((int64_t)m->arc.size() > m->arc_cap) {
-            cudaFree(g->d_arc);
+            graph_free_dev(g, g->d_arc);
             g->d_arc = nullptr;
             DDP_CUDA(cudaMalloc(&g->d_arc, sizeof(uint2) * m->arc.size()));
             m->arc_cap = (int64_t)m->arc.size();
         }
         if ((int64_t)m->rarc.size() > m->rarc_cap) {
-            cudaFree(g->d_rarc);
+            graph_free_dev(g, g->d_rarc);
             g->d_rarc = nullptr;
             DDP_CUDA(cudaMalloc(&g->d_rarc, sizeof(uint2) * m->rarc.size()));
             m->rarc_cap = (int64_t)m->rarc.size();
@@ -414,6 +414,7 @@ int dyn_upload(ddp_graph *g) {
         DDP_CUDA(cudaMemcpy(g->d_roff, m->rbeg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
         DDP_CUDA(cudaMemcpy(g->d_roend, m->rend.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
         m->full = false;
+        g->layout_gen++;
         m->dirty_arc.clear();
         m->dirty_rarc.clear();
         m->dirty_row.clear();
@@ -426,18 +427,25 @@ int dyn_upload(ddp_graph *g) {
         std::sort(dirty.begin(), dirty.end());
         dirty.erase(std::unique(dirty.begin(), dirty.end()), dirty.end());
         const int64_t k = (int64_t)dirty.size();
+        std::vector<long long> sl(dirty.begin(), dirty.end());
+        std::vector<uint2> val((size_t)k);
+        for (int64_t i = 0; i < k; i++) val[(size_t)i] = src[(size_t)dirty[(size_t)i]];
+        const int h = g->hook.fn ? g->hook.fn(g->hook.ctx, 0, dst, nullptr, sl.data(), val.data(), k)
+                                 : SCATTER_LAUNCH;
+        if (h != SCATTER_LAUNCH) {
+            if (h) return h;
+            dirty.clear();
+            return DDP_OK;
+        }
         if (k > d->scat_cap) {
-            cudaFree(d->d_slot);
-            cudaFree(d->d_val);
+            graph_free_dev(g, d->d_slot);
+            graph_free_dev(g, d->d_val);
             d->d_slot = nullptr;
             d->d_val = nullptr;
             DDP_CUDA(cudaMalloc(&d->d_slot, sizeof(long long) * k));
             DDP_CUDA(cudaMalloc(&d->d_val, sizeof(uint2) * k));
             d->scat_cap = k;
         }
-        std::vector<long long> sl(dirty.begin(), dirty.end());
-        std::vector<uint2> val((size_t)k);
-        for (int64_t i = 0; i < k; i++) val[(size_t)i] = src[(size_t)dirty[(size_t)i]];
         DDP_CUDA(cudaMemcpyAsync(d->d_slot, sl.data(), sizeof(long long) * k, cudaMemcpyHostToDevice, g->stream));
         DDP_CUDA(cudaMemcpyAsync(d->d_val, val.data(), sizeof(uint2) * k, cudaMemcpyHostToDevice, g->stream));
         k_scatter_arcs<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(dst, d->d_slot, d->d_val, (int)k);
@@ -452,16 +460,22 @@ int dyn_upload(ddp_graph *g) {
         std::sort(drow.begin(), drow.end());
         drow.erase(std::unique(drow.begin(), drow.end()), drow.end());
         const int64_t k = (int64_t)drow.size();
-        if (k > d->rows_cap) {
-            cudaFree(d->d_rows);
-            d->d_rows = nullptr;
-            DDP_CUDA(cudaMalloc(&d->d_rows, sizeof(int4) * k));
-            d->rows_cap = k;
-        }
         std::vector<int4> r((size_t)k);
         for (int64_t i = 0; i < k; i++) {
             const int32_t u = drow[(size_t)i];
             r[(size_t)i] = make_int4(u, b[(size_t)u], e[(size_t)u], 0);
+        }
+        const int h = g->hook.fn ? g->hook.fn(g->hook.ctx, 1, db, de, r.data(), nullptr, k) : SCATTER_LAUNCH;
+        if (h != SCATTER_LAUNCH) {
+            if (h) return h;
+            drow.clear();
+            return DDP_OK;
+        }
+        if (k > d->rows_cap) {
+            graph_free_dev(g, d->d_rows);
+            d->d_rows = nullptr;
+            DDP_CUDA(cudaMalloc(&d->d_rows, sizeof(int4) * k));
+            d->rows_cap = k;
         }
         DDP_CUDA(cudaMemcpyAsync(d->d_rows, r.data(), sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
         k_scatter_rows<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(db, de, d->d_rows, (int)k);
@@ -650,6 +664,7 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     const int32_t n = g->n;
     ddp_dyn *d = new ddp_dyn();
     d->g = g;
+    graph_ref(g);
     d->s = source;
     d->t = target;
     d->hkind = hkind;
@@ -751,7 +766,10 @@ int ddp_dyn_free(ddp_dyn *d) {
     cudaFree(d->d_upd);
     // the graph keeps its dynamic layout and mirror (other searches and
     // ddp_graph_read_csr see the updated graph)
-    if (d->g) d->g->dyn_active = false;
+    if (d->g) {
+        d->g->dyn_active = false;
+        graph_unref(d->g);
+    }
     delete d;
     return DDP_OK;
 }

@@ -58,6 +58,7 @@ struct SearchCtl {
     unsigned int hcap;    // hop cap of the last BFS
     int cur_q;            // query the slot is working on (batch)
     int far_n, far_sel;   // far pile left by the last run (dynamic resume)
+    int cur_ver;          // graph version of the current search (serving)
     unsigned int bar_count, bar_gen;  // grid barrier (single-query form)
 };
 

@@ -430,10 +430,10 @@ int ddp_gen_pairs(int32_t n, const int32_t *off, const int32_t *col, int32_t npa
 }
 
 /* ---------------- 2D geometric k-NN graph -------------------------------- */
-/* Points uniform on an integer grid [0, side)^2, each joined in both
- * directions to its k nearest neighbours (ties by index), duplicates
- * removed; w = max(1, round(wscale * length / spacing)) with
- * spacing = side / sqrt(n), i.e. wscale per mean point spacing. */
+/* Points uniform on an integer grid [0, side)^2, numbered in Morton order,
+ * each joined in both directions to its k nearest neighbours (ties by
+ * index), duplicates removed; w = max(1, round(wscale * length / spacing))
+ * with spacing = side / sqrt(n), i.e. wscale per mean point spacing. */
 typedef struct {
     int32_t n, k, side, gcells;
     const int32_t *xy;
@@ -509,6 +509,58 @@ int ddp_gen_geometric(int32_t n, int32_t k, int32_t side, uint32_t wscale, uint6
     for (int32_t i = 0; i < n; i++) {
         xy[2 * i] = (int32_t)rng_below(&r, (uint64_t)side);
         xy[2 * i + 1] = (int32_t)rng_below(&r, (uint64_t)side);
+    }
+    /* number the points along a Morton (Z-order) curve: nodes close in the
+     * plane get close ids, so a search's state and arc reads stay local in
+     * memory (the plane is what the search explores) */
+    {
+        uint64_t *key = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+        if (!key) return -2;
+        for (int32_t i = 0; i < n; i++) {
+            uint64_t m = 0, x = (uint32_t)xy[2 * i], y = (uint32_t)xy[2 * i + 1];
+            for (int b = 0; b < 31; b++) m |= ((x >> b) & 1ull) << (2 * b) | ((y >> b) & 1ull) << (2 * b + 1);
+            key[i] = (m << 1) >> 1;
+        }
+        /* LSD radix sort of (key, point) on 62-bit keys, 8 passes of 8 bits */
+        uint64_t *k2 = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+        int32_t *p1 = (int32_t *)malloc(sizeof(int32_t) * (size_t)n), *p2 = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+        if (!k2 || !p1 || !p2) {
+            free(key);
+            free(k2);
+            free(p1);
+            free(p2);
+            return -2;
+        }
+        for (int32_t i = 0; i < n; i++) p1[i] = i;
+        for (int pass = 0; pass < 8; pass++) {
+            int64_t cnt[257] = {0};
+            const int sh = 8 * pass;
+            for (int32_t i = 0; i < n; i++) cnt[((key[i] >> sh) & 255) + 1]++;
+            for (int b = 0; b < 256; b++) cnt[b + 1] += cnt[b];
+            for (int32_t i = 0; i < n; i++) {
+                const int64_t d = cnt[(key[i] >> sh) & 255]++;
+                k2[d] = key[i];
+                p2[d] = p1[i];
+            }
+            uint64_t *tk = key;
+            key = k2;
+            k2 = tk;
+            int32_t *tp = p1;
+            p1 = p2;
+            p2 = tp;
+        }
+        int32_t *nxy = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)n);
+        if (!nxy) return -2;
+        for (int32_t i = 0; i < n; i++) {
+            nxy[2 * i] = xy[2 * p1[i]];
+            nxy[2 * i + 1] = xy[2 * p1[i] + 1];
+        }
+        memcpy(xy, nxy, sizeof(int32_t) * 2 * (size_t)n);
+        free(nxy);
+        free(key);
+        free(k2);
+        free(p1);
+        free(p2);
     }
     /* grid buckets, about 2 points per cell */
     int32_t G = (int32_t)sqrt((double)n / 2.0);

@@ -3,7 +3,10 @@
 // Replaces LIB/include/graph.h:93-118 (Graph<T>::read_graph), graph.cuh:62-72
 // (GPU_Graph<T>::__gpu_alloc) and DA_star/genOpCSR.cpp:31-53 (reverse CSR,
 // built here in memory instead of written to graph_op.txt).
+#include <chrono>
+#include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -19,6 +22,25 @@ void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int code, const std::string &msg) {
     set_error(msg);
     return code;
+}
+
+bool trace_on() {
+    static const bool on = [] {
+        const char *v = std::getenv("DDP_TRACE");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
+void trace(const char *fmt, ...) {
+    if (!trace_on()) return;
+    const auto t = std::chrono::steady_clock::now().time_since_epoch();
+    std::fprintf(stderr, "[ddp %.6f] ", std::chrono::duration<double>(t).count());
+    va_list ap;
+    va_start(ap, fmt);
+    std::vfprintf(stderr, fmt, ap);
+    va_end(ap);
+    std::fputc('\n', stderr);
 }
 
 int cuda_fail(cudaError_t e, const char *what) {
@@ -106,8 +128,22 @@ static int upload_csr(ddp_graph *g, const int32_t *off, const int32_t *col, cons
     return DDP_OK;
 }
 
+void graph_free_dev(ddp_graph *g, void *p) {
+    if (!p) return;
+    if (g->defer_free)
+        g->deferred.push_back(p);
+    else
+        cudaFree(p);
+}
+
+void graph_flush_frees(ddp_graph *g) {
+    for (void *p : g->deferred) cudaFree(p);
+    g->deferred.clear();
+}
+
 void graph_release(ddp_graph *g) {
     if (!g) return;
+    graph_flush_frees(g);
     workspace_release(g);
     cudaFree(g->d_off);
     cudaFree(g->d_arc);
@@ -123,6 +159,12 @@ void graph_release(ddp_graph *g) {
     dyn_mirror_free(g->dyn);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
+}
+
+void graph_ref(ddp_graph *g) { g->refs.fetch_add(1); }
+
+void graph_unref(ddp_graph *g) {
+    if (g && g->refs.fetch_sub(1) == 1) graph_release(g);
 }
 
 }  // namespace ddp
@@ -244,7 +286,7 @@ int ddp_graph_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint
 }
 
 int ddp_graph_free(ddp_graph *g) {
-    graph_release(g);
+    graph_unref(g);  // objects built on the graph keep it until they are freed
     return DDP_OK;
 }
 

@@ -1,6 +1,7 @@
 // Host-side handle types shared by the translation units of libddp_gb300.
 #pragma once
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -8,8 +9,25 @@
 
 struct DynMirror;
 
+// Runs a scatter of dynamic-graph changes into device arrays without a
+// kernel launch of its own (a serving kernel that holds every SM runs it in
+// place).  kind 0: arcs, dst0[list[i]] = vals[i] with list long long and
+// vals uint2; kind 1: row bounds, for r = list[i] (int4 {row, begin, end}):
+// dst0[r.x] = r.y, dst1[r.x] = r.z.  list and vals are host memory.
+// Returns DDP_OK when done, SCATTER_LAUNCH when the caller must run the
+// scatter itself, or an error code.
+constexpr int SCATTER_LAUNCH = -1;
+struct ScatterHook {
+    int (*fn)(void *ctx, int kind, void *dst0, void *dst1, const void *list, const void *vals,
+              int64_t k) = nullptr;
+    void *ctx = nullptr;
+};
+
 struct ddp_graph {
     std::mutex mu;
+    // the handle plus every object that keeps a pointer to the graph
+    // (heuristics, batches, dynamic searches, servers); the last one frees it
+    std::atomic<int> refs{1};
     int device = 0;
     cudaStream_t stream = nullptr;
     int32_t n = 0;
@@ -33,6 +51,12 @@ struct ddp_graph {
     int32_t *d_roend = nullptr;
     DynMirror *dyn = nullptr;  // host mirror of a dynamic graph
     bool dyn_active = false;          // a ddp_dyn search owns the graph's updates
+    // set while a serving kernel runs on the graph: scatters go through the
+    // hook, and device frees (which would wait for that kernel) are deferred
+    ScatterHook hook;
+    bool defer_free = false;
+    int64_t layout_gen = 0;  // bumps when the whole dynamic layout is uploaded again
+    std::vector<void *> deferred;
     // single-query workspace, allocated on first use
     struct Workspace *ws = nullptr;
 };
@@ -46,4 +70,9 @@ int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *
 int64_t dyn_live_arcs(const ddp_graph *g);
 int dyn_upload(ddp_graph *g);
 int dyn_graph_prepare(ddp_graph *g);
+// cudaFree now, or later (graph_flush_frees) while g->defer_free is set
+void graph_free_dev(ddp_graph *g, void *p);
+void graph_ref(ddp_graph *g);
+void graph_unref(ddp_graph *g);
+void graph_flush_frees(ddp_graph *g);
 }  // namespace ddp

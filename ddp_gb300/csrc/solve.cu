@@ -142,33 +142,76 @@ __device__ SearchResult slot_search(const Grp &grp, const DevGraph &G, const Slo
 }
 
 template <int HK, class Grp>
-__device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B, const BatchArgs &A,
+__device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B, const BatchArgs &A,
                            uint32_t *epoch, WarpRows *wrows, CtaQ *sq, bool async) {
     SearchCtl *ctl = B.ctl;
     long long t0 = 0;
+    int vbuf = -1;  // versioned serving: graph buffer the current search holds
     for (;;) {
         if (grp.rank() == 0) {
             int q;
             if (A.serve) {
-                // claim the next published request; leave when paused or
-                // after idle_limit empty polls
+                // claim the next published request.  A slot that finds no
+                // work for idle_limit polls votes to exit and keeps polling
+                // (new work takes its vote back); when every slot has voted,
+                // all of them leave together, so the launch never shrinks
+                // to a few slots while requests keep coming.
                 q = -1;
-                for (int idle = 0; idle <= A.idle_limit;) {
-                    if (*A.pause) break;
+                bool voted = false;
+                // a slot that voted waits for the others at most ~500 idle
+                // periods (slots that never became resident cannot vote)
+                for (int idle = 0, waited = 0;;) {
+                    if (*A.pause || *(volatile int *)A.closing) break;
                     const int p = *A.pub;
                     const int c = *(volatile int *)A.work;
                     if (c < p) {
+                        if (voted) {
+                            atomicSub(A.idle_votes, 1);
+                            voted = false;
+                        }
                         if (atomicCAS(A.work, c, c + 1) == c) {
                             q = c;
                             break;
                         }
                         continue;
                     }
-                    idle++;
+                    if (idle < A.idle_limit) {
+                        idle++;
+                    } else if (!voted) {
+                        atomicAdd(A.idle_votes, 1);
+                        voted = true;
+                    } else if (*(volatile int *)A.idle_votes >= A.serve_slots) {
+                        atomicExch(A.closing, 1);
+                        break;
+                    } else if (++waited > 500 * A.idle_limit) {
+                        break;
+                    }
                     __nanosleep(1000);
                 }
                 __threadfence_system();  // requests were written before pub
                 if (q < 0) q = A.nq;     // exit marker
+                if (q < A.nq && A.vtab) {
+                    // pin the latest graph version: count this search on its
+                    // buffer, then re-read the version.  Buffer v % K is only
+                    // rewritten for version v + K, after version v + K - 1 was
+                    // published and the buffer's count was seen at zero, so
+                    // the pin holds while fewer than K - 1 versions appeared
+                    // in between.  A pin that keeps failing fails the request
+                    // (cost -1: the host re-runs it).
+                    ctl->cur_ver = -1;
+                    for (uint32_t spins = 0; spins < 4096; spins++) {
+                        const int v = *A.cur_ver;
+                        const int b = v % A.nver;
+                        atomicAdd(A.inflight + b, 1);
+                        __threadfence_system();
+                        if (*A.cur_ver - v < A.nver - 1) {
+                            ctl->cur_ver = v;
+                            vbuf = b;
+                            break;
+                        }
+                        atomicSub(A.inflight + b, 1);
+                    }
+                }
             } else {
                 q = atomicAdd(A.work, 1);
             }
@@ -188,19 +231,33 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
         grp.sync();
         const int q = *(volatile int *)&ctl->cur_q;
         if (q >= A.nq) break;
+        const int qver = A.vtab ? *(volatile int *)&ctl->cur_ver : A.version;
+        DevGraph G = G0;
+        if (A.vtab && qver >= 0) {
+            // the table (host memory) is rewritten while the kernel runs
+            static_assert(sizeof(DevGraph) % 8 == 0, "DevGraph is copied in 8-byte words");
+            const volatile unsigned long long *src =
+                reinterpret_cast<const volatile unsigned long long *>(A.vtab + qver % A.nver);
+            unsigned long long *dst = reinterpret_cast<unsigned long long *>(&G);
+            for (int i = 0; i < (int)(sizeof(DevGraph) / 8); i++) dst[i] = src[i];
+        }
         // serving requests live in host memory written while the kernel
         // runs: read them uncached
         const int32_t s = A.serve ? *(const volatile int32_t *)(A.S + q) : __ldg(A.S + q);
         const int32_t t = A.serve ? *(const volatile int32_t *)(A.T + q) : __ldg(A.T + q);
-        if (s < 0 || s >= G.n || t < 0 || t >= G.n) {
+        if (qver < 0 || s < 0 || s >= G.n || t < 0 || t >= G.n) {
             if (grp.rank() == 0) {
-                A.cost[q] = DDP_INF;
+                A.cost[q] = qver < 0 ? -1 : DDP_INF;
                 if (A.plen) A.plen[q] = -1;
                 if (A.qstatus) A.qstatus[q] = -1;
                 if (A.serve) {
-                    A.ver[q] = A.version;
+                    A.ver[q] = qver;
                     __threadfence_system();
                     A.done[q] = 1;
+                }
+                if (vbuf >= 0) {
+                    atomicSub(A.inflight + vbuf, 1);
+                    vbuf = -1;
                 }
             }
             grp.sync();
@@ -239,9 +296,13 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
             if (A.plen) A.plen[q] = len;
             if (A.qstatus) A.qstatus[q] = ctl->status;
             if (A.serve) {
-                A.ver[q] = A.version;
+                A.ver[q] = qver;
                 __threadfence_system();
                 A.done[q] = 1;
+            }
+            if (vbuf >= 0) {
+                atomicSub(A.inflight + vbuf, 1);
+                vbuf = -1;
             }
             if (A.stats) {
                 long long *st6 = A.stats + DDP_STATS * (size_t)q;
@@ -267,10 +328,138 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G, const SlotBufs &B,
     }
 }
 
+// One maintenance sub, spread over threads tid, tid + nth, ...
+__device__ void svc_sub(const SvcSub &j, long long tid, long long nth) {
+    const long long k = j.k;
+    switch (j.kind) {
+    case SVC_SCATTER_ARCS: {
+        uint2 *dst = reinterpret_cast<uint2 *>(j.p0);
+        const volatile long long *slot = reinterpret_cast<const volatile long long *>(j.p2);
+        const volatile uint2 *val = reinterpret_cast<const volatile uint2 *>(j.p3);
+        for (long long i = tid; i < k; i += nth) {
+            const uint2 v = make_uint2(val[i].x, val[i].y);
+            dst[slot[i]] = v;
+        }
+        break;
+    }
+    case SVC_SCATTER_ROWS: {
+        int32_t *db = reinterpret_cast<int32_t *>(j.p0);
+        int32_t *de = reinterpret_cast<int32_t *>(j.p1);
+        const volatile int *rows = reinterpret_cast<const volatile int *>(j.p2);
+        for (long long i = tid; i < k; i += nth) {
+            const int r = rows[4 * i];
+            db[r] = rows[4 * i + 1];
+            de[r] = rows[4 * i + 2];
+        }
+        break;
+    }
+    case SVC_GATHER_ARCS: {
+        uint2 *dst = reinterpret_cast<uint2 *>(j.p0);
+        const uint2 *src = reinterpret_cast<const uint2 *>(j.p1);
+        const volatile long long *slot = reinterpret_cast<const volatile long long *>(j.p2);
+        for (long long i = tid; i < k; i += nth) {
+            const long long x = slot[i];
+            dst[x] = __ldcg(src + x);
+        }
+        break;
+    }
+    case SVC_GATHER_INTS: {
+        int32_t *dst = reinterpret_cast<int32_t *>(j.p0);
+        const int32_t *src = reinterpret_cast<const int32_t *>(j.p1);
+        const volatile int *idx = reinterpret_cast<const volatile int *>(j.p2);
+        for (long long i = tid; i < k; i += nth) {
+            const int x = idx[i];
+            dst[x] = __ldcg(src + x);
+        }
+        break;
+    }
+    case SVC_COPY_WORDS: {
+        uint32_t *dst = reinterpret_cast<uint32_t *>(j.p0);
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(j.p1);
+        // 16-byte body when both ends allow it (device allocations do)
+        long long head = 0;
+        if (((j.p0 | j.p1) & 15) == 0) {
+            // eight loads in flight per thread (one CTA must still stream)
+            const long long k4 = k / 4;
+            uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+            const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+            long long i = tid;
+            for (; i + 7 * nth < k4; i += 8 * nth) {
+                uint4 r[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) r[u] = __ldcg(s4 + i + u * nth);
+#pragma unroll
+                for (int u = 0; u < 8; u++) d4[i + u * nth] = r[u];
+            }
+            for (; i < k4; i += nth) d4[i] = __ldcg(s4 + i);
+            head = 4 * k4;
+        }
+        for (long long i = head + tid; i < k; i += nth) dst[i] = __ldcg(src + i);
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+__global__ void k_svc(SvcSub j) {
+    svc_sub(j, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// Service CTA of a serving launch: runs the graph maintenance jobs of update
+// batches while the search slots hold every SM.  It leaves when the slots
+// close (or on pause).
+__device__ void service_loop(const BatchArgs &A) {
+    __shared__ SvcSub sub[SVC_MAX_SUB];
+    __shared__ int job[3];  // run?, nsub, seq
+    for (;;) {
+        if (threadIdx.x == 0) {
+            job[0] = 0;
+            for (;;) {
+                const int seq = A.svc->seq;
+                if (seq != A.svc->done) {
+                    A.svc->taken = seq;
+                    __threadfence_system();
+                    const int ns = min(max(A.svc->nsub, 0), SVC_MAX_SUB);
+                    for (int i = 0; i < ns; i++) {
+                        const volatile SvcSub &x = A.svc->sub[i];
+                        sub[i].kind = x.kind;
+                        sub[i].k = x.k;
+                        sub[i].p0 = x.p0;
+                        sub[i].p1 = x.p1;
+                        sub[i].p2 = x.p2;
+                        sub[i].p3 = x.p3;
+                    }
+                    job[0] = 1;
+                    job[1] = ns;
+                    job[2] = seq;
+                    break;
+                }
+                if (*(volatile int *)A.closing || *A.pause) break;
+                __nanosleep(2000);
+            }
+        }
+        __syncthreads();
+        if (!job[0]) return;
+        for (int i = 0; i < job[1]; i++) {
+            svc_sub(sub[i], threadIdx.x, blockDim.x);
+            __syncthreads();  // subs run in order
+        }
+        __threadfence_system();
+        __syncthreads();
+        if (threadIdx.x == 0) A.svc->done = job[2];
+        __syncthreads();
+    }
+}
+
 template <int HK>
 __global__ void __launch_bounds__(512, 2) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
     __shared__ WarpRows wrows[MAX_WARPS];
     __shared__ CtaQ sq;
+    if (A.svc && (int)blockIdx.x == A.serve_slots) {
+        service_loop(A);
+        return;
+    }
     if (A.group <= 1) {
         SlotBufs B = slot_of(sa, blockIdx.x);
         CtaGroup grp{&B.ctl->status};
@@ -333,6 +522,17 @@ static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CA
 int64_t bfs_budget(int32_t n) { return std::max<int64_t>(4096, (int64_t)n / 32); }
 
 // Launches the persistent slot kernel for heuristic kind `hkind`.
+cudaError_t svc_run_direct(const SvcSub *subs, int nsub, cudaStream_t st) {
+    for (int i = 0; i < nsub; i++) {
+        if (subs[i].k <= 0) continue;
+        const long long blocks = std::min<long long>((subs[i].k + 255) / 256, 4L * device_sms());
+        k_svc<<<(unsigned)blocks, 256, 0, st>>>(subs[i]);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaStreamSynchronize(st);
+}
+
 cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
                          cudaStream_t st) {
     void *args[] = {&G, &sa, &A};
@@ -432,6 +632,7 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
     std::lock_guard<std::mutex> lk(g->mu);
     ddp_heuristic *h = new ddp_heuristic();
     h->g = g;
+    graph_ref(g);
     h->kind = kind;
     h->target = target;
     std::vector<int32_t> host;
@@ -546,6 +747,7 @@ int ddp_heuristic_free(ddp_heuristic *h) {
     if (!h) return DDP_OK;
     cudaFree(h->d_hops);
     cudaFree(h->d_h);
+    graph_unref(h->g);
     delete h;
     return DDP_OK;
 }
@@ -760,9 +962,17 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     A.pub = nullptr;
     A.pause = nullptr;
     A.idle_limit = 0;
+    A.idle_votes = nullptr;
+    A.closing = nullptr;
+    A.serve_slots = 0;
+    A.svc = nullptr;
     A.done = nullptr;
     A.ver = nullptr;
     A.version = 0;
+    A.vtab = nullptr;
+    A.nver = 0;
+    A.cur_ver = nullptr;
+    A.inflight = nullptr;
     A.K = b->o.K;
     A.group = b->group;
     A.sync_engine = (b->o.flags & DDP_OPT_SYNC) != 0;
@@ -797,6 +1007,7 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_batch *b = new ddp_batch();
     b->g = g;
+    graph_ref(g);
     b->hkind = hkind;
     if (opts) b->o = *opts;
     b->block = b->o.block > 0 ? std::min(b->o.block, 512) : 512;
@@ -1045,6 +1256,7 @@ int ddp_batch_free(ddp_batch *b) {
     cudaFree(b->d_t1);
     cudaFree(b->d_work);
     if (b->stream && !b->o.stream) cudaStreamDestroy(b->stream);
+    graph_unref(b->g);
     delete b;
     return DDP_OK;
 }

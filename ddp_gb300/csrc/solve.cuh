@@ -21,6 +21,28 @@ struct SlotArrays {
     uint32_t *epoch = nullptr;            // nslots: per-query tag counter of the hop array
 };
 
+// Graph maintenance jobs of a serving launch, run by its service CTA (or by
+// k_svc when no serving kernel runs).  Lists live in host memory mapped into
+// the device.  Kinds (k elements):
+//   SVC_SCATTER_ARCS  ((uint2 *)p0)[((long long *)p2)[i]] = ((uint2 *)p3)[i]
+//   SVC_SCATTER_ROWS  r = ((int4 *)p2)[i]: ((int *)p0)[r.x] = r.y, ((int *)p1)[r.x] = r.z
+//   SVC_GATHER_ARCS   j = ((long long *)p2)[i]: ((uint2 *)p0)[j] = ((uint2 *)p1)[j]
+//   SVC_GATHER_INTS   j = ((int *)p2)[i]: ((int *)p0)[j] = ((int *)p1)[j]
+//   SVC_COPY_WORDS    ((uint32_t *)p0)[i] = ((uint32_t *)p1)[i]
+enum { SVC_SCATTER_ARCS = 0, SVC_SCATTER_ROWS, SVC_GATHER_ARCS, SVC_GATHER_INTS, SVC_COPY_WORDS };
+struct SvcSub {
+    int kind, pad;
+    long long k;
+    unsigned long long p0, p1, p2, p3;
+};
+constexpr int SVC_MAX_SUB = 8;
+// The host fills nsub and sub[] and publishes seq; the service CTA marks
+// taken = seq, runs the subs in order, and marks done = seq.
+struct SvcJob {
+    int seq, taken, done, nsub;
+    SvcSub sub[SVC_MAX_SUB];
+};
+
 struct BatchArgs {
     const int32_t *S, *T;
     int32_t nq;
@@ -39,13 +61,24 @@ struct BatchArgs {
     int serve;
     const volatile int *pub;    // published request count
     const volatile int *pause;  // non-zero: stop claiming, exit
-    int idle_limit;             // polls (~1 us each) before an idle slot exits
+    int idle_limit;             // polls (~1 us each) before a slot votes to exit
+    int *idle_votes;            // slots that found no work for idle_limit polls
+    int *closing;               // set once every slot voted: all slots exit
+    int serve_slots;            // search slots in the launch
+    volatile SvcJob *svc;       // non-null: CTA serve_slots is the service CTA
     volatile int *done;         // per request: 1 once cost/ver are written
     int32_t *ver;               // per request: graph version it ran on
     int version;
+    // versioned graphs (serving): version v lives in vtab[v % nver]
+    const DevGraph *vtab;         // host memory, rewritten while the kernel runs
+    int nver;
+    const volatile int *cur_ver;  // latest published version (host memory)
+    int *inflight;                // per buffer: searches running on it (host memory)
 };
 
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops);
+// Runs maintenance subs with ordinary launches on st (no serving kernel runs).
+cudaError_t svc_run_direct(const SvcSub *subs, int nsub, cudaStream_t st);
 int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, bool hops,
                 cudaStream_t st);
 void slots_free(SlotArrays &sa);

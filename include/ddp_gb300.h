@@ -199,9 +199,11 @@ int ddp_dyn_free(ddp_dyn *d);
 typedef struct ddp_server ddp_server;
 /* Slots (one CTA each, fixed queue/state footprint; as many as fit in half of
  * free device memory) serve requests published in a ring of max_requests
- * entries in pinned host memory mapped into the device. */
+ * entries in pinned host memory mapped into the device.  The graph is kept
+ * in `versions` (2..64) device copies so that updates never stop searches
+ * in flight; the graph switches to the dynamic layout. */
 int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t max_requests,
-                     ddp_server **out);
+                     int32_t versions, ddp_server **out);
 /* Publishes n requests; *first_id = id of the first.  Non-blocking. */
 int ddp_serve_submit(ddp_server *s, int32_t n, const int32_t *sources, const int32_t *targets,
                      int64_t *first_id);
@@ -210,8 +212,9 @@ int ddp_serve_submit(ddp_server *s, int32_t n, const int32_t *sources, const int
  * may be NULL.  Non-blocking except for rare re-runs of oversized searches. */
 int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int64_t *latency_ns,
                    int32_t *versions, int32_t *nout);
-/* Applies an update batch (ddp_dyn_update flags) between requests: claiming
- * pauses, running searches finish, the graph changes, the version bumps. */
+/* Applies an update batch (ddp_dyn_update flags): the master graph changes
+ * and is published as the next version once its ring buffer is free;
+ * searches already running keep the version they started on. */
 int ddp_serve_update(ddp_server *s, int32_t n, const int32_t *flag, const int32_t *u, const int32_t *v,
                      const uint32_t *w);
 /* submitted, completed, slots, kernel launches, graph version, re-runs */

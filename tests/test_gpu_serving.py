@@ -57,17 +57,19 @@ def test_serving_mix_equals_alone_and_oracle(gpu, oracle):
     srv.close()
 
 
-def test_serving_with_updates(gpu, oracle):
-    """Weight changes, deletes and inserts between requests: each answer
+@pytest.mark.parametrize("nver,rounds", [(8, 4), (2, 8)])
+def test_serving_with_updates(gpu, oracle, nver, rounds):
+    """Weight changes, deletes and inserts between requests while searches
+    run (the graph ring is reused when rounds >= versions): each answer
     equals the oracle on the graph version it reports."""
     d = gpu
     g, dg = _geo(d, 20_000, 41)
-    srv = d.Server(dg, d.H_EUCLID, max_requests=4096, grid=32)
+    srv = d.Server(dg, d.H_EUCLID, max_requests=4096, versions=nver, grid=32)
     rng = np.random.default_rng(5)
     versions = [(g.off.copy(), g.col.copy(), g.w.copy(), d.euclid_rho_fp(g))]
     off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
     submitted = []
-    for rnd in range(4):
+    for rnd in range(rounds):
         S = rng.integers(0, g.n, 40).astype(np.int32)
         T = rng.integers(0, g.n, 40).astype(np.int32)
         srv.submit(S, T)
@@ -99,5 +101,5 @@ def test_serving_with_updates(gpu, oracle):
         gv = d.CSR(g.n, vo, vc, vw, xy=g.xy)
         want = _oracle(oracle, gv, s_, t_, 0)  # h = 0: the cost does not depend on h
         assert costs[k] == want, (i, int(ver[k]))
-    assert srv.stats()["version"] == 4
+    assert srv.stats()["version"] == rounds
     srv.close()
