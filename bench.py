@@ -69,7 +69,8 @@ def args_parse():
     p.add_argument("--delta", type=int, default=0)
     p.add_argument("--K", type=int, default=0)
     p.add_argument("--group", type=int, default=19, help="CTAs per query slot")
-    p.add_argument("--heuristic", default="capped", choices=["capped", "bfs", "zero"],
+    p.add_argument("--landmarks", type=int, default=16, help="landmark count for --heuristic landmark")
+    p.add_argument("--heuristic", default="capped", choices=["capped", "bfs", "zero", "landmark"],
                    help="capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
                         "get last level + 1); bfs: full reverse BFS; zero: h = 0")
     p.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
@@ -138,11 +139,12 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch(config_name, pairs):
+def traffic_per_launch(config_name, pairs, heuristic="capped"):
     """dram bytes of one k_batch launch from the committed ncu summary
-    (profiles/k_batch_<config>.md, line `traffic_bytes_per_query: X`), scaled
-    to this launch's query count."""
-    p = os.path.join(ROOT, "profiles", f"k_batch_{config_name}.md")
+    (profiles/k_batch_<config>[_<heuristic>].md, line
+    `traffic_bytes_per_query: X`), scaled to this launch's query count."""
+    suffix = "" if heuristic == "capped" else f"_{heuristic}"
+    p = os.path.join(ROOT, "profiles", f"k_batch_{config_name}{suffix}.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_query:"):
@@ -152,13 +154,17 @@ def traffic_per_launch(config_name, pairs):
     return None
 
 
-def algorithmic_bytes(st):
+def algorithmic_bytes(st, landmarks=0):
     """Per-query bytes of the algorithm (graph-search accounting):
     12 B per expanded node (2 offsets + g), 16 B per scanned arc (head, w,
     h(head), g(head)), 16 B per successful relaxation (g, parent, queue
     push), and for the heuristic BFS 12 B per reached node + 8 B per scanned
-    reverse arc."""
+    reverse arc.  With L landmarks h is read only for a relaxation that
+    improves g: 12 B per scanned arc and 16 + 8 L B per relaxation (the
+    node's landmark row), no BFS."""
     st = np.asarray(st, np.float64)
+    if landmarks:
+        return 12 * st[:, 0] + 12 * st[:, 1] + (16 + 8 * landmarks) * st[:, 2]
     return 12 * st[:, 0] + 16 * st[:, 1] + 16 * st[:, 2] + 12 * st[:, 4] + 8 * st[:, 5]
 
 
@@ -482,7 +488,16 @@ def main():
     # time the steps are recorded on it
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
-    hkind = {"capped": d.H_BFS_CAPPED, "bfs": d.H_BFS_HOPS, "zero": d.H_ZERO}[a.heuristic]
+    hkind = {"capped": d.H_BFS_CAPPED, "bfs": d.H_BFS_HOPS, "zero": d.H_ZERO,
+             "landmark": d.H_LANDMARK}[a.heuristic]
+    lm = a.landmarks if a.heuristic == "landmark" else 0
+    lm_s = None
+    if lm:
+        # per-graph preprocessing (2 x L exhaustive searches), outside the timed region
+        torch.cuda.synchronize(dev)
+        l0 = time.perf_counter()
+        dg.build_landmarks(lm, seed=c["gseed"])
+        lm_s = time.perf_counter() - l0
     opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group)
     be = d.BatchEngine(dg, hkind, stream=stream.cuda_stream, **opts)
     dS = torch.from_numpy(S).to(dev)
@@ -524,10 +539,10 @@ def main():
     launches = be.launches() * a.steps
     value = world * pairs * a.steps / tmax
     kernel_s = elapsed / a.steps
-    alg = float(algorithmic_bytes(st).sum())
+    alg = float(algorithmic_bytes(st, lm).sum())
     peak, peak_kind = peak_hbm()
     achieved = alg / kernel_s / 1e9
-    traffic = traffic_per_launch(a.config, pairs)
+    traffic = traffic_per_launch(a.config, pairs, a.heuristic)
     lat_service = (t1 - t0) / 1e6
     lat_complete = (t1 - t0.min()) / 1e6
 
@@ -584,7 +599,8 @@ def main():
         "ms_per_step": 1000 * tmax / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)",
         "config": {"workload": workload_name(c), "n": g.n, "e": g.e, "pairs_per_gpu": pairs,
-                   "heuristic": a.heuristic,
+                   "heuristic": a.heuristic, "landmarks": lm or None,
+                   "landmark_build_s": lm_s,
                    "slots": be.info()["slots"], "block": be.info()["block"], "K": a.K,
                    "group": be.info()["group"],
                    "delta": a.delta or "auto",
@@ -598,7 +614,8 @@ def main():
         "speedup_vs_plain": (value / world / plain["qps"]) if plain else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_batch<1>", "algorithmic_bytes_per_launch": alg,
+                     "kernel": {"landmark": "k_batch<4>", "zero": "k_batch<0>"}.get(a.heuristic, "k_batch<1>"),
+                     "algorithmic_bytes_per_launch": alg,
                      "kernel_ms": 1000 * kernel_s},
         "work_per_query": {"phases_mean": float(st[:, 3].mean()), "expanded_mean": float(st[:, 0].mean()), "arcs_scanned_mean": float(st[:, 1].mean()),
                            "relaxed_mean": float(st[:, 2].mean()), "bfs_reached_mean": float(st[:, 4].mean()),

@@ -24,7 +24,7 @@ import numpy as np
 
 from ._lib import DdpError, Opts, check, lib, ptr  # noqa: F401
 
-H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED, H_EUCLID = 0, 1, 2, 3, 4, 5
+H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED, H_EUCLID, H_LANDMARK = 0, 1, 2, 3, 4, 5, 6
 INF = 2147483647
 # per-query counters: expanded, scanned, relaxed, phases, bfs_reached,
 # bfs_scanned, far_scanned, touched
@@ -347,6 +347,12 @@ class DeviceGraph:
 
     def set_euclid(self, rho_fp: int) -> None:
         check(lib().ddp_graph_set_euclid(self.handle, int(rho_fp)))
+
+    def build_landmarks(self, count: int = 16, seed: int = 1) -> np.ndarray:
+        """Landmark table for H_LANDMARK; returns the landmark ids."""
+        ids = np.empty(count, np.int32)
+        check(lib().ddp_landmarks_build(self.handle, int(count), int(seed), ptr(ids)))
+        return ids
 
     def info(self):
         n, e, lo, hi = C.c_int32(), C.c_int64(), C.c_uint32(), C.c_uint32()

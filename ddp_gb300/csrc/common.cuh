@@ -69,7 +69,13 @@ struct DevGraph {
     // Null for static graphs, where row u ends at off[u+1].
     const int32_t *oend;
     const int32_t *roend;
+    // Landmark distances (ALT heuristic), null when not built: row v holds
+    // lm_L values d(L_i, v) then lm_L values d(v, L_i), LM_UNREACHED when
+    // there is no path.  lm_L is a multiple of 4 (rows of int4).
+    const int4 *lm;
+    int32_t lm_L;
 };
+constexpr int32_t LM_UNREACHED = 0x7FFFFFFF;
 
 __device__ __forceinline__ int row_end(const int32_t *off, const int32_t *oend, int u) {
     return oend ? __ldcg(oend + u) : __ldg(off + u + 1);

@@ -557,6 +557,7 @@ int dyn_graph_prepare(ddp_graph *g) {
 // uploads the touched slots.  ups receives the search-relevant updates.
 int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
                     const uint32_t *w, std::vector<int4> &ups) {
+    g->update_count++;  // landmark distances no longer hold
     int rcp = dyn_graph_prepare(g);
     if (rcp) return rcp;
     DynMirror *m = g->dyn;

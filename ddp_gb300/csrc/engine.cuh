@@ -146,6 +146,41 @@ struct HeurManhattan {
     }
 };
 
+// ALT lower bound: max over landmarks L of d(L,t) - d(L,v) and d(v,L) - d(t,L)
+// (triangle inequality, so admissible and consistent).  A landmark that
+// reaches v but not t, or is reached from t but not from v, proves that v
+// cannot reach t.
+struct HeurALT {
+    const int4 *tab;  // DevGraph::lm
+    int32_t L;        // landmarks, a multiple of 4
+    int32_t t;
+    __device__ __forceinline__ static void term(int32_t a, int32_t b, int32_t &h, bool &cut) {
+        // a - b with a from the row that must be larger
+        if (a != LM_UNREACHED && b != LM_UNREACHED) h = max(h, a - b);
+        else if (a == LM_UNREACHED && b != LM_UNREACHED) cut = true;
+    }
+    __device__ uint32_t operator()(int32_t v) const {
+        const int W = L >> 2;
+        const int4 *rv = tab + (size_t)v * (2 * W);
+        const int4 *rt = tab + (size_t)t * (2 * W);
+        int32_t h = 0;
+        bool cut = false;
+        for (int i = 0; i < W; i++) {
+            const int4 fv = __ldg(rv + i), ft = __ldg(rt + i);
+            const int4 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
+            term(ft.x, fv.x, h, cut);
+            term(ft.y, fv.y, h, cut);
+            term(ft.z, fv.z, h, cut);
+            term(ft.w, fv.w, h, cut);
+            term(bv.x, bt.x, h, cut);
+            term(bv.y, bt.y, h, cut);
+            term(bv.z, bt.z, h, cut);
+            term(bv.w, bt.w, h, cut);
+        }
+        return cut ? INF_G : (uint32_t)h;
+    }
+};
+
 // floor(sqrt(x)) for x < 2^62, exact: a float estimate, then integer fix-up
 __host__ __device__ __forceinline__ uint64_t isqrt_floor(uint64_t x) {
     uint64_t r = (uint64_t)sqrt((double)x);
@@ -289,6 +324,7 @@ struct SearchParams {
                    // state stays resumable after graph updates
     int resume;    // continue from the slot's far pile instead of starting at s
     int no_touch_log;  // do not log first touches (slots that are never reset)
+    // t < 0: no target, the search settles everything reachable from s
 };
 
 struct SearchResult {
@@ -351,8 +387,8 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     for (;;) {
         const int PH = (it + 1) & 3, RS = (it + 3) & 3;
         // f(t) snapshot: only decreases, so a stale value only prunes less.
-        const uint64_t st_t = __ldcg(B.state + P.t);
-        const uint32_t ht = H(P.t);
+        const uint64_t st_t = P.t >= 0 ? __ldcg(B.state + P.t) : ~0ull;
+        const uint32_t ht = P.t >= 0 ? H(P.t) : 0u;
         const uint64_t ft64 = (uint64_t)st_g(st_t) + ht;
         const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
         int64_t end = 0;
@@ -602,8 +638,8 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     }
     grp.sync();
     SearchResult r;
-    const uint64_t st_t = __ldcg(B.state + P.t);
-    const uint64_t c = (uint64_t)st_g(st_t) + H(P.t);
+    const uint64_t st_t = P.t >= 0 ? __ldcg(B.state + P.t) : ~0ull;
+    const uint64_t c = (uint64_t)st_g(st_t) + (P.t >= 0 ? H(P.t) : 0u);
     r.cost = (st_g(st_t) >= INF_G || c >= INF_G) ? 0xFFFFFFFFu : (uint32_t)c;
     r.iters = it;
     if (grp.rank() == 0) ctl->iters = it;

@@ -97,8 +97,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
             // ---- drain the bucket asynchronously -----------------------
             int c_f = 0, c_t = 0, c_loc = 0;  // staged far pushes, touches, own children
             for (;;) {
-                const uint64_t st_t = __ldcg(B.state + P.t);
-                const uint64_t ft64 = (uint64_t)st_g(st_t) + H(P.t);
+                const uint64_t st_t = P.t >= 0 ? __ldcg(B.state + P.t) : ~0ull;
+                const uint64_t ft64 = (uint64_t)st_g(st_t) + (P.t >= 0 ? H(P.t) : 0u);
                 const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
                 // 1. take work: own children first, else claim from the ring
                 int n = 0;
@@ -283,8 +283,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
         }
         // ---- split the far pile at Tsplit ---------------------------------
         {
-            const uint64_t st_t = __ldcg(B.state + P.t);
-            const uint64_t ft64 = (uint64_t)st_g(st_t) + H(P.t);
+            const uint64_t st_t = P.t >= 0 ? __ldcg(B.state + P.t) : ~0ull;
+            const uint64_t ft64 = (uint64_t)st_g(st_t) + (P.t >= 0 ? H(P.t) : 0u);
             const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
             unsigned int local_min = 0xFFFFFFFFu;
             int c_n = 0, c_f = 0;
@@ -368,8 +368,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
     }
     __syncthreads();
     SearchResult r;
-    const uint64_t st_t = __ldcg(B.state + P.t);
-    const uint64_t c = (uint64_t)st_g(st_t) + H(P.t);
+    const uint64_t st_t = P.t >= 0 ? __ldcg(B.state + P.t) : ~0ull;
+    const uint64_t c = (uint64_t)st_g(st_t) + (P.t >= 0 ? H(P.t) : 0u);
     r.cost = (st_g(st_t) >= INF_G || c >= INF_G) ? 0xFFFFFFFFu : (uint32_t)c;
     r.iters = phases;
     return r;

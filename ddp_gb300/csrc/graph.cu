@@ -68,6 +68,9 @@ DevGraph graph_view(const ddp_graph *g) {
     d.drarc = g->d_drarc;
     d.oend = g->d_oend;
     d.roend = g->d_roend;
+    const bool lm_ok = g->d_lm && g->lm_stamp == g->update_count;
+    d.lm = lm_ok ? g->d_lm : nullptr;
+    d.lm_L = lm_ok ? g->lm_L : 0;
     return d;
 }
 
@@ -156,6 +159,7 @@ void graph_release(ddp_graph *g) {
     cudaFree(g->d_drarc);
     cudaFree(g->d_oend);
     cudaFree(g->d_roend);
+    cudaFree(g->d_lm);
     dyn_mirror_free(g->dyn);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;

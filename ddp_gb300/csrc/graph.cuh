@@ -57,6 +57,13 @@ struct ddp_graph {
     bool defer_free = false;
     int64_t layout_gen = 0;  // bumps when the whole dynamic layout is uploaded again
     std::vector<void *> deferred;
+    int64_t update_count = 0;  // update batches applied (dynamic graphs)
+    // landmark distances for the ALT heuristic (DevGraph::lm), built for
+    // the graph as it was at update_count == lm_stamp
+    int4 *d_lm = nullptr;
+    int32_t lm_L = 0;
+    int64_t lm_stamp = -1;
+    std::vector<int32_t> lm_ids;
     // single-query workspace, allocated on first use
     struct Workspace *ws = nullptr;
 };

@@ -126,6 +126,37 @@ __global__ void __launch_bounds__(512, 2)
     }
 }
 
+// ---- landmarks (ALT heuristic) ---------------------------------------------
+
+// Exhaustive search from P.s (P.t < 0) over the whole grid; dist[v] = d(s, v)
+// or LM_UNREACHED.
+__global__ void __launch_bounds__(512, 2)
+    k_sssp(DevGraph G, SlotArrays sa, SearchParams P, int32_t *dist, int32_t *out) {
+    __shared__ WarpRows wrows[MAX_WARPS];
+    SlotBufs B = slot_of(sa, 0);
+    GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
+    run_search(grp, G, B, HeurZero{}, P, wrows);  // ends on a group barrier
+    for (int64_t v = grp.rank(); v < G.n; v += grp.size()) {
+        const uint32_t gv = st_g(__ldcg(B.state + v));
+        dist[v] = gv >= INF_G ? LM_UNREACHED : (int32_t)gv;
+    }
+    if (grp.rank() == 0) out[2] = B.ctl->status;
+}
+
+// tab row v, column c <- dist[v]
+__global__ void k_put_column(int32_t *tab, int32_t width, int32_t c, const int32_t *dist, int32_t n) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) tab[v * width + c] = dist[v];
+}
+
+// h(v) of the landmark heuristic for target t (INF_G -> -1)
+__global__ void k_alt_values(DevGraph G, int32_t t, int32_t *out) {
+    const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= G.n) return;
+    const uint32_t h = HeurALT{G.lm, G.lm_L, t}(v);
+    out[v] = h >= INF_G ? -1 : (int32_t)h;
+}
+
 // Batched GA*: each slot is a group of CTAs (one CTA, or `group` CTAs of a
 // cooperative launch) that claims queries from a shared counter, so groups
 // finishing short searches take the next query (dynamic load balance over
@@ -275,6 +306,8 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         } else if (HK == 3) {
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
             r = slot_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows, sq, async);
+        } else if (HK == 4) {
+            r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, t}, P, wrows, sq, async);
         } else {
             r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
         }
@@ -517,6 +550,15 @@ static cudaError_t coop_launch(K kernel, int grid, int block, void **args, cudaS
 
 static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CAPPED; }
 
+// The batch kernel instance for a heuristic kind.
+static const void *batch_kernel(int hkind) {
+    if (is_bfs_kind(hkind)) return (const void *)k_batch<1>;
+    if (hkind == DDP_H_MANHATTAN) return (const void *)k_batch<2>;
+    if (hkind == DDP_H_EUCLID) return (const void *)k_batch<3>;
+    if (hkind == DDP_H_LANDMARK) return (const void *)k_batch<4>;
+    return (const void *)k_batch<0>;
+}
+
 // Nodes a capped heuristic BFS reaches before it stops (at the end of the
 // level that crosses this count).
 int64_t bfs_budget(int32_t n) { return std::max<int64_t>(4096, (int64_t)n / 32); }
@@ -536,20 +578,14 @@ cudaError_t svc_run_direct(const SvcSub *subs, int nsub, cudaStream_t st) {
 cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
                          cudaStream_t st) {
     void *args[] = {&G, &sa, &A};
-    const void *fn = is_bfs_kind(hkind)           ? (const void *)k_batch<1>
-                     : (hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
-                     : (hkind == DDP_H_EUCLID)    ? (const void *)k_batch<3>
-                                                  : (const void *)k_batch<0>;
+    const void *fn = batch_kernel(hkind);
     if (coop) return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, st);
     return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st);
 }
 
 int slots_per_sm(int hkind, int block) {
     int per_sm = 0;
-    const void *fn = is_bfs_kind(hkind)           ? (const void *)k_batch<1>
-                     : (hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
-                     : (hkind == DDP_H_EUCLID)    ? (const void *)k_batch<3>
-                                                  : (const void *)k_batch<0>;
+    const void *fn = batch_kernel(hkind);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
     return per_sm;
 }
@@ -635,7 +671,10 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
     graph_ref(g);
     h->kind = kind;
     h->target = target;
-    std::vector<int32_t> host;
+    auto bail = [&](int rc) {
+        ddp_heuristic_free(h);
+        return rc;
+    };
     switch (kind) {
     case DDP_H_ZERO:
         if (out_h) std::fill(out_h, out_h + g->n, 0);
@@ -643,15 +682,9 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
     case DDP_H_BFS_HOPS:
     case DDP_H_BFS_CAPPED: {
         int rc = workspace_ensure(g, (int64_t)g->n + 1024);
-        if (rc) {
-            delete h;
-            return rc;
-        }
+        if (rc) return bail(rc);
         cudaError_t e = cudaMalloc(&h->d_hops, sizeof(uint32_t) * (size_t)g->n);
-        if (e != cudaSuccess) {
-            delete h;
-            return cuda_fail(e, "cudaMalloc(hops)");
-        }
+        if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(hops)"));
         DevGraph G = graph_view(g);
         SlotArrays sa = g->ws->sa;
         DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl), g->stream));
@@ -659,20 +692,13 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
         long long budget = kind == DDP_H_BFS_CAPPED ? (long long)bfs_budget(g->n) : 0;
         void *args[] = {&G, &sa, &h->d_hops, &target, &budget};
         e = coop_launch(k_bfs_single, grid, 512, args, g->stream);
-        if (e != cudaSuccess) {
-            cudaFree(h->d_hops);
-            delete h;
-            return cuda_fail(e, "k_bfs_single launch");
-        }
+        if (e != cudaSuccess) return bail(cuda_fail(e, "k_bfs_single launch"));
         SearchCtl ctl;
         DDP_CUDA(cudaMemcpyAsync(&ctl, sa.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, g->stream));
         DDP_CUDA(cudaStreamSynchronize(g->stream));
-        if (ctl.status & (ST_OVERFLOW | ST_TIMEOUT)) {
-            cudaFree(h->d_hops);
-            delete h;
-            return fail(ctl.status & ST_TIMEOUT ? DDP_ERR_TIMEOUT : DDP_ERR_QUEUE_OVERFLOW,
-                        "heuristic BFS did not complete");
-        }
+        if (ctl.status & (ST_OVERFLOW | ST_TIMEOUT))
+            return bail(fail(ctl.status & ST_TIMEOUT ? DDP_ERR_TIMEOUT : DDP_ERR_QUEUE_OVERFLOW,
+                             "heuristic BFS did not complete"));
         h->cap = ctl.hcap;
         if (out_h) {
             std::vector<uint32_t> hops((size_t)g->n);
@@ -690,10 +716,7 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
         break;
     }
     case DDP_H_MANHATTAN: {
-        if (!g->d_xy) {
-            delete h;
-            return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
-        }
+        if (!g->d_xy) return bail(fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)"));
         h->tx = g->h_xy[2 * (size_t)target];
         h->ty = g->h_xy[2 * (size_t)target + 1];
         if (out_h)
@@ -705,10 +728,7 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
         break;
     }
     case DDP_H_EUCLID: {
-        if (!g->d_xy) {
-            delete h;
-            return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
-        }
+        if (!g->d_xy) return bail(fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)"));
         h->tx = g->h_xy[2 * (size_t)target];
         h->ty = g->h_xy[2 * (size_t)target + 1];
         if (out_h)
@@ -721,26 +741,168 @@ int ddp_heuristic_build(ddp_graph *g, int32_t target, int32_t kind, const int32_
         break;
     }
     case DDP_H_USER: {
-        if (!user_h) {
-            delete h;
-            return fail(DDP_ERR_INVALID, "user_h is null");
-        }
+        if (!user_h) return bail(fail(DDP_ERR_INVALID, "user_h is null"));
         cudaError_t e = cudaMalloc(&h->d_h, sizeof(int32_t) * (size_t)g->n);
-        if (e != cudaSuccess) {
-            delete h;
-            return cuda_fail(e, "cudaMalloc(h)");
-        }
+        if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(h)"));
         DDP_CUDA(cudaMemcpy(h->d_h, user_h, sizeof(int32_t) * (size_t)g->n,
                             cudaMemcpyHostToDevice));
         if (out_h) std::memcpy(out_h, user_h, sizeof(int32_t) * (size_t)g->n);
         break;
     }
+    case DDP_H_LANDMARK: {
+        const DevGraph G = graph_view(g);
+        if (!G.lm) return bail(fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)"));
+        if (out_h) {
+            int32_t *d = nullptr;
+            cudaError_t e = cudaMalloc(&d, sizeof(int32_t) * (size_t)g->n);
+            if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(h)"));
+            k_alt_values<<<(g->n + 255) / 256, 256, 0, g->stream>>>(G, target, d);
+            e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(out_h, d, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+            cudaFree(d);
+            if (e != cudaSuccess) return bail(cuda_fail(e, "landmark heuristic values"));
+        }
+        break;
+    }
     default:
-        delete h;
-        return fail(DDP_ERR_INVALID, "unknown heuristic kind");
+        return bail(fail(DDP_ERR_INVALID, "unknown heuristic kind"));
     }
     *out = h;
     return DDP_OK;
+}
+
+}  // extern "C"
+
+namespace ddp {
+// d(src, v) for every v (reverse: d(v, src)) into the device array dist.
+static int sssp_into(ddp_graph *g, int32_t src, bool reverse, int32_t *dist) {
+    DevGraph G = graph_view(g);
+    if (reverse) {
+        std::swap(G.off, G.roff);
+        std::swap(G.arc, G.rarc);
+        std::swap(G.oend, G.roend);
+        std::swap(G.doff, G.droff);
+        std::swap(G.darc, G.drarc);
+    }
+    SearchParams P{src, -1, auto_delta(g), 0, 0, 0, 0};
+    int64_t cap = (int64_t)g->n + 1024;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        int rc = workspace_ensure(g, cap);
+        if (rc) return rc;
+        Workspace *w = g->ws;
+        DDP_CUDA(cudaMemsetAsync(w->sa.ctl, 0, sizeof(SearchCtl), g->stream));
+        const int grid = coop_grid(k_sssp, 512, 0);
+        void *args[] = {&G, &w->sa, &P, &dist, &w->d_out};
+        cudaError_t e = coop_launch(k_sssp, grid, 512, args, g->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "k_sssp launch");
+        DDP_CUDA(cudaMemsetAsync(w->sa.q, 0xFF, sizeof(uint2) * (size_t)w->sa.cap_q * 2, g->stream));
+        k_reset_touched<<<dim3(256, 1), 256, 0, g->stream>>>(w->sa);
+        DDP_CUDA(cudaGetLastError());
+        int32_t res[4];
+        DDP_CUDA(cudaMemcpyAsync(res, w->d_out, sizeof(res), cudaMemcpyDeviceToHost, g->stream));
+        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        if (res[2] & ST_TIMEOUT) return fail(DDP_ERR_TIMEOUT, "landmark search barrier timed out");
+        if (res[2] & ST_OVERFLOW) {
+            cap *= 2;
+            continue;
+        }
+        return DDP_OK;
+    }
+    return fail(DDP_ERR_QUEUE_OVERFLOW, "landmark search queue overflow after retries");
+}
+}  // namespace ddp
+
+extern "C" {
+
+int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out_ids) {
+    if (!g) return fail(DDP_ERR_INVALID, "null graph");
+    if (count < 4 || count > 32 || count % 4)
+        return fail(DDP_ERR_INVALID, "landmark count must be 4, 8, ..., 32");
+    std::lock_guard<std::mutex> lk(g->mu);
+    const int32_t n = g->n;
+    const int32_t width = 2 * count;
+    int32_t *dist = nullptr, *tab = nullptr;
+    cudaError_t e = cudaMalloc(&dist, sizeof(int32_t) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&tab, sizeof(int32_t) * (size_t)n * width);
+    if (e != cudaSuccess) {
+        cudaFree(dist);
+        return cuda_fail(e, "cudaMalloc(landmarks)");
+    }
+    auto done = [&](int rc) {
+        cudaFree(dist);
+        if (rc) cudaFree(tab);
+        return rc;
+    };
+    // farthest-point selection: the next landmark maximises the smallest
+    // round trip d(L, v) + d(v, L) over the landmarks so far (nodes that no
+    // landmark relates to come first); the first one is the farthest from a
+    // seeded random node
+    std::vector<int64_t> score((size_t)n, INT64_MAX);
+    std::vector<int32_t> fw((size_t)n), bw((size_t)n);
+    auto measure = [&](int32_t src, int col) -> int {
+        int rc = sssp_into(g, src, false, dist);
+        if (rc) return rc;
+        if (col >= 0) k_put_column<<<(n + 255) / 256, 256, 0, g->stream>>>(tab, width, col, dist, n);
+        DDP_CUDA(cudaMemcpyAsync(fw.data(), dist, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, g->stream));
+        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        rc = sssp_into(g, src, true, dist);
+        if (rc) return rc;
+        if (col >= 0) k_put_column<<<(n + 255) / 256, 256, 0, g->stream>>>(tab, width, col + count, dist, n);
+        DDP_CUDA(cudaMemcpyAsync(bw.data(), dist, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, g->stream));
+        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        for (int32_t v = 0; v < n; v++) {
+            const bool f = fw[(size_t)v] != LM_UNREACHED, b = bw[(size_t)v] != LM_UNREACHED;
+            const int64_t x = (f && b) ? (int64_t)fw[(size_t)v] + bw[(size_t)v]
+                              : f       ? fw[(size_t)v]
+                              : b       ? bw[(size_t)v]
+                                        : INT64_MAX;
+            score[(size_t)v] = std::min(score[(size_t)v], x);
+        }
+        return DDP_OK;
+    };
+    uint64_t x = seed + 0x9E3779B97F4A7C15ull;  // splitmix64
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    int rc = measure((int32_t)(x % (uint64_t)n), -1);
+    if (rc) return done(rc);
+    std::vector<int32_t> ids;
+    {
+        // the first landmark: farthest (round trip) from the random node
+        int32_t best = 0;
+        int64_t bs = -1;
+        for (int32_t v = 0; v < n; v++) {
+            const bool f = fw[(size_t)v] != LM_UNREACHED, b = bw[(size_t)v] != LM_UNREACHED;
+            const int64_t y = (f ? fw[(size_t)v] : 0) + (b ? bw[(size_t)v] : 0);
+            if (y > bs) {
+                bs = y;
+                best = v;
+            }
+        }
+        ids.push_back(best);
+    }
+    std::fill(score.begin(), score.end(), INT64_MAX);
+    for (int i = 0; i < count; i++) {
+        if (i > 0) {
+            int32_t best = 0;
+            for (int32_t v = 1; v < n; v++)
+                if (score[(size_t)v] > score[(size_t)best]) best = v;
+            ids.push_back(best);
+        }
+        rc = measure(ids.back(), i);
+        if (rc) return done(rc);
+    }
+    DDP_CUDA(cudaGetLastError());
+    DDP_CUDA(cudaStreamSynchronize(g->stream));
+    cudaFree(g->d_lm);
+    g->d_lm = reinterpret_cast<int4 *>(tab);
+    g->lm_L = count;
+    g->lm_stamp = g->update_count;
+    g->lm_ids = ids;
+    if (out_ids) std::memcpy(out_ids, ids.data(), sizeof(int32_t) * (size_t)count);
+    return done(DDP_OK);
 }
 
 int ddp_heuristic_free(ddp_heuristic *h) {
@@ -761,6 +923,8 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
     if (h && h->g != g) return fail(DDP_ERR_INVALID, "heuristic belongs to another graph");
     if (h && h->kind != DDP_H_ZERO && h->target != target)
         return fail(DDP_ERR_INVALID, "heuristic was built for another target");
+    if (h && h->kind == DDP_H_LANDMARK && !graph_view(g).lm)
+        return fail(DDP_ERR_INVALID, "landmark table is stale (the graph was updated)");
     ddp_opts o = opts ? *opts : ddp_opts{};
     std::lock_guard<std::mutex> lk(g->mu);
     cudaStream_t st = o.stream ? (cudaStream_t)o.stream : g->stream;
@@ -783,12 +947,14 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             HeurManhattan Hm{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->wmin};
             HeurEuclid He{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->rho_fp};
             HeurArray Ha{h ? h->d_h : nullptr};
+            HeurALT Hl{G.lm, G.lm_L, target};
             HeurZero Hz{};
             const void *fn;
             if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) { fn = (const void *)k_solve_cta<HeurHops>; hp = &Hh; }
             else if (kind == DDP_H_MANHATTAN) { fn = (const void *)k_solve_cta<HeurManhattan>; hp = &Hm; }
             else if (kind == DDP_H_EUCLID) { fn = (const void *)k_solve_cta<HeurEuclid>; hp = &He; }
             else if (kind == DDP_H_USER) { fn = (const void *)k_solve_cta<HeurArray>; hp = &Ha; }
+            else if (kind == DDP_H_LANDMARK) { fn = (const void *)k_solve_cta<HeurALT>; hp = &Hl; }
             else { fn = (const void *)k_solve_cta<HeurZero>; hp = &Hz; }
             void *args[] = {&G, &w->sa, hp, &P, &w->d_out, &w->d_path, &g->n};
             e = cudaLaunchKernel(fn, dim3(1), dim3(block), args, 0, st);
@@ -812,6 +978,11 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             int grid = coop_grid(k_solve_single<HeurArray>, block, o.grid);
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurArray>, grid, block, args, st);
+        } else if (kind == DDP_H_LANDMARK) {
+            HeurALT H{G.lm, G.lm_L, target};
+            int grid = coop_grid(k_solve_single<HeurALT>, block, o.grid);
+            void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
+            e = coop_launch(k_solve_single<HeurALT>, grid, block, args, st);
         } else {
             HeurZero H{};
             int grid = coop_grid(k_solve_single<HeurZero>, block, o.grid);
@@ -977,6 +1148,7 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     A.group = b->group;
     A.sync_engine = (b->o.flags & DDP_OPT_SYNC) != 0;
     DevGraph G = graph_view(b->g);
+    if (b->hkind == DDP_H_LANDMARK && !G.lm) return cudaErrorInvalidValue;  // stale table
     cudaError_t e = cudaMemsetAsync(b->d_work, 0, sizeof(int) * 2, b->stream);
     if (e != cudaSuccess) return e;
     // fresh control blocks (barrier counters included) for every launch
@@ -985,10 +1157,7 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     const int grid = b->sa.nslots * b->group;
     SlotArrays sa = b->sa;
     void *args[] = {&G, &sa, &A};
-    const void *fn = is_bfs_kind(b->hkind)           ? (const void *)k_batch<1>
-                     : (b->hkind == DDP_H_MANHATTAN) ? (const void *)k_batch<2>
-                     : (b->hkind == DDP_H_EUCLID)    ? (const void *)k_batch<3>
-                                                     : (const void *)k_batch<0>;
+    const void *fn = batch_kernel(b->hkind);
     if (b->group > 1)
         return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
     return cudaLaunchKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
@@ -1001,8 +1170,12 @@ extern "C" {
 int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out) {
     if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN && hkind != DDP_H_EUCLID)
-        return fail(DDP_ERR_INVALID, "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED, MANHATTAN or EUCLID");
+    if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN && hkind != DDP_H_EUCLID &&
+        hkind != DDP_H_LANDMARK)
+        return fail(DDP_ERR_INVALID,
+                    "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED, MANHATTAN, EUCLID or LANDMARK");
+    if (hkind == DDP_H_LANDMARK && !graph_view(g).lm)
+        return fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)");
     if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID) && !g->d_xy)
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_batch *b = new ddp_batch();
@@ -1020,14 +1193,7 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     }
     // slots: occupancy-limited, then memory-limited (half of free memory)
     int per_sm = 0;
-    if (is_bfs_kind(hkind))
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, b->block, 0);
-    else if (hkind == DDP_H_MANHATTAN)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, b->block, 0);
-    else if (hkind == DDP_H_EUCLID)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<3>, b->block, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<0>, b->block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(hkind), b->block, 0);
     b->group = std::max(1, b->o.group);
     const int coresident = std::max(1, per_sm) * sm_count();
     if (b->group > coresident) b->group = coresident;

@@ -57,10 +57,16 @@ enum ddp_heuristic_kind {
     DDP_H_EUCLID = 5,    /* floor(rho * floor(|xy(v) - xy(t)|)), rho a 16.16
                             fixed-point lower bound of w / length over the arcs
                             (ddp_graph_set_euclid); integer arithmetic only    */
-    DDP_H_BFS_CAPPED = 4 /* DDP_H_BFS_HOPS with the BFS stopped after the level
+    DDP_H_BFS_CAPPED = 4, /* DDP_H_BFS_HOPS with the BFS stopped after the level
                             where it has reached max(4096, n/32) nodes; nodes
                             not reached get (last level + 1) x min weight,
                             which stays admissible and consistent            */
+    DDP_H_LANDMARK = 6   /* ALT: max over landmarks L of d(L,t) - d(L,v) and
+                            d(v,L) - d(t,L) (triangle inequality: admissible
+                            and consistent); needs ddp_landmarks_build.  No
+                            reference counterpart (the reference only has
+                            bfs_hx.cu hop counts, which carry little on random
+                            graphs)                                           */
 };
 
 typedef struct ddp_graph ddp_graph;         /* device-resident CSR + reverse CSR */
@@ -112,6 +118,15 @@ int ddp_graph_free(ddp_graph *g);
 
 /* ---- heuristic: GA_star/bfs_hx.cu (program), LIB a_star.h:34
  *      set_huiristics(U*) ------------------------------------------------ */
+/* Landmark table for DDP_H_LANDMARK: `count` (4, 8, ..., 32) landmarks picked
+ * farthest-first from a seeded start, with exact distances to and from every
+ * node (2 x count exhaustive searches on the device, count x 8 bytes per
+ * node).  out_ids (nullable) receives the landmarks.  Updates to the graph
+ * (ddp_dyn_update, ddp_serve_update) make the table stale: landmark
+ * heuristics then fail with DDP_ERR_INVALID until it is rebuilt.  No
+ * reference counterpart. */
+int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out_ids);
+
 /* Builds h for `target` on the device.  user_h (DDP_H_USER only) holds n
  * values; negative values mean "target unreachable from here".  out_h
  * (optional, n values) receives h, -1 for nodes that cannot reach target. */

@@ -1,0 +1,135 @@
+"""Landmark (ALT) heuristic: the device-built distance table against scipy's
+Dijkstra, h values against the ALT formula, and exact costs (single query
+and batched) against the oracle, including graphs where many node pairs are
+disconnected."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+UNR = 0x7FFFFFFF
+
+
+def _scipy_dists(g, ids):
+    sp = pytest.importorskip("scipy.sparse")
+    cg = pytest.importorskip("scipy.sparse.csgraph")
+    src = np.repeat(np.arange(g.n), np.diff(g.off))
+    live = g.col >= 0
+    # parallel arcs: keep the lightest (csr_matrix would add them)
+    order = np.lexsort((g.w[live], g.col[live], src[live]))
+    a, b, w = src[live][order], g.col[live][order], g.w[live][order].astype(np.float64)
+    first = np.ones(len(a), bool)
+    first[1:] = (a[1:] != a[:-1]) | (b[1:] != b[:-1])
+    A = sp.csr_matrix((w[first], (a[first], b[first])), shape=(g.n, g.n))
+    fw = cg.dijkstra(A, indices=ids)
+    bw = cg.dijkstra(A.T.tocsr(), indices=ids)
+    conv = lambda x: np.where(np.isfinite(x), np.round(x), UNR).astype(np.int64)
+    return conv(fw), conv(bw)
+
+
+def _alt(fw, bw, t):
+    """h(v) for target t from landmark distances (rows: landmarks); -1 = cut."""
+    n = fw.shape[1]
+    h = np.zeros(n, np.int64)
+    cut = np.zeros(n, bool)
+    for F, B in zip(fw, bw):
+        ok = (F[t] != UNR) & (F != UNR)
+        h = np.where(ok, np.maximum(h, F[t] - F), h)
+        cut |= (F[t] == UNR) & (F != UNR)
+        ok = (B != UNR) & (B[t] != UNR)
+        h = np.where(ok, np.maximum(h, B - B[t]), h)
+        cut |= (B == UNR) & (B[t] != UNR)
+    return np.where(cut, -1, h)
+
+
+def _oracle(O, g, s, t):
+    gs = g.with_sentinel()
+    f, c, _, _, _ = O.astar(gs.n, gs.off[:-1], gs.col, gs.w, np.zeros(gs.n, np.int32), s, t)
+    return c if f else 2147483647
+
+
+@pytest.mark.parametrize("count", [4, 16])
+def test_landmark_table_and_values(gpu, count):
+    d = gpu
+    g = d.gen_random_chain(3000, 4, 1, 50, 71)
+    dg = d.DeviceGraph.from_csr(g)
+    ids = dg.build_landmarks(count, seed=3)
+    assert len(set(ids.tolist())) == count
+    fw, bw = _scipy_dists(g, ids)
+    rng = np.random.default_rng(2)
+    for t in rng.integers(0, g.n, 6):
+        h = dg.heuristic(int(t), d.H_LANDMARK, want_values=True)
+        assert np.array_equal(h.values.astype(np.int64), _alt(fw, bw, int(t)))
+        assert h.values[t] == 0
+
+
+def test_landmark_single_and_batch_exact(gpu, oracle):
+    d = gpu
+    g = d.gen_random_chain(20000, 6, 1, 100, 72)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.build_landmarks(8, seed=5)
+    rng = np.random.default_rng(9)
+    S = rng.integers(0, g.n, 48).astype(np.int32)
+    T = rng.integers(0, g.n, 48).astype(np.int32)
+    want = np.array([_oracle(oracle, g, int(s), int(t)) for s, t in zip(S, T)])
+    for k in range(6):
+        h = dg.heuristic(int(T[k]), d.H_LANDMARK)
+        r = dg.solve(int(S[k]), int(T[k]), h)
+        assert r.cost == want[k]
+        ok, why = oracle.check_path(g.off, g.col, g.w, r.path, int(S[k]), int(T[k]), r.cost, 0)
+        assert ok, why
+    for group in (1, 4):
+        be = d.BatchEngine(dg, d.H_LANDMARK, group=group)
+        cost, _ = be.solve(S, T)
+        assert np.array_equal(cost, want), group
+        for i in range(0, 48, 11):
+            ok, why = oracle.check_path(g.off, g.col, g.w, be.path(i), int(S[i]), int(T[i]), int(cost[i]), 0)
+            assert ok, why
+
+
+def test_landmark_disconnected(gpu, oracle):
+    """Sparse random arcs (no chain): many pairs have no path; the cut rule
+    must prune only nodes that cannot reach t."""
+    d = gpu
+    rng = np.random.default_rng(4)
+    n, e = 4000, 5000
+    a = rng.integers(0, n, e)
+    b = rng.integers(0, n, e)
+    keep = a != b
+    a, b = a[keep], b[keep]
+    order = np.argsort(a, kind="stable")
+    a, b = a[order], b[order]
+    off = np.zeros(n + 1, np.int64)
+    np.add.at(off, a + 1, 1)
+    off = np.cumsum(off).astype(np.int32)
+    w = rng.integers(1, 30, len(b)).astype(np.uint32)
+    g = d.CSR(n, off, b.astype(np.int32), w)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.build_landmarks(8, seed=1)
+    S = rng.integers(0, n, 64).astype(np.int32)
+    T = rng.integers(0, n, 64).astype(np.int32)
+    # plus pairs two arcs apart (reachable)
+    u = np.flatnonzero(np.diff(off) > 0)[:200:25]
+    mid = g.col[off[u]]
+    far = np.array([g.col[off[m]] if off[m + 1] > off[m] else m for m in mid])
+    S = np.concatenate([S, u]).astype(np.int32)
+    T = np.concatenate([T, far]).astype(np.int32)
+    want = np.array([_oracle(oracle, g, int(s), int(t)) for s, t in zip(S, T)])
+    assert (want == d.INF).any() and (want != d.INF).any()
+    cost, _ = d.BatchEngine(dg, d.H_LANDMARK, group=1).solve(S, T)
+    assert np.array_equal(cost, want)
+
+
+def test_landmark_table_goes_stale(gpu):
+    d = gpu
+    g = d.gen_random_chain(2000, 4, 1, 50, 73)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.build_landmarks(4)
+    dg.heuristic(5, d.H_LANDMARK).close()
+    dyn = d.DynamicSearch(dg, 0, 5, d.H_ZERO)
+    dyn.update([1], [0], [7], [1])
+    with pytest.raises(d.DdpError):
+        dg.heuristic(5, d.H_LANDMARK)
+    dyn.close()
+    dg.build_landmarks(4)  # rebuilt on the updated graph
+    dg.heuristic(5, d.H_LANDMARK).close()
