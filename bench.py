@@ -3,9 +3,12 @@
 
 Workload (default, `--config c4`): 4,096 seeded source/target pairs on a
 4M-node random digraph (Hamiltonian chain + uniform arcs, average out-degree
-8, int32 weights uniform in [1,100]); heuristic h = reverse-BFS hop count to
-the target x min weight, built per query inside the batch kernel.  One step
-= one batch of all pairs through the persistent batch kernel.
+8, int32 weights uniform in [1,100]); heuristic h = the ALT landmark bound
+from 16 landmarks (the landmark table is built once per graph, outside the
+timed region; `--heuristic capped` restores the per-query reverse BFS built
+inside the batch kernel); slot shape, bucket width and K from the
+autotuner, run on random queries before timing.  One step = one batch of
+all pairs through the persistent batch kernel.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -68,10 +71,15 @@ def args_parse():
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--delta", type=int, default=0)
     p.add_argument("--K", type=int, default=0)
-    p.add_argument("--group", type=int, default=19, help="CTAs per query slot")
+    p.add_argument("--group", type=int, default=19, help="CTAs per query slot (with --no-tune)")
+    p.add_argument("--no-tune", action="store_true",
+                   help="take group/block/delta/K from the flags instead of the autotuner")
+    p.add_argument("--tune-sample", type=int, default=0,
+                   help="random queries the autotuner times (0 = as many as the measured batch)")
     p.add_argument("--landmarks", type=int, default=16, help="landmark count for --heuristic landmark")
-    p.add_argument("--heuristic", default="capped", choices=["capped", "bfs", "zero", "landmark"],
-                   help="capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
+    p.add_argument("--heuristic", default="landmark", choices=["capped", "bfs", "zero", "landmark"],
+                   help="landmark: ALT bound from --landmarks landmarks (table built once per graph); "
+                        "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
                         "get last level + 1); bfs: full reverse BFS; zero: h = 0")
     p.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
     p.add_argument("--plain-sample", type=int, default=16, help="queries timed on plain single-query GA*")
@@ -499,6 +507,18 @@ def main():
         dg.build_landmarks(lm, seed=c["gseed"])
         lm_s = time.perf_counter() - l0
     opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group)
+    tuned = None
+    if not a.no_tune:
+        # autotuner on random queries (not the measured pairs), outside the timed region
+        trng = np.random.default_rng(c["pseed"] + 99991)
+        ns = a.tune_sample or pairs
+        tS = trng.integers(0, g.n, ns).astype(np.int32)
+        tT = trng.integers(0, g.n, ns).astype(np.int32)
+        u0 = time.perf_counter()
+        best, tq, ntr = d.tune_batch(dg, hkind, tS, tT, grid=a.slots, stream=stream.cuda_stream)
+        tuned = {"options": best, "sample_qps": tq, "trials": ntr, "sample": int(ns),
+                 "seconds": time.perf_counter() - u0}
+        opts = dict(best)
     be = d.BatchEngine(dg, hkind, stream=stream.cuda_stream, **opts)
     dS = torch.from_numpy(S).to(dev)
     dT = torch.from_numpy(T).to(dev)
@@ -600,10 +620,10 @@ def main():
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)",
         "config": {"workload": workload_name(c), "n": g.n, "e": g.e, "pairs_per_gpu": pairs,
                    "heuristic": a.heuristic, "landmarks": lm or None,
-                   "landmark_build_s": lm_s,
-                   "slots": be.info()["slots"], "block": be.info()["block"], "K": a.K,
+                   "landmark_build_s": lm_s, "autotuner": tuned,
+                   "slots": be.info()["slots"], "block": be.info()["block"], "K": opts["K"],
                    "group": be.info()["group"],
-                   "delta": a.delta or "auto",
+                   "delta": opts["delta"] or "auto",
                    "l2": "inputs larger than L2 (graph ~%d MB + per-slot state)" % ((g.e * 16 + g.n * 8) >> 20),
                    "parallelism": f"replicas x{world} (queries sharded, no collective)"},
         "latency_ms": {"p50": float(np.percentile(lat_complete, 50)), "p99": float(np.percentile(lat_complete, 99)),

@@ -472,6 +472,19 @@ class BatchEngine:
             pass
 
 
+def tune_batch(graph: DeviceGraph, hkind: int, S, T, **base) -> tuple:
+    """Autotuner (ddp_batch_tune): times the batch engine on the sample
+    (S, T) and returns (options dict for BatchEngine, queries/s, trials)."""
+    S, T = _i32(S), _i32(T)
+    b = _opts(**base)
+    o = Opts()
+    q = C.c_double()
+    n = C.c_int32()
+    check(lib().ddp_batch_tune(graph.handle, int(hkind), len(S), ptr(S), ptr(T), C.byref(b), C.byref(o),
+                               C.byref(q), C.byref(n)))
+    return dict(K=o.K, delta=o.delta, block=o.block, grid=o.grid, group=o.group), q.value, n.value
+
+
 class DynamicSearch:
     """A resident A* search that follows edge-update batches (ddp_dyn):
     replaces DA_star/DA_dyn_cpu.cu.  The graph switches to growable rows."""

@@ -49,6 +49,8 @@ SIGNATURES = {
     "ddp_batch_info": (C.c_int, [vp, i32p, i64p, i32p]),
     "ddp_batch_group": (C.c_int, [vp, i32p]),
     "ddp_batch_launches": (C.c_int, [vp, i32p]),
+    "ddp_batch_tune": (C.c_int, [vp, C.c_int32, C.c_int32, i32p, i32p, C.POINTER(Opts), C.POINTER(Opts),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "ddp_batch_free": (C.c_int, [vp]),
     "ddp_dyn_create": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(Opts), C.POINTER(vp)]),
     "ddp_dyn_update": (C.c_int, [vp, C.c_int32, i32p, i32p, i32p, u32p, i32p]),

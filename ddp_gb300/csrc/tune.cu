@@ -1,0 +1,110 @@
+// Autotuner for the batch engine: picks CTAs per slot (group), threads per
+// CTA (block), the bucket width (delta) and the per-iteration expansion cap
+// (K) by timing the engine on a caller-supplied sample of queries.
+//
+// No reference counterpart (the reference hard-codes K per run and has no
+// batched form).  Search: the (group, block) grid first, since it decides
+// how many queries run at once and dominates throughput; then delta around
+// the automatic choice; then K for multi-CTA slots (one-CTA slots run the
+// asynchronous engine, which has no K).  Every trial must return the same
+// costs as the first one: a mismatch is reported as an error, never tuned
+// around.
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "graph.cuh"
+#include "solve.cuh"
+
+using namespace ddp;
+
+namespace {
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Queries/s of one configuration on the sample (one warm-up pass on a
+// prefix, then one timed pass over the whole sample); costs into `cost`.
+int trial(ddp_graph *g, int32_t hkind, const ddp_opts &o, int32_t n, const int32_t *S, const int32_t *T,
+          std::vector<int32_t> &cost, double *qps) {
+    ddp_batch *b = nullptr;
+    int rc = ddp_batch_create(g, hkind, &o, &b);
+    if (rc) return rc;
+    std::vector<int32_t> plen((size_t)n);
+    cost.assign((size_t)n, 0);
+    const int32_t warm = n < 64 ? n : 64;
+    rc = ddp_batch_solve(b, warm, S, T, cost.data(), plen.data());
+    if (!rc) {
+        const double t0 = now_s();
+        rc = ddp_batch_solve(b, n, S, T, cost.data(), plen.data());
+        const double dt = now_s() - t0;
+        *qps = dt > 0 ? n / dt : 0.0;
+    }
+    ddp_batch_free(b);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *sources, const int32_t *targets,
+                   const ddp_opts *base, ddp_opts *best, double *best_qps, int32_t *trials) {
+    if (!g || !sources || !targets || !best || n < 1) return fail(DDP_ERR_INVALID, "bad tuning arguments");
+    ddp_opts b0 = base ? *base : ddp_opts{};
+    std::vector<int32_t> ref, cost;
+    double top = -1.0;
+    ddp_opts top_o = b0;
+    int count = 0;
+    auto run = [&](const ddp_opts &o) -> int {
+        double q = 0.0;
+        int rc = trial(g, hkind, o, n, sources, targets, ref.empty() ? ref : cost, &q);
+        if (rc) return rc;
+        count++;
+        if (count > 1 && cost != ref)
+            return fail(DDP_ERR_CUDA, "autotuner: two configurations returned different costs");
+        if (q > top) {
+            top = q;
+            top_o = o;
+        }
+        return DDP_OK;
+    };
+    // 1. slot shape
+    const int shapes[][2] = {{1, 512}, {1, 256}, {2, 512}, {4, 512}, {8, 512}, {19, 512}};
+    for (const auto &sh : shapes) {
+        ddp_opts o = b0;
+        o.group = sh[0];
+        o.block = sh[1];
+        o.K = 0;
+        o.delta = 0;
+        int rc = run(o);
+        if (rc) return rc;
+    }
+    // 2. bucket width around the automatic one
+    const uint32_t d0 = auto_delta(g);
+    const ddp_opts shape = top_o;
+    for (uint32_t dv : {d0 / 2, d0 * 2}) {
+        if (dv < 1 || dv == d0) continue;
+        ddp_opts o = shape;
+        o.delta = (int32_t)dv;
+        int rc = run(o);
+        if (rc) return rc;
+    }
+    // 3. expansion cap per iteration (phase-synchronous groups only)
+    if (top_o.group > 1) {
+        const ddp_opts shaped = top_o;
+        for (int32_t k : {1024, 8192}) {
+            ddp_opts o = shaped;
+            o.K = k;
+            int rc = run(o);
+            if (rc) return rc;
+        }
+    }
+    *best = top_o;
+    if (best_qps) *best_qps = top;
+    if (trials) *trials = count;
+    return DDP_OK;
+}
+
+}  // extern "C"

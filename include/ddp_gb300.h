@@ -183,6 +183,16 @@ int ddp_batch_group(const ddp_batch *b, int32_t *group);
 int ddp_batch_launches(const ddp_batch *b, int32_t *launches);
 int ddp_batch_free(ddp_batch *b);
 
+/* Autotuner: times the batch engine on the n sample queries for a grid of
+ * slot shapes (group x block), then bucket widths around the automatic one,
+ * then K (multi-CTA slots), and returns the fastest options in *best (other
+ * fields copied from base, which may be NULL).  Every configuration must
+ * return the same costs, else DDP_ERR_CUDA.  best_qps / trials (nullable)
+ * receive the winner's queries/s and the number of timed configurations.
+ * The reference fixes K by hand per run; no counterpart. */
+int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *sources, const int32_t *targets,
+                   const ddp_opts *base, ddp_opts *best, double *best_qps, int32_t *trials);
+
 /* ---- dynamic A*: DA_star/DA_dyn_cpu.cu (program), LIB d_a_star.cuh:9-86
  *      (GPU_D_A_Star, declared there but not compiling) ------------------- */
 typedef struct ddp_dyn ddp_dyn;
