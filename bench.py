@@ -56,7 +56,7 @@ def workload_name(c):
     return (f"batched multi-query GA*: {c['pairs']} seeded (s,t) pairs, target BFS hops log-uniform in "
             f"[{c['hop_lo']},{c['hop_hi']}] (clipped to what the graph realises), on a {c['n']:,}-node "
             f"random digraph (Hamiltonian chain + uniform arcs), avg out-degree {c['deg']}, int32 w U[{c['wmin']},"
-            f"{c['wmax']}], h = reverse-BFS hops x min w per target")
+            f"{c['wmax']}]; heuristic in config.heuristic")
 
 
 def args_parse():

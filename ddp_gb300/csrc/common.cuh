@@ -70,12 +70,15 @@ struct DevGraph {
     const int32_t *oend;
     const int32_t *roend;
     // Landmark distances (ALT heuristic), null when not built: row v holds
-    // lm_L values d(L_i, v) then lm_L values d(v, L_i), LM_UNREACHED when
-    // there is no path.  lm_L is a multiple of 4 (rows of int4).
-    const int4 *lm;
+    // lm_L values q(L_i, v) then lm_L values q(v, L_i), 16 bits each, with
+    // q = floor(d / lm_scale) and LM_UNREACHED16 when there is no path.
+    // lm_L is a multiple of 4 (rows of 8-byte words).
+    const uint2 *lm;
     int32_t lm_L;
+    int32_t lm_scale;
 };
-constexpr int32_t LM_UNREACHED = 0x7FFFFFFF;
+constexpr int32_t LM_UNREACHED = 0x7FFFFFFF;  // exhaustive-search distances
+constexpr uint32_t LM_UNREACHED16 = 0xFFFFu;  // table entries
 
 __device__ __forceinline__ int row_end(const int32_t *off, const int32_t *oend, int u) {
     return oend ? __ldcg(oend + u) : __ldg(off + u + 1);

@@ -147,35 +147,37 @@ struct HeurManhattan {
 };
 
 // ALT lower bound: max over landmarks L of d(L,t) - d(L,v) and d(v,L) - d(t,L)
-// (triangle inequality, so admissible and consistent).  A landmark that
-// reaches v but not t, or is reached from t but not from v, proves that v
-// cannot reach t.
+// (triangle inequality, so admissible and consistent).  The table holds
+// q = floor(d / s); d(a) - d(b) >= s (q_a - q_b) - (s - 1), which is the
+// exact difference when s = 1.  A landmark that reaches v but not t, or is
+// reached from t but not from v, proves that v cannot reach t.
 struct HeurALT {
-    const int4 *tab;  // DevGraph::lm
-    int32_t L;        // landmarks, a multiple of 4
+    const uint2 *tab;  // DevGraph::lm: rows of L / 2 words
+    int32_t L;         // landmarks, a multiple of 4
+    int32_t s;         // DevGraph::lm_scale
     int32_t t;
-    __device__ __forceinline__ static void term(int32_t a, int32_t b, int32_t &h, bool &cut) {
+    __device__ __forceinline__ void term(uint32_t a, uint32_t b, int32_t &h, bool &cut) const {
         // a - b with a from the row that must be larger
-        if (a != LM_UNREACHED && b != LM_UNREACHED) h = max(h, a - b);
-        else if (a == LM_UNREACHED && b != LM_UNREACHED) cut = true;
+        if (a != LM_UNREACHED16 && b != LM_UNREACHED16) h = max(h, ((int32_t)a - (int32_t)b) * s - (s - 1));
+        else if (a == LM_UNREACHED16 && b != LM_UNREACHED16) cut = true;
+    }
+    __device__ __forceinline__ void terms(uint2 a, uint2 b, int32_t &h, bool &cut) const {
+        term(a.x & 0xFFFFu, b.x & 0xFFFFu, h, cut);
+        term(a.x >> 16, b.x >> 16, h, cut);
+        term(a.y & 0xFFFFu, b.y & 0xFFFFu, h, cut);
+        term(a.y >> 16, b.y >> 16, h, cut);
     }
     __device__ uint32_t operator()(int32_t v) const {
-        const int W = L >> 2;
-        const int4 *rv = tab + (size_t)v * (2 * W);
-        const int4 *rt = tab + (size_t)t * (2 * W);
+        const int W = L >> 2;  // 8-byte words per half row (4 landmarks each)
+        const uint2 *rv = tab + (size_t)v * (2 * W);
+        const uint2 *rt = tab + (size_t)t * (2 * W);
         int32_t h = 0;
         bool cut = false;
         for (int i = 0; i < W; i++) {
-            const int4 fv = __ldg(rv + i), ft = __ldg(rt + i);
-            const int4 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
-            term(ft.x, fv.x, h, cut);
-            term(ft.y, fv.y, h, cut);
-            term(ft.z, fv.z, h, cut);
-            term(ft.w, fv.w, h, cut);
-            term(bv.x, bt.x, h, cut);
-            term(bv.y, bt.y, h, cut);
-            term(bv.z, bt.z, h, cut);
-            term(bv.w, bt.w, h, cut);
+            const uint2 fv = __ldg(rv + i), ft = __ldg(rt + i);
+            const uint2 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
+            terms(ft, fv, h, cut);
+            terms(bv, bt, h, cut);
         }
         return cut ? INF_G : (uint32_t)h;
     }

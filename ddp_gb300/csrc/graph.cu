@@ -71,6 +71,7 @@ DevGraph graph_view(const ddp_graph *g) {
     const bool lm_ok = g->d_lm && g->lm_stamp == g->update_count;
     d.lm = lm_ok ? g->d_lm : nullptr;
     d.lm_L = lm_ok ? g->lm_L : 0;
+    d.lm_scale = lm_ok ? g->lm_scale : 1;
     return d;
 }
 

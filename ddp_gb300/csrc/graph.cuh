@@ -60,8 +60,9 @@ struct ddp_graph {
     int64_t update_count = 0;  // update batches applied (dynamic graphs)
     // landmark distances for the ALT heuristic (DevGraph::lm), built for
     // the graph as it was at update_count == lm_stamp
-    int4 *d_lm = nullptr;
+    uint2 *d_lm = nullptr;
     int32_t lm_L = 0;
+    int32_t lm_scale = 1;
     int64_t lm_stamp = -1;
     std::vector<int32_t> lm_ids;
     // single-query workspace, allocated on first use

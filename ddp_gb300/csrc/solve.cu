@@ -149,11 +149,19 @@ __global__ void k_put_column(int32_t *tab, int32_t width, int32_t c, const int32
     if (v < n) tab[v * width + c] = dist[v];
 }
 
+// 16-bit table entries from exhaustive-search distances: floor(d / scale)
+__global__ void k_pack_landmarks(const int32_t *tab32, uint16_t *tab16, int64_t count, int32_t scale) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t d = tab32[i];
+        tab16[i] = d == LM_UNREACHED ? (uint16_t)LM_UNREACHED16 : (uint16_t)(d / scale);
+    }
+}
+
 // h(v) of the landmark heuristic for target t (INF_G -> -1)
 __global__ void k_alt_values(DevGraph G, int32_t t, int32_t *out) {
     const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= G.n) return;
-    const uint32_t h = HeurALT{G.lm, G.lm_L, t}(v);
+    const uint32_t h = HeurALT{G.lm, G.lm_L, G.lm_scale, t}(v);
     out[v] = h >= INF_G ? -1 : (int32_t)h;
 }
 
@@ -307,7 +315,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
             r = slot_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows, sq, async);
         } else if (HK == 4) {
-            r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, t}, P, wrows, sq, async);
+            r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, G.lm_scale, t}, P, wrows, sq, async);
         } else {
             r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
         }
@@ -841,6 +849,7 @@ int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out
     // seeded random node
     std::vector<int64_t> score((size_t)n, INT64_MAX);
     std::vector<int32_t> fw((size_t)n), bw((size_t)n);
+    int32_t maxd = 0;  // largest finite landmark distance (sets the 16-bit scale)
     auto measure = [&](int32_t src, int col) -> int {
         int rc = sssp_into(g, src, false, dist);
         if (rc) return rc;
@@ -854,6 +863,10 @@ int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out
         DDP_CUDA(cudaStreamSynchronize(g->stream));
         for (int32_t v = 0; v < n; v++) {
             const bool f = fw[(size_t)v] != LM_UNREACHED, b = bw[(size_t)v] != LM_UNREACHED;
+            if (col >= 0) {
+                if (f) maxd = std::max(maxd, fw[(size_t)v]);
+                if (b) maxd = std::max(maxd, bw[(size_t)v]);
+            }
             const int64_t x = (f && b) ? (int64_t)fw[(size_t)v] + bw[(size_t)v]
                               : f       ? fw[(size_t)v]
                               : b       ? bw[(size_t)v]
@@ -894,14 +907,27 @@ int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out
         rc = measure(ids.back(), i);
         if (rc) return done(rc);
     }
-    DDP_CUDA(cudaGetLastError());
-    DDP_CUDA(cudaStreamSynchronize(g->stream));
+    // 16-bit entries: q = floor(d / scale) with every finite q below the
+    // unreachable marker
+    const int32_t scale = std::max(1, (maxd + 65533) / 65534);
+    uint16_t *tab16 = nullptr;
+    e = cudaMalloc(&tab16, sizeof(uint16_t) * (size_t)n * width);
+    if (e != cudaSuccess) return done(cuda_fail(e, "cudaMalloc(landmarks)"));
+    k_pack_landmarks<<<4 * device_sms(), 256, 0, g->stream>>>(tab, tab16, (int64_t)n * width, scale);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) {
+        cudaFree(tab16);
+        return done(cuda_fail(e, "landmark table packing"));
+    }
     cudaFree(g->d_lm);
-    g->d_lm = reinterpret_cast<int4 *>(tab);
+    g->d_lm = reinterpret_cast<uint2 *>(tab16);
+    g->lm_scale = scale;
     g->lm_L = count;
     g->lm_stamp = g->update_count;
     g->lm_ids = ids;
     if (out_ids) std::memcpy(out_ids, ids.data(), sizeof(int32_t) * (size_t)count);
+    cudaFree(tab);  // the 32-bit staging table
     return done(DDP_OK);
 }
 
@@ -947,7 +973,7 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             HeurManhattan Hm{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->wmin};
             HeurEuclid He{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->rho_fp};
             HeurArray Ha{h ? h->d_h : nullptr};
-            HeurALT Hl{G.lm, G.lm_L, target};
+            HeurALT Hl{G.lm, G.lm_L, G.lm_scale, target};
             HeurZero Hz{};
             const void *fn;
             if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) { fn = (const void *)k_solve_cta<HeurHops>; hp = &Hh; }
@@ -979,7 +1005,7 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurArray>, grid, block, args, st);
         } else if (kind == DDP_H_LANDMARK) {
-            HeurALT H{G.lm, G.lm_L, target};
+            HeurALT H{G.lm, G.lm_L, G.lm_scale, target};
             int grid = coop_grid(k_solve_single<HeurALT>, block, o.grid);
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurALT>, grid, block, args, st);

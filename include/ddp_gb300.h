@@ -119,9 +119,11 @@ int ddp_graph_free(ddp_graph *g);
 /* ---- heuristic: GA_star/bfs_hx.cu (program), LIB a_star.h:34
  *      set_huiristics(U*) ------------------------------------------------ */
 /* Landmark table for DDP_H_LANDMARK: `count` (4, 8, ..., 32) landmarks picked
- * farthest-first from a seeded start, with exact distances to and from every
- * node (2 x count exhaustive searches on the device, count x 8 bytes per
- * node).  out_ids (nullable) receives the landmarks.  Updates to the graph
+ * farthest-first from a seeded start, with distances to and from every
+ * node from 2 x count exhaustive searches on the device, stored as 16-bit
+ * entries (count x 4 bytes per node): exact while every distance is below
+ * 65535, else floor(d / s) with the smallest such scale s, the bound then
+ * losing at most s - 1 per landmark term.  out_ids (nullable) receives the landmarks.  Updates to the graph
  * (ddp_dyn_update, ddp_serve_update) make the table stale: landmark
  * heuristics then fail with DDP_ERR_INVALID until it is rebuilt.  No
  * reference counterpart. */

@@ -133,3 +133,28 @@ def test_landmark_table_goes_stale(gpu):
     dyn.close()
     dg.build_landmarks(4)  # rebuilt on the updated graph
     dg.heuristic(5, d.H_LANDMARK).close()
+
+
+def test_landmark_scaled_table_admissible(gpu, oracle):
+    """Weights up to 60,000 push distances past 16 bits: the table stores
+    floor(d / s); h must stay a lower bound of the true distance to t and
+    costs stay exact."""
+    d = gpu
+    g = d.gen_random_chain(3000, 4, 20000, 60000, 74)
+    dg = d.DeviceGraph.from_csr(g)
+    ids = dg.build_landmarks(8, seed=4)
+    lfw, _ = _scipy_dists(g, ids)
+    assert lfw[lfw != UNR].max() > 65534  # the table needs a scale > 1
+    rng = np.random.default_rng(6)
+    for t in rng.integers(0, g.n, 4):
+        h = dg.heuristic(int(t), d.H_LANDMARK, want_values=True).values.astype(np.int64)
+        _, to_t = _scipy_dists(g, np.array([int(t)]))  # d(v, t) via the reverse graph
+        dv = to_t[0]
+        ok = dv != UNR
+        assert (h[ok] <= dv[ok]).all() and (h[ok] >= 0).all()
+        assert h[int(t)] == 0
+    S = rng.integers(0, g.n, 24).astype(np.int32)
+    T = rng.integers(0, g.n, 24).astype(np.int32)
+    want = np.array([_oracle(oracle, g, int(s), int(t)) for s, t in zip(S, T)])
+    cost, _ = d.BatchEngine(dg, d.H_LANDMARK, group=1).solve(S, T)
+    assert np.array_equal(cost, want)
