@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(512, 2)
     const uint32_t scale = G.wmin;
     int32_t *fa = reinterpret_cast<int32_t *>(B.q0);
     int32_t *fb = reinterpret_cast<int32_t *>(B.q1);
-    uint2 *far_buf = (*(volatile int *)&B.ctl->far_sel) ? B.f1 : B.f0;
+    uint4 *far_buf = (*(volatile int *)&B.ctl->far_sel) ? B.f1 : B.f0;  // f re-derived (keep mode)
     const int64_t far_base = *(volatile int *)&B.ctl->far_n;
 
     if (!A.initial) {
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(512, 2)
             const int x = A.inv[i];
             B.state[x] = st_make(bv.x, (int32_t)bv.y);
             const int s = atomicAdd(&dc->far_add, 1);
-            if (far_base + s < B.cap_f) far_buf[far_base + s] = make_uint2((uint32_t)x, bv.x);
+            if (far_base + s < B.cap_f) far_buf[far_base + s] = make_uint4((uint32_t)x, bv.x, 0u, 0u);
             else atomicOr(&B.ctl->status, ST_OVERFLOW);
             atomicAdd(&dc->reseeded, 1);
         }
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(512, 2)
                 const uint64_t got = atomicCAS(B.state + up.z, cur, st_make(ng, up.y));
                 if (got == cur) {
                     const int s = atomicAdd(&dc->far_add, 1);
-                    if (far_base + s < B.cap_f) far_buf[far_base + s] = make_uint2((uint32_t)up.z, ng);
+                    if (far_base + s < B.cap_f) far_buf[far_base + s] = make_uint4((uint32_t)up.z, ng, 0u, 0u);
                     else atomicOr(&B.ctl->status, ST_OVERFLOW);
                     atomicAdd(&dc->relaxed, 1);
                     break;

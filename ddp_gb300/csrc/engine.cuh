@@ -66,7 +66,7 @@ struct SearchCtl {
 struct SlotBufs {
     unsigned long long *state;  // n, (g << 32) | parent; all-ones = unreached
     uint2 *q0, *q1;             // near / next ping-pong, cap_q entries {node, g}
-    uint2 *f0, *f1;             // far ping-pong, cap_f entries
+    uint4 *f0, *f1;             // far ping-pong, cap_f entries {node, g, f, 0}
     int32_t *touched;           // n: nodes whose state must be reset
     uint32_t *hops;             // n: per-target hop heuristic (may be null)
     SearchCtl *ctl;
@@ -263,7 +263,7 @@ struct WarpRows {
     uint32_t g[32];
     int u[32];
     uint2 sn[64];    // staged near/next pushes
-    uint2 sf[64];    // staged far pushes
+    uint4 sf[64];    // staged far pushes
     int st[64];      // staged first touches / BFS frontier pushes
 };
 
@@ -367,7 +367,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     grp.sync();
 
     uint2 *qcur = B.q0, *qnxt = B.q1;
-    uint2 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
+    uint4 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
     int64_t nnear = P.resume ? 0 : 1, head = 0, nnext = 0, nfar = far_resume;
     const uint32_t hs = H(P.s);
     uint32_t T = sat_add(hs, P.delta);
@@ -431,8 +431,8 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                         }
                     }
                 }
-                stage_push(requeue, make_uint2((uint32_t)u, gu), wr.sf, c_f, &ctl->fq[PH], fcur, nfar,
-                           B.cap_f, ctl, PH);
+                stage_push(requeue, make_uint4((uint32_t)u, gu, 0u, 0u), wr.sf, c_f, &ctl->fq[PH],  // keep mode: f re-derived
+                           fcur, nfar, B.cap_f, ctl, PH);
                 int total;
                 int ex = warp_excl_scan(deg, &total);
                 wr.excl[lane] = ex;
@@ -504,7 +504,8 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                         if (to_near || to_far) n_rel++;
                         const uint2 en = make_uint2((uint32_t)v[r], ng[r]);
                         stage_push(to_near, en, wr.sn, c_n, &ctl->nq[PH], qnxt, nnext, B.cap_q, ctl, PH);
-                        stage_push(to_far, en, wr.sf, c_f, &ctl->fq[PH], fcur, nfar, B.cap_f, ctl, PH);
+                        stage_push(to_far, make_uint4(en.x, en.y, sat_add(ng[r], hv[r]), 0u), wr.sf, c_f,
+                                   &ctl->fq[PH], fcur, nfar, B.cap_f, ctl, PH);
                         // at most n first touches: the touched log never overflows
                         stage_push(first, v[r], wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, PH);
                     }
@@ -515,8 +516,13 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             stage_flush(wr.sf, c_f, &ctl->fq[PH], fcur, nfar, B.cap_f, ctl, PH);
             stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, PH);
         } else {
-            // split the far pile at Tsplit (or compact it at T)
+            // split the far pile at Tsplit (or compact it at T).  Entries
+            // carry f from their push: a split reads no node state, stale
+            // entries are dropped when they are popped.  Keep mode (h may
+            // have changed since the push) and compaction (which must drop
+            // stale entries) re-check the state and h.
             const uint32_t thr = compacting ? T : Tsplit;
+            const bool recheck = P.keep || compacting;
             if (grp.rank() == 0) ctl->far_scanned += (unsigned long long)nfar;
             uint2 *dst = compacting ? qnxt : qcur;
             const int64_t dbase = compacting ? nnext : 0;
@@ -526,12 +532,17 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                  base = 32 * claim_chunk(&ctl->ck[PH])) {
                 const int64_t idx = base + lane;
                 bool to_near = false, keep = false;
-                uint2 en = make_uint2(0u, 0u);
+                uint4 en = make_uint4(0u, 0u, 0u, 0u);
                 if (idx < nfar) {
                     en = __ldcg(fcur + idx);
-                    uint64_t sv = __ldcg(B.state + en.x);
-                    if (st_g(sv) == en.y) {
-                        uint64_t f = (uint64_t)en.y + H((int)en.x);
+                    bool live = true;
+                    uint64_t f = en.z;
+                    if (recheck) {
+                        live = st_g(__ldcg(B.state + en.x)) == en.y;
+                        f = (uint64_t)en.y + H((int)en.x);
+                        en.z = f >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)f;
+                    }
+                    if (live) {
                         if (f < ft && f < thr) {
                             to_near = true;
                         } else if (f < ft || (P.keep && f < INF_G)) {
@@ -540,7 +551,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                         }
                     }
                 }
-                stage_push(to_near, en, wr.sn, c_n, &ctl->nq[PH], dst, dbase, B.cap_q, ctl, PH);
+                stage_push(to_near, make_uint2(en.x, en.y), wr.sn, c_n, &ctl->nq[PH], dst, dbase, B.cap_q, ctl, PH);
                 // compaction never grows the pile
                 stage_push(keep, en, wr.sf, c_f, &ctl->fq[PH], falt, 0, B.cap_f, ctl, PH);
             }
@@ -572,7 +583,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             break;
         }
         if (compacting) {
-            uint2 *t2 = fcur;
+            uint4 *t2 = fcur;
             fcur = falt;
             falt = t2;
             nfar = b;
@@ -601,7 +612,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                 splitting = true;  // the split code path runs the compaction
             }
         } else {
-            uint2 *t2 = fcur;
+            uint4 *t2 = fcur;
             fcur = falt;
             falt = t2;
             nfar = b;
@@ -671,7 +682,7 @@ __device__ uint32_t run_bfs_hops(const Grp &grp, const DevGraph &G, const SlotBu
     const bool has_diff = G.doff != nullptr;
     // frontier ping-pong: the two near queues, or (when q0 is the
     // asynchronous ring that must stay clean) q1 and the second far pile
-    int *fa = reinterpret_cast<int *>(spare_q0 ? B.f1 : B.q0);
+    int *fa = spare_q0 ? reinterpret_cast<int *>(B.f1) : reinterpret_cast<int *>(B.q0);
     int *fb = reinterpret_cast<int *>(B.q1);
     const int64_t capf = 2 * (spare_q0 ? min(B.cap_q, B.cap_f) : B.cap_q);  // uint2 slots reused as ints
     const uint32_t max_lvl = tag ? 254u : 0xFFFFFFF0u;

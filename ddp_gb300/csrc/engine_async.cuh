@@ -82,7 +82,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
     const bool far_in_f1 = P.resume && (*(volatile int *)&ctl->far_sel) != 0;
     __syncthreads();
 
-    uint2 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
+    uint4 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
     int64_t nfar = far_resume;
     uint32_t T = sat_add(H(P.s), P.delta);
     uint32_t Tsplit = T;
@@ -170,8 +170,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                         }
                     }
                 }
-                stage_push(requeue, make_uint2((uint32_t)u, gu), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
-                           ctl, 0);
+                stage_push(requeue, make_uint4((uint32_t)u, gu, 0u, 0u), wr.sf, c_f, &sq->far_cnt,  // keep mode: f re-derived
+                           fcur, nfar, B.cap_f, ctl, 0);
                 int total;
                 const int ex = warp_excl_scan(deg, &total);
                 wr.excl[lane] = ex;
@@ -186,7 +186,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                     const int k = kb + lane;
                     bool to_near = false, to_far = false, first = false;
                     int v = 0;
-                    uint32_t ng = 0;
+                    uint32_t ng = 0, fpush = 0;
                     if (k < total) {
                         const int o = row_owner(wr, k);
                         const uint2 a = row_arc(G, wr, o, k, true);
@@ -198,6 +198,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             if (ng < st_g(cur)) {
                                 const uint32_t hv = H(v);
                                 const uint64_t fv = (uint64_t)ng + hv;
+                                fpush = fv >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)fv;
                                 if (P.keep ? hv < INF_G : fv < ft) {
                                     const uint64_t nv = st_make(ng, wr.u[o]);
                                     for (;;) {
@@ -248,8 +249,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                         }
                         __syncwarp();
                     }
-                    stage_push(to_far, make_uint2((uint32_t)v, ng), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
-                               ctl, 0);
+                    stage_push(to_far, make_uint4((uint32_t)v, ng, fpush, 0u), wr.sf, c_f, &sq->far_cnt, fcur, nfar,
+                               B.cap_f, ctl, 0);
                     stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, 0);
                 }
                 __syncwarp();
@@ -292,12 +293,20 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
             for (int64_t base = (int64_t)warp * 32; base < nfar; base += (int64_t)(blockDim.x >> 5) * 32) {
                 const int64_t idx = base + lane;
                 bool to_near = false, keep = false;
-                uint2 en = make_uint2(0u, 0u);
+                uint4 en = make_uint4(0u, 0u, 0u, 0u);
                 if (idx < nfar) {
+                    // entries carry f from their push (no node state read:
+                    // stale entries are dropped when popped); keep mode
+                    // re-checks, since h may have changed since the push
                     en = __ldcg(fcur + idx);
-                    const uint64_t sv = __ldcg(B.state + en.x);
-                    if (st_g(sv) == en.y) {
-                        const uint64_t f = (uint64_t)en.y + H((int)en.x);
+                    bool live = true;
+                    uint64_t f = en.z;
+                    if (P.keep) {
+                        live = st_g(__ldcg(B.state + en.x)) == en.y;
+                        f = (uint64_t)en.y + H((int)en.x);
+                        en.z = f >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)f;
+                    }
+                    if (live) {
                         if (f < ft && f < Tsplit) {
                             to_near = true;
                         } else if (f < ft || (P.keep && f < INF_G)) {
@@ -308,7 +317,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                 }
                 // split output goes to ring positions [0, m): the ring is
                 // clean and nobody reads it until the split is over
-                stage_push(to_near, en, wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
+                stage_push(to_near, make_uint2(en.x, en.y), wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
                 stage_push(keep, en, wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
             }
             stage_flush(wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
@@ -329,7 +338,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                 sq->head = 0;
                 sq->pending = m;
             }
-            uint2 *t2 = fcur;
+            uint4 *t2 = fcur;
             fcur = falt;
             falt = t2;
             nfar = kept;

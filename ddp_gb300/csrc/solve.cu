@@ -26,7 +26,7 @@ size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops) {
     b += sizeof(int32_t) * (size_t)n;             // touched
     if (hops) b += sizeof(uint32_t) * (size_t)n;
     b += 2 * sizeof(uint2) * (size_t)cap_q;
-    b += 2 * sizeof(uint2) * (size_t)cap_f;
+    b += 2 * sizeof(uint4) * (size_t)cap_f;
     b += sizeof(SearchCtl);
     return b;
 }
@@ -43,7 +43,7 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * S));
     if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
     DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * 2 * S));
-    DDP_CUDA(cudaMalloc(&sa.f, sizeof(uint2) * (size_t)cap_f * 2 * S));
+    DDP_CUDA(cudaMalloc(&sa.f, sizeof(uint4) * (size_t)cap_f * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
     DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));

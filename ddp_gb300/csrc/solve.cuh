@@ -16,7 +16,7 @@ struct SlotArrays {
     int32_t *touched = nullptr;           // nslots x n
     uint32_t *hops = nullptr;             // nslots x n (per-target heuristic) or null
     uint2 *q = nullptr;                   // nslots x 2 x cap_q
-    uint2 *f = nullptr;                   // nslots x 2 x cap_f
+    uint4 *f = nullptr;                   // nslots x 2 x cap_f {node, g, f, 0}
     SearchCtl *ctl = nullptr;             // nslots
     uint32_t *epoch = nullptr;            // nslots: per-query tag counter of the hop array
 };
