@@ -168,11 +168,11 @@ def algorithmic_bytes(st, landmarks=0):
     h(head), g(head)), 16 B per successful relaxation (g, parent, queue
     push), and for the heuristic BFS 12 B per reached node + 8 B per scanned
     reverse arc.  With L landmarks h is read only for a relaxation that
-    improves g: 12 B per scanned arc and 16 + 8 L B per relaxation (the
-    node's landmark row), no BFS."""
+    improves g: 12 B per scanned arc and 16 + 4 L B per relaxation (the
+    node's row of 2 L 16-bit distances), no BFS."""
     st = np.asarray(st, np.float64)
     if landmarks:
-        return 12 * st[:, 0] + 12 * st[:, 1] + (16 + 8 * landmarks) * st[:, 2]
+        return 12 * st[:, 0] + 12 * st[:, 1] + (16 + 4 * landmarks) * st[:, 2]
     return 12 * st[:, 0] + 16 * st[:, 1] + 16 * st[:, 2] + 12 * st[:, 4] + 8 * st[:, 5]
 
 
