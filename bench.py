@@ -183,6 +183,17 @@ def make_workload(c, pairs, rank):
     return g, S, T, want
 
 
+def max_over_ranks(x, world, dev):
+    """The job's time is the slowest replica's: MAX over ranks (NCCL on GPU
+    tensors, gloo on CPU ones)."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(a, c, world, rank):
     """The reference's CPU A* (oracle restatement of GA_star/A_star_cpu.cpp)
     on all host cores: each step = one bounded sample of the workload."""
@@ -548,11 +559,7 @@ def main():
         torch.cuda.synchronize(dev)
     barrier()
     elapsed = ev0.elapsed_time(ev1) / 1000.0
-    tmax = elapsed
-    if world > 1:
-        t = torch.tensor([elapsed], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tmax = float(t.item())
+    tmax = max_over_ranks(elapsed, world, dev)
     clocks = ck.summary()
     costs = dcost.cpu().numpy()
     st, t0, t1 = be.stats()
