@@ -47,6 +47,7 @@ CONFIGS = {
                seconds=1.0, update_ms=10, wchanges=500, deletes=100, inserts=100),
     "c5-small": dict(n=500_000, k=6, side=1 << 20, wscale=100000, gseed=5005, rates=[5000, 20000, 50000],
                      seconds=0.5, update_ms=10, wchanges=500, deletes=100, inserts=100),
+    "c2dyn": dict(rows=1024, cols=1024, wall=0.30, gseed=2202, useed=2303, batches=50, moves=200),
     "c4-small": dict(n=400_000, deg=8, wmin=1, wmax=100, pairs=1024, hop_lo=4, hop_hi=400, gseed=4004,
                      pseed=4400),
 }
@@ -310,21 +311,40 @@ def bench_dynamic(a, c):
     B.build()
     import ddp_gb300 as d
     from oracle import oracle as O
-    base = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
-    fl, u, v, w = d.gen_updates(base, c["batches"], c["per_batch"], c["inserts"], c["wmin"], c["wmax"], c["useed"])
+    if "rows" in c:
+        # maze with moving obstacles (maze/create_maze.cpp:137-251): every cell a node
+        R, Cc = c["rows"], c["cols"]
+        wall = d.maze_walls(R, Cc, c["wall"], c["gseed"])
+        base = d.grid_from_walls(R, Cc, wall)
+        prot = np.zeros(R * Cc, np.uint8)
+        prot[0] = prot[-1] = 1
+        counts, fl, u, v, w = d.gen_maze_moves(R, Cc, wall, c["batches"], c["moves"], c["useed"], prot)
+        bounds = np.concatenate([[0], np.cumsum(counts)])
+        s, t = 0, R * Cc - 1
+        workload = (f"dynamic A* on a {R}x{Cc} maze ({int(100 * c['wall'])}% walls, every cell a node), "
+                    f"{c['batches']} batches of {c['moves']} obstacle moves (cells open / close, unit arcs "
+                    f"inserted / deleted both ways), BFS-hops heuristic, s=(0,0), t=(end)")
+    else:
+        base = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
+        fl, u, v, w = d.gen_updates(base, c["batches"], c["per_batch"], c["inserts"], c["wmin"], c["wmax"],
+                                    c["useed"])
+        bounds = np.arange(0, c["batches"] + 1) * c["per_batch"]
+        s, t = int(base.perm[0]), int(base.perm[-1])
+        workload = (f"dynamic A*: {c['n']:,}-node random digraph, avg out-degree {c['deg']}, "
+                    f"w U[{c['wmin']},{c['wmax']}], BFS-hops x min w heuristic, {c['batches']} batches x "
+                    f"{c['per_batch']} updates ({c['inserts']} inserts of new arcs, "
+                    f"{c['per_batch'] - c['inserts']} deletes of existing non-chain arcs)")
     g = base.with_sentinel()
-    s, t = int(base.perm[0]), int(base.perm[-1])
     dg = d.DeviceGraph.from_csr(g)
     t0 = time.perf_counter()
     dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS)
     t_init = time.perf_counter() - t0
-    per = c["per_batch"]
     nb = c["batches"]
     sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}
     off, col, ww = g.off[:-1].copy(), g.col.copy(), g.w.copy()
     dyn_t, scratch_t, cpu_t, exact, costs, inval = [], [], [], True, [], []
     for b in range(nb):
-        sl = slice(b * per, (b + 1) * per)
+        sl = slice(int(bounds[b]), int(bounds[b + 1]))
         t0 = time.perf_counter()
         cost = dyn.update(fl[sl], u[sl], v[sl], w[sl])
         dyn_t.append(time.perf_counter() - t0)
@@ -346,10 +366,8 @@ def bench_dynamic(a, c):
     out = {"metric": "dynamic A* update batch latency (exact)", "value": 1000 * float(np.mean(dyn_t)),
            "unit": "ms/batch", "higher_is_better": False, "n_gpus": 1, "steps": nb, "warmup": 0,
            "dtype": "int32", "data": "synthetic (seeded generators)",
-           "config": {"workload": f"dynamic A*: {c['n']:,}-node random digraph, avg out-degree {c['deg']}, "
-                                  f"w U[{c['wmin']},{c['wmax']}], BFS-hops x min w heuristic, {nb} batches x "
-                                  f"{per} updates ({c['inserts']} inserts of new arcs, {per - c['inserts']} "
-                                  f"deletes of existing non-chain arcs)", "n": g.n, "e": g.e},
+           "config": {"workload": workload, "n": g.n, "e": g.e,
+                      "updates_per_batch_mean": float(np.mean(np.diff(bounds)))},
            "batch_ms": {"p50": 1000 * _pct(dyn_t, 50), "p99": 1000 * _pct(dyn_t, 99),
                         "initial_search_ms": 1000 * t_init},
            "gpu_from_scratch_ms_per_batch": 1000 * float(np.mean(scratch_t)),
@@ -477,7 +495,7 @@ def main():
         if rank == 0:
             bench_single(a, c)
         return
-    if a.config == "c3":
+    if a.config in ("c3", "c2dyn"):
         if rank == 0:
             bench_dynamic(a, c)
         return

@@ -136,6 +136,53 @@ def gen_maze(rows: int, cols: int, wall_p: float, seed: int) -> CSR:
     return g
 
 
+def maze_walls(rows: int, cols: int, wall_p: float, seed: int) -> np.ndarray:
+    """The wall mask of gen_maze(rows, cols, wall_p, seed) (uint8, 1 = wall)."""
+    return (gen_maze(rows, cols, wall_p, seed).extra["cell_node"] < 0).astype(np.uint8)
+
+
+def grid_from_walls(rows: int, cols: int, wall: np.ndarray) -> CSR:
+    """Maze with every cell a node (walls have no arcs), the reference's
+    maze/create_maze.cpp layout; xy = (col, row)."""
+    cells = rows * cols
+    wall = np.ascontiguousarray(wall, np.uint8)
+    off = np.empty(cells + 1, np.int32)
+    col = np.empty(4 * cells, np.int32)
+    w = np.empty(4 * cells, np.uint32)
+    ne = C.c_int64()
+    rc = lib().ddp_gen_grid_from_walls(rows, cols, wall.ctypes.data_as(C.POINTER(C.c_uint8)), ptr(off),
+                                       ptr(col), ptr(w, C.c_uint32), C.byref(ne))
+    if rc:
+        raise DdpError(rc, "ddp_gen_grid_from_walls failed")
+    e = ne.value
+    idx = np.arange(cells, dtype=np.int32)
+    xy = np.stack([idx % cols, idx // cols], axis=1).astype(np.int32)
+    return CSR(cells, off, col[:e].copy(), w[:e].copy(), xy=xy)
+
+
+def gen_maze_moves(rows: int, cols: int, wall: np.ndarray, nbatches: int, moves: int, seed: int,
+                   protect: Optional[np.ndarray] = None):
+    """Obstacle-move batches (ddp_gen_maze_moves); updates `wall` in place.
+    Returns (counts, flag, u, v, w)."""
+    assert wall.dtype == np.uint8 and wall.flags["C_CONTIGUOUS"]
+    cap = max(1, 16 * moves * nbatches)
+    counts = np.empty(max(nbatches, 1), np.int32)
+    flag = np.empty(cap, np.int32)
+    u = np.empty(cap, np.int32)
+    v = np.empty(cap, np.int32)
+    w = np.empty(cap, np.uint32)
+    tot = C.c_int64()
+    pr = None if protect is None else np.ascontiguousarray(protect, np.uint8)
+    u8 = C.POINTER(C.c_uint8)
+    rc = lib().ddp_gen_maze_moves(rows, cols, wall.ctypes.data_as(u8), None if pr is None else pr.ctypes.data_as(u8),
+                                  nbatches, moves, seed, ptr(counts), ptr(flag), ptr(u), ptr(v),
+                                  ptr(w, C.c_uint32), cap, C.byref(tot))
+    if rc:
+        raise DdpError(rc, "ddp_gen_maze_moves failed")
+    k = tot.value
+    return counts[:nbatches].copy(), flag[:k].copy(), u[:k].copy(), v[:k].copy(), w[:k].copy()
+
+
 def gen_updates(g: CSR, nbatches: int, per_batch: int, inserts_per_batch: int, wmin: int, wmax: int,
                 seed: int, protect_next: Optional[np.ndarray] = None):
     """Update batches in the Updates.txt model: per batch, `inserts_per_batch`

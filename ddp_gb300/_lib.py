@@ -75,6 +75,9 @@ SIGNATURES = {
     "ddp_free": (None, [vp]),
     "ddp_gen_random_chain": (C.c_int, [C.c_int32, C.c_int64, C.c_uint32, C.c_uint32, C.c_uint64, i32p, i32p,
                                        u32p, i32p]),
+    "ddp_gen_grid_from_walls": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), i32p, i32p, u32p, C.POINTER(C.c_int64)]),
+    "ddp_gen_maze_moves": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), C.c_int32, C.c_int32, C.c_uint64, i32p, i32p,
+                                     i32p, i32p, u32p, C.c_int64, C.POINTER(C.c_int64)]),
     "ddp_gen_maze": (C.c_int, [C.c_int32, C.c_int32, C.c_uint32, C.c_uint64, i32p, i32p, i64p, i32p, i32p,
                                u32p, i32p]),
     "ddp_gen_updates": (C.c_int, [C.c_int32, C.c_int64, i32p, i32p, u32p, i32p, C.c_int32, C.c_int32, C.c_int32,

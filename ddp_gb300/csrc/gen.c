@@ -665,3 +665,115 @@ int ddp_gen_geometric(int32_t n, int32_t k, int32_t side, uint32_t wscale, uint6
     free(rev);
     return 0;
 }
+
+/* ---------------- maze with every cell a node, and obstacle moves -------- */
+/* CSR over all rows x cols cells (node = cell id); a wall cell has no arcs
+ * and no open neighbour points to it.  Arc order per cell as
+ * maze/create_maze.cpp:93-111: up, down, right, left. */
+int ddp_gen_grid_from_walls(int32_t rows, int32_t cols, const uint8_t *wall, int32_t *off, int32_t *col,
+                            uint32_t *w, int64_t *n_arcs) {
+    if (rows < 1 || cols < 1 || !wall) return -1;
+    int64_t m = 0;
+    for (int32_t i = 0; i < rows; i++)
+        for (int32_t j = 0; j < cols; j++) {
+            const int64_t c = (int64_t)i * cols + j;
+            off[c] = (int32_t)m;
+            if (wall[c]) continue;
+            if (i > 0 && !wall[c - cols]) { col[m] = (int32_t)(c - cols); w[m++] = 1; }
+            if (i < rows - 1 && !wall[c + cols]) { col[m] = (int32_t)(c + cols); w[m++] = 1; }
+            if (j < cols - 1 && !wall[c + 1]) { col[m] = (int32_t)(c + 1); w[m++] = 1; }
+            if (j > 0 && !wall[c - 1]) { col[m] = (int32_t)(c - 1); w[m++] = 1; }
+        }
+    off[(int64_t)rows * cols] = (int32_t)m;
+    *n_arcs = m;
+    return 0;
+}
+
+/* Obstacle moves (the dynamic maze workload of maze/create_maze.cpp:137-251,
+ * restated so that every batch is consistent with the update semantics):
+ * per batch, `moves` wall cells open and `moves` open cells close (the two
+ * sets disjoint, cells in `protect` never close).  An opened cell gets unit
+ * arcs both ways to each neighbour open after the batch; a closed cell loses
+ * its arcs both ways to each neighbour open before the batch.  Each pair is
+ * listed once.  Inserts come first, then deletes; a delete never targets an
+ * arc inserted in the same batch.  wall (rows x cols) is updated in place.
+ * counts[b] receives each batch's line count; the lines go to
+ * flag/u/v/w (capacity cap); returns -3 when cap is too small. */
+int ddp_gen_maze_moves(int32_t rows, int32_t cols, uint8_t *wall, const uint8_t *protect, int32_t nbatches,
+                       int32_t moves, uint64_t seed, int32_t *counts, int32_t *flag, int32_t *uu, int32_t *vv,
+                       uint32_t *ww, int64_t cap, int64_t *total) {
+    if (rows < 1 || cols < 1 || !wall || nbatches < 0 || moves < 0) return -1;
+    const int64_t cells = (int64_t)rows * cols;
+    rng_t r;
+    rng_seed(&r, seed, 7);
+    uint8_t *mark = (uint8_t *)calloc((size_t)cells, 1); /* 1 opening, 2 closing */
+    int64_t *picked = (int64_t *)malloc(sizeof(int64_t) * (size_t)(2 * (moves > 0 ? moves : 1)));
+    if (!mark || !picked) {
+        free(mark);
+        free(picked);
+        return -2;
+    }
+    int64_t k = 0;
+    int rc = 0;
+    const int di[4] = {-1, 1, 0, 0}, dj[4] = {0, 0, 1, -1};
+#define EMIT(F, A, B)                  \
+    do {                               \
+        if (k >= cap) { rc = -3; goto out; } \
+        flag[k] = (F);                 \
+        uu[k] = (int32_t)(A);          \
+        vv[k] = (int32_t)(B);          \
+        ww[k] = (F) ? 1u : 0u;         \
+        k++;                           \
+    } while (0)
+    for (int32_t b = 0; b < nbatches; b++) {
+        const int64_t k0 = k;
+        int32_t nopen = 0, nclose = 0;
+        /* pick cells to open (walls) and to close (open, unprotected) */
+        for (int32_t tries = 0; nopen < moves && tries < 64 * moves + 1024; tries++) {
+            const int64_t c = (int64_t)rng_below(&r, (uint64_t)cells);
+            if (wall[c] && !mark[c]) { mark[c] = 1; picked[nopen++] = c; }
+        }
+        for (int32_t tries = 0; nclose < moves && tries < 64 * moves + 1024; tries++) {
+            const int64_t c = (int64_t)rng_below(&r, (uint64_t)cells);
+            if (!wall[c] && !mark[c] && !(protect && protect[c])) { mark[c] = 2; picked[nopen + nclose++] = c; }
+        }
+        /* inserts: opened cell <-> neighbours open after the batch */
+        for (int32_t p = 0; p < nopen; p++) {
+            const int64_t c = picked[p];
+            const int32_t i = (int32_t)(c / cols), j = (int32_t)(c % cols);
+            for (int q = 0; q < 4; q++) {
+                const int32_t a = i + di[q], bj = j + dj[q];
+                if (a < 0 || a >= rows || bj < 0 || bj >= cols) continue;
+                const int64_t d = (int64_t)a * cols + bj;
+                const int after_open = (!wall[d] && mark[d] != 2) || mark[d] == 1;
+                if (!after_open) continue;
+                if (mark[d] == 1 && d < c) continue; /* the pair is listed by d */
+                EMIT(1, c, d);
+                EMIT(1, d, c);
+            }
+        }
+        /* deletes: closed cell <-> neighbours open before the batch */
+        for (int32_t p = 0; p < nclose; p++) {
+            const int64_t c = picked[nopen + p];
+            const int32_t i = (int32_t)(c / cols), j = (int32_t)(c % cols);
+            for (int q = 0; q < 4; q++) {
+                const int32_t a = i + di[q], bj = j + dj[q];
+                if (a < 0 || a >= rows || bj < 0 || bj >= cols) continue;
+                const int64_t d = (int64_t)a * cols + bj;
+                if (wall[d]) continue; /* no arc before the batch */
+                if (mark[d] == 2 && d < c) continue;
+                EMIT(0, c, d);
+                EMIT(0, d, c);
+            }
+        }
+        for (int32_t p = 0; p < nopen; p++) { wall[picked[p]] = 0; mark[picked[p]] = 0; }
+        for (int32_t p = 0; p < nclose; p++) { wall[picked[nopen + p]] = 1; mark[picked[nopen + p]] = 0; }
+        counts[b] = (int32_t)(k - k0);
+    }
+out:
+#undef EMIT
+    free(mark);
+    free(picked);
+    *total = k;
+    return rc;
+}

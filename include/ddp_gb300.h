@@ -298,6 +298,21 @@ int ddp_gen_updates(int32_t n, int64_t e, const int32_t *off, const int32_t *col
                     const int32_t *protect_next, int32_t nbatches, int32_t per_batch,
                     int32_t inserts_per_batch, uint32_t wmin, uint32_t wmax, uint64_t seed,
                     int32_t *flag, int32_t *uu, int32_t *vv, uint32_t *ww);
+/* Maze with every cell a node (node = row * cols + col; a wall cell has no
+ * arcs), as maze/create_maze.cpp:64-113 builds it; off has rows*cols+1
+ * entries, col/w at most 4 per cell. */
+int ddp_gen_grid_from_walls(int32_t rows, int32_t cols, const uint8_t *wall, int32_t *off, int32_t *col,
+                            uint32_t *w, int64_t *n_arcs);
+/* Obstacle-move update batches (maze/create_maze.cpp:137-251): per batch,
+ * `moves` walls open and `moves` open cells (not in `protect`, nullable)
+ * close; unit arcs inserted both ways between each opened cell and its open
+ * neighbours, arcs deleted both ways around each closed cell; every batch
+ * is consistent with ddp_dyn_update's semantics.  `wall` is updated in
+ * place; counts[b] = lines of batch b; lines in flag/u/v/w (capacity cap,
+ * at most 16 x moves per batch); -3 when cap is too small. */
+int ddp_gen_maze_moves(int32_t rows, int32_t cols, uint8_t *wall, const uint8_t *protect, int32_t nbatches,
+                       int32_t moves, uint64_t seed, int32_t *counts, int32_t *flag, int32_t *u, int32_t *v,
+                       uint32_t *w, int64_t cap, int64_t *total);
 /* Points uniform on [0, side)^2 (xy, 2n int32), each joined both ways to its
  * k nearest neighbours, w = max(1, round(wscale * length / spacing)) with
  * spacing = side / sqrt(n).  off has n+1 entries; col/w hold at most 2kn arcs. */

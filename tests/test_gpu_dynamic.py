@@ -160,3 +160,20 @@ def test_dynamic_zero_heuristic_and_recreate(gpu, oracle):
     hh = dg.heuristic(s, d.H_BFS_HOPS)
     assert dg.solve(t, s, hh).cost == dyn.cost
     dyn.close()
+
+
+def test_dynamic_maze_obstacle_moves(gpu, oracle):
+    """The maze workload of maze/create_maze.cpp:137-251: obstacles move
+    every batch (cells open and close), dynamic costs equal from scratch."""
+    d = gpu
+    rows, cols = 96, 96
+    wall = d.maze_walls(rows, cols, 0.3, 21)
+    g = d.grid_from_walls(rows, cols, wall).with_sentinel()
+    prot = np.zeros(rows * cols, np.uint8)
+    prot[0] = prot[-1] = 1
+    counts, fl, u, v, w = d.gen_maze_moves(rows, cols, wall, 10, 40, 22, prot)
+    batches, pos = [], 0
+    for c in counts:
+        batches.append((fl[pos:pos + c], u[pos:pos + c], v[pos:pos + c], w[pos:pos + c]))
+        pos += c
+    _run(d, oracle, g, batches, 0, rows * cols - 1, check_csr_every=3)

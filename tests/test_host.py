@@ -143,3 +143,31 @@ def test_graph_validation_needs_no_gpu(ddp):
     rc = L.ddp_graph_from_csr(2, 2, ddp.ptr(off), 3, ddp.ptr(col), ddp.ptr(w, ctypes.c_uint32), ctypes.byref(h))
     assert rc == 1  # DDP_ERR_INVALID: offsets not ending at e
     assert b"offsets" in L.ddp_last_error()
+
+
+def test_maze_moves_are_consistent(ddp, oracle):
+    """Obstacle-move batches applied with the reference's batch semantics
+    give exactly the maze of the final wall mask."""
+    d = ddp
+    rows, cols = 40, 50
+    wall = d.maze_walls(rows, cols, 0.3, 5)
+    g0 = d.grid_from_walls(rows, cols, wall)
+    prot = np.zeros(rows * cols, np.uint8)
+    prot[0] = prot[-1] = 1
+    w2 = wall.copy()
+    counts, fl, u, v, w = d.gen_maze_moves(rows, cols, w2, 6, 30, 9, prot)
+    assert (w2 != wall).sum() > 0 and prot[w2.astype(bool)].sum() == 0
+    off, col, ww = g0.off[:-1].copy(), g0.col.copy(), g0.w.copy()
+    pos = 0
+    for c in counts:
+        sl = slice(pos, pos + c)
+        pos += c
+        off, col, ww, _ = oracle.apply_batch(len(off), off, col, ww, fl[sl], u[sl], v[sl], w[sl])
+    g1 = d.grid_from_walls(rows, cols, w2)
+
+    def rows_of(off_n, col, w):
+        o = np.append(off_n, len(col))
+        return [sorted((int(a), int(b)) for a, b in zip(col[o[i]:o[i + 1]], w[o[i]:o[i + 1]]) if a >= 0)
+                for i in range(rows * cols)]
+
+    assert rows_of(off, col, ww) == rows_of(g1.off[:-1], g1.col, g1.w)
