@@ -532,6 +532,28 @@ def tune_batch(graph: DeviceGraph, hkind: int, S, T, **base) -> tuple:
     return dict(K=o.K, delta=o.delta, block=o.block, grid=o.grid, group=o.group), q.value, n.value
 
 
+def k_paths(graph: DeviceGraph, s: int, t: int, k: int, hkind: int = H_BFS_HOPS, restore: bool = True):
+    """Up to k successive paths by last-arc deletion (ddp_kpaths, the
+    reference's k-short method).  Returns [(cost, path)] for the paths found."""
+    costs = np.empty(k, np.int32)
+    offs = np.zeros(k + 1, np.int64)
+    found = C.c_int32()
+    cap = max(1024, 4 * k * 64)
+    while True:
+        buf = np.empty(cap, np.int32)
+        rc = lib().ddp_kpaths(graph.handle, int(s), int(t), int(hkind), int(k), int(bool(restore)), ptr(costs),
+                              ptr(buf), cap, offs.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(found))
+        if rc == 0:
+            break
+        if offs[-1] > cap:  # buffer too small: the graph state was restored only if asked; retry larger
+            if not restore:
+                raise DdpError(rc, "path buffer too small (use restore=True to retry)")
+            cap = int(offs[-1])
+            continue
+        check(rc)
+    return [(int(costs[i]), buf[offs[i]:offs[i + 1]].copy()) for i in range(found.value)]
+
+
 class DynamicSearch:
     """A resident A* search that follows edge-update batches (ddp_dyn):
     replaces DA_star/DA_dyn_cpu.cu.  The graph switches to growable rows."""

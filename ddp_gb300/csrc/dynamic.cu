@@ -807,3 +807,75 @@ int64_t dyn_live_arcs(const ddp_graph *g) {
     return k;
 }
 }  // namespace ddp
+
+extern "C" {
+
+// Successive shortest paths by last-arc deletion, the method of
+// k-short/DA_dyn_cpu.cu:1297-1340: after each path, delete the path's last
+// arc (the first live (u, v) of the graph) and let the dynamic search repair.
+int ddp_kpaths(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, int32_t k, int32_t restore,
+               int32_t *costs, int32_t *path_buf, int64_t path_cap, int64_t *path_offsets, int32_t *found) {
+    if (!g || !costs || !path_offsets || !found || k < 1 || path_cap < 0 || (path_cap > 0 && !path_buf))
+        return fail(DDP_ERR_INVALID, "bad k-paths arguments");
+    ddp_dyn *d = nullptr;
+    int rc = ddp_dyn_create(g, source, target, hkind, nullptr, &d);
+    if (rc) return rc;
+    std::vector<int4> removed;  // {u, v, w}
+    std::vector<int32_t> path;
+    int64_t used = 0;
+    int32_t nfound = 0;
+    path_offsets[0] = 0;
+    for (int32_t i = 0; i < k; i++) {
+        const int32_t cost = d->cost;
+        costs[i] = cost;
+        int32_t len = 0;
+        if (cost != DDP_INF) {
+            rc = ddp_dyn_path(d, nullptr, 0, &len);
+            if (rc) break;
+            path.resize((size_t)len);
+            rc = ddp_dyn_path(d, path.data(), len, &len);
+            if (rc) break;
+            nfound++;
+        }
+        for (int32_t j = 0; j < len && used + j < path_cap; j++) path_buf[used + j] = path[(size_t)j];
+        used += len;
+        path_offsets[i + 1] = used;
+        for (int32_t r = i + 1; r < k; r++) {  // in case the loop stops here
+            costs[r] = DDP_INF;
+            path_offsets[r + 1] = used;
+        }
+        if (cost == DDP_INF || len < 2 || i == k - 1) break;
+        const int32_t u = path[(size_t)len - 2], v = path[(size_t)len - 1];
+        uint32_t w = 0;
+        {
+            std::lock_guard<std::mutex> lk(g->mu);
+            const DynMirror *m = g->dyn;
+            for (int32_t j = m->beg[(size_t)u]; j < m->end[(size_t)u]; j++)
+                if ((int32_t)m->arc[(size_t)j].x == v) {
+                    w = m->arc[(size_t)j].y;
+                    break;
+                }
+        }
+        removed.push_back(make_int4(u, v, (int)w, 0));
+        const int32_t fl = 0;
+        const uint32_t w0 = 0;
+        rc = ddp_dyn_update(d, 1, &fl, &u, &v, &w0, nullptr);
+        if (rc) break;
+    }
+    if (!rc && restore && !removed.empty()) {
+        std::vector<int32_t> fl(removed.size(), 1), uu, vv;
+        std::vector<uint32_t> ww;
+        for (const int4 &x : removed) {
+            uu.push_back(x.x);
+            vv.push_back(x.y);
+            ww.push_back((uint32_t)x.z);
+        }
+        rc = ddp_dyn_update(d, (int32_t)removed.size(), fl.data(), uu.data(), vv.data(), ww.data(), nullptr);
+    }
+    ddp_dyn_free(d);
+    *found = nfound;
+    if (!rc && used > path_cap) return fail(DDP_ERR_INVALID, "path buffer too small (path_offsets[k] holds the size needed)");
+    return rc;
+}
+
+}  // extern "C"

@@ -221,6 +221,18 @@ int ddp_dyn_path(ddp_dyn *d, int32_t *buf, int32_t cap, int32_t *len);
 int ddp_dyn_stats(const ddp_dyn *d, int64_t *stats);
 int ddp_dyn_free(ddp_dyn *d);
 
+/* Up to k successive source -> target paths by last-arc deletion
+ * (k-short/DA_dyn_cpu.cu:1297-1340): path i is the shortest path after the
+ * last arcs of paths 0..i-1 were deleted, found by the dynamic search.
+ * costs[i] (DDP_INF once no path is left); the paths are concatenated in
+ * path_buf, path i at [path_offsets[i], path_offsets[i+1]); *found = paths
+ * found.  The deletions stay in the graph, as in the reference, unless
+ * restore != 0 (the arcs are re-inserted, at the ends of their rows).
+ * DDP_ERR_INVALID when path_cap is too small (path_offsets[k] is then the
+ * size needed; costs are filled). */
+int ddp_kpaths(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, int32_t k, int32_t restore,
+               int32_t *costs, int32_t *path_buf, int64_t path_cap, int64_t *path_offsets, int32_t *found);
+
 /* ---- serving: continuous batching with interleaved updates (no reference
  *      counterpart: the reference answers one (s,t) per process) --------- */
 typedef struct ddp_server ddp_server;

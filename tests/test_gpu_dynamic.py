@@ -177,3 +177,29 @@ def test_dynamic_maze_obstacle_moves(gpu, oracle):
         batches.append((fl[pos:pos + c], u[pos:pos + c], v[pos:pos + c], w[pos:pos + c]))
         pos += c
     _run(d, oracle, g, batches, 0, rows * cols - 1, check_csr_every=3)
+
+
+def test_k_paths_match_successive_oracle(gpu, oracle):
+    """ddp_kpaths (the reference's k-short method: delete the last arc of
+    each path, re-solve) against the oracle doing the same deletions; wide
+    weights make ties unlikely, so paths compare exactly."""
+    d = gpu
+    base = d.gen_random_chain(3000, 4, 1, 1_000_000, 31)
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    dg = d.DeviceGraph.from_csr(g)
+    res = d.k_paths(dg, s, t, 6, d.H_BFS_HOPS, restore=True)
+    assert len(res) >= 2
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    zeros = np.zeros(g.n, np.int32)
+    for cost, path in res:
+        f, c, p, _, _ = oracle.astar(len(off), off, col, w, zeros, s, t)
+        p = list(p)
+        if p and p[0] == t:
+            p = p[::-1]
+        assert f and c == cost and p == list(path)
+        off, col, w, _ = oracle.apply_batch(len(off), off, col, w, [0], [int(path[-2])], [int(path[-1])], [0])
+    # restore=True put the deleted arcs back: the first answer again
+    assert dg.solve(s, t, dg.heuristic(t, d.H_BFS_HOPS)).cost == res[0][0]
+    costs = [c for c, _ in res]
+    assert costs == sorted(costs)
