@@ -254,14 +254,16 @@ def gen_pairs(g: CSR, npairs: int, hop_lo: int, hop_hi: int, seed: int, bfs_cap_
 
 # ---------------------------------------------------------------------------
 # text I/O in the reference's formats
-def read_graph_text(path: str) -> CSR:
+def read_graph_text(path: str, binary: bool = False) -> CSR:
+    """Graph file in the reference's text format (parsed in parallel), or
+    the binary format of write_graph_bin."""
     n = C.c_int32()
     e = C.c_int64()
     off = C.POINTER(C.c_int32)()
     col = C.POINTER(C.c_int32)()
     w = C.POINTER(C.c_uint32)()
-    check(lib().ddp_io_read_graph_text(path.encode(), C.byref(n), C.byref(e), C.byref(off), C.byref(col),
-                                       C.byref(w)))
+    fn = lib().ddp_io_read_graph_bin if binary else lib().ddp_io_read_graph_text
+    check(fn(path.encode(), C.byref(n), C.byref(e), C.byref(off), C.byref(col), C.byref(w)))
     try:
         N, E = n.value, e.value
         g = CSR(N, np.ctypeslib.as_array(off, (N + 1,)).copy(),
@@ -271,6 +273,15 @@ def read_graph_text(path: str) -> CSR:
         for p in (off, col, w):
             lib().ddp_free(C.cast(p, C.c_void_p))
     return g
+
+
+def read_graph_bin(path: str) -> CSR:
+    return read_graph_text(path, binary=True)
+
+
+def write_graph_bin(path: str, g: CSR) -> None:
+    check(lib().ddp_io_write_graph_bin(path.encode(), g.n, g.e, ptr(_i32(g.off)), ptr(_i32(g.col)),
+                                       ptr(_u32(g.w), C.c_uint32)))
 
 
 def write_graph_text(path: str, g: CSR) -> None:

@@ -69,6 +69,8 @@ SIGNATURES = {
     "ddp_bfs_hops_noalloc": (C.c_int, [C.c_int32, vp, vp, C.c_int32, vp, vp]),
     "ddp_io_read_graph_text": (C.c_int, [C.c_char_p, i32p, i64p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(u32p)]),
     "ddp_io_write_graph_text": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, i32p, i32p, u32p]),
+    "ddp_io_write_graph_bin": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, i32p, i32p, u32p]),
+    "ddp_io_read_graph_bin": (C.c_int, [C.c_char_p, i32p, i64p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(u32p)]),
     "ddp_io_read_ints_text": (C.c_int, [C.c_char_p, C.c_int64, i32p, i64p]),
     "ddp_io_write_ints_text": (C.c_int, [C.c_char_p, C.c_int64, i32p]),
     "ddp_io_read_updates_text": (C.c_int, [C.c_char_p, i32p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(i32p),

@@ -8,6 +8,7 @@
  * Files are read whole and parsed with a hand-written integer scanner; the
  * reference's iostream / fscanf parse takes seconds at 10^7 arcs.
  */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -72,6 +73,50 @@ static int scan_i64(scan_t *s, int64_t *out) {
     return 1;
 }
 
+/* ---- parallel parse: the file is cut at whitespace into one chunk per
+ * thread; pass 1 counts each chunk's tokens, pass 2 parses every token
+ * straight into its place (token k of the body is col, offset or weight by
+ * its index alone). */
+typedef struct {
+    const char *p, *end;
+    int64_t first, count; /* body token index of the chunk's first token, tokens */
+    int64_t N, E;
+    int32_t *o, *c;
+    uint32_t *w;
+    int bad;
+} chunk_t;
+
+static int is_space(char ch) { return ch == ' ' || ch == '\n' || ch == '\r' || ch == '\t'; }
+
+static void *count_chunk(void *arg) {
+    chunk_t *k = (chunk_t *)arg;
+    int64_t n = 0;
+    int in = 0;
+    for (const char *p = k->p; p < k->end; p++) {
+        const int sp = is_space(*p);
+        if (!sp && !in) n++;
+        in = !sp;
+    }
+    k->count = n;
+    return NULL;
+}
+
+static void *parse_chunk(void *arg) {
+    chunk_t *k = (chunk_t *)arg;
+    scan_t s = {k->p, k->end};
+    int64_t x;
+    for (int64_t t = k->first; t < k->first + k->count; t++) {
+        if (scan_i64(&s, &x) != 1) {
+            k->bad = 1;
+            return NULL;
+        }
+        if (t < k->E) k->c[t] = (int32_t)x;
+        else if (t < k->E + k->N) k->o[t - k->E] = (int32_t)x;
+        else if (t < 2 * k->E + k->N) k->w[t - k->E - k->N] = (uint32_t)x;
+    }
+    return NULL;
+}
+
 int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **off, int32_t **col,
                            uint32_t **w) {
     char *buf;
@@ -80,7 +125,7 @@ int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **o
     int rc = read_file(path, &buf, &len);
     if (rc) return rc == -2 ? DDP_ERR_OOM : DDP_ERR_IO;
     scan_t s = {buf, buf + len};
-    int64_t N, E, x;
+    int64_t N, E;
     if (scan_i64(&s, &N) != 1 || scan_i64(&s, &E) != 1 || N < 1 || E < 0 || N > INT32_MAX ||
         E > INT32_MAX) {
         free(buf);
@@ -96,18 +141,46 @@ int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **o
         free(ww);
         return DDP_ERR_OOM;
     }
-    int bad = 0;
-    for (int64_t i = 0; i < E && !bad; i++) {
-        if (scan_i64(&s, &x) != 1) bad = 1;
-        else c[i] = (int32_t)x;
+    /* chunks: about 8 MB each, at most 32 threads */
+    const char *body = s.p;
+    const size_t blen = (size_t)(buf + len - body);
+    int T = (int)(blen / (8u << 20)) + 1;
+    if (T > 32) T = 32;
+    chunk_t ch[32];
+    const char *p = body;
+    for (int i = 0; i < T; i++) {
+        const char *q = (i == T - 1) ? buf + len : body + blen / (size_t)T * (size_t)(i + 1);
+        if (q < p) q = p;
+        while (q < buf + len && !is_space(*q)) q++; /* never split a number */
+        ch[i].p = p;
+        ch[i].end = q;
+        ch[i].N = N;
+        ch[i].E = E;
+        ch[i].o = o;
+        ch[i].c = c;
+        ch[i].w = ww;
+        ch[i].bad = 0;
+        p = q;
     }
-    for (int64_t i = 0; i < N && !bad; i++) {
-        if (scan_i64(&s, &x) != 1) bad = 1;
-        else o[i] = (int32_t)x;
+    pthread_t th[32];
+    for (int i = 1; i < T; i++)
+        if (pthread_create(&th[i], NULL, count_chunk, &ch[i])) count_chunk(&ch[i]), th[i] = 0;
+    count_chunk(&ch[0]);
+    for (int i = 1; i < T; i++)
+        if (th[i]) pthread_join(th[i], NULL);
+    int64_t total = 0;
+    for (int i = 0; i < T; i++) {
+        ch[i].first = total;
+        total += ch[i].count;
     }
-    for (int64_t i = 0; i < E && !bad; i++) {
-        if (scan_i64(&s, &x) != 1) bad = 1;
-        else ww[i] = (uint32_t)x;
+    int bad = total < 2 * E + N;
+    if (!bad) {
+        for (int i = 1; i < T; i++)
+            if (pthread_create(&th[i], NULL, parse_chunk, &ch[i])) parse_chunk(&ch[i]), th[i] = 0;
+        parse_chunk(&ch[0]);
+        for (int i = 1; i < T; i++)
+            if (th[i]) pthread_join(th[i], NULL);
+        for (int i = 0; i < T; i++) bad |= ch[i].bad;
     }
     free(buf);
     if (bad) {
@@ -125,19 +198,111 @@ int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **o
     return DDP_OK;
 }
 
+/* buffered decimal writer (fprintf per number takes seconds at 10^7) */
+typedef struct {
+    FILE *f;
+    char b[1 << 16];
+    size_t n;
+    int err;
+} out_t;
+
+static void out_flush(out_t *o) {
+    if (o->n && fwrite(o->b, 1, o->n, o->f) != o->n) o->err = 1;
+    o->n = 0;
+}
+
+static void out_i64(out_t *o, int64_t v, char sep) {
+    if (o->n + 24 > sizeof(o->b)) out_flush(o);
+    char t[24];
+    int k = 0;
+    uint64_t u = v < 0 ? (uint64_t)(-(v + 1)) + 1u : (uint64_t)v;
+    do {
+        t[k++] = (char)('0' + (int)(u % 10u));
+        u /= 10u;
+    } while (u);
+    if (v < 0) o->b[o->n++] = '-';
+    while (k) o->b[o->n++] = t[--k];
+    o->b[o->n++] = sep;
+}
+
 int ddp_io_write_graph_text(const char *path, int32_t n, int64_t e, const int32_t *off,
                             const int32_t *col, const uint32_t *w) {
     if (!path || n < 1 || e < 0 || !off || (e > 0 && (!col || !w))) return DDP_ERR_INVALID;
-    FILE *f = fopen(path, "w");
+    out_t *o = (out_t *)malloc(sizeof(out_t));
+    if (!o) return DDP_ERR_OOM;
+    o->f = fopen(path, "w");
+    o->n = 0;
+    o->err = 0;
+    if (!o->f) {
+        free(o);
+        return DDP_ERR_IO;
+    }
+    out_i64(o, n, ' ');
+    out_i64(o, e, '\n');
+    for (int64_t i = 0; i < e; i++) out_i64(o, col[i], ' ');
+    o->b[o->n++] = '\n';
+    for (int32_t i = 0; i < n; i++) out_i64(o, off[i], ' ');
+    o->b[o->n++] = '\n';
+    for (int64_t i = 0; i < e; i++) out_i64(o, (int64_t)w[i], ' ');
+    o->b[o->n++] = '\n';
+    out_flush(o);
+    const int bad = o->err | (fclose(o->f) != 0);
+    free(o);
+    return bad ? DDP_ERR_IO : DDP_OK;
+}
+
+/* ---- binary graph file: "DDPG" 1 (int32 each), n, e (int64), off[n+1],
+ * col[e] (int32), w[e] (uint32), little-endian ---------------------------- */
+int ddp_io_write_graph_bin(const char *path, int32_t n, int64_t e, const int32_t *off, const int32_t *col,
+                           const uint32_t *w) {
+    if (!path || n < 1 || e < 0 || !off || (e > 0 && (!col || !w))) return DDP_ERR_INVALID;
+    FILE *f = fopen(path, "wb");
     if (!f) return DDP_ERR_IO;
-    fprintf(f, "%d %lld\n", n, (long long)e);
-    for (int64_t i = 0; i < e; i++) fprintf(f, "%d ", col[i]);
-    fprintf(f, "\n");
-    for (int32_t i = 0; i < n; i++) fprintf(f, "%d ", off[i]);
-    fprintf(f, "\n");
-    for (int64_t i = 0; i < e; i++) fprintf(f, "%u ", w[i]);
-    fprintf(f, "\n");
-    return fclose(f) == 0 ? DDP_OK : DDP_ERR_IO;
+    const int32_t hdr[2] = {0x47504444, 1}; /* "DDPG", version */
+    const int64_t ne[2] = {n, e};
+    int ok = fwrite(hdr, sizeof(hdr), 1, f) == 1 && fwrite(ne, sizeof(ne), 1, f) == 1 &&
+             fwrite(off, sizeof(int32_t), (size_t)n + 1, f) == (size_t)n + 1 &&
+             (e == 0 || (fwrite(col, sizeof(int32_t), (size_t)e, f) == (size_t)e &&
+                         fwrite(w, sizeof(uint32_t), (size_t)e, f) == (size_t)e));
+    ok = (fclose(f) == 0) && ok;
+    return ok ? DDP_OK : DDP_ERR_IO;
+}
+
+int ddp_io_read_graph_bin(const char *path, int32_t *n, int64_t *e, int32_t **off, int32_t **col, uint32_t **w) {
+    if (!path || !n || !e || !off || !col || !w) return DDP_ERR_INVALID;
+    FILE *f = fopen(path, "rb");
+    if (!f) return DDP_ERR_IO;
+    int32_t hdr[2];
+    int64_t ne[2];
+    if (fread(hdr, sizeof(hdr), 1, f) != 1 || hdr[0] != 0x47504444 || hdr[1] != 1 ||
+        fread(ne, sizeof(ne), 1, f) != 1 || ne[0] < 1 || ne[0] > INT32_MAX || ne[1] < 0 || ne[1] > INT32_MAX) {
+        fclose(f);
+        return DDP_ERR_IO;
+    }
+    const int64_t N = ne[0], E = ne[1];
+    int32_t *o = (int32_t *)malloc(sizeof(int32_t) * (size_t)(N + 1));
+    int32_t *c = (int32_t *)malloc(sizeof(int32_t) * (size_t)(E > 0 ? E : 1));
+    uint32_t *ww = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(E > 0 ? E : 1));
+    int ok = o && c && ww && fread(o, sizeof(int32_t), (size_t)N + 1, f) == (size_t)N + 1 &&
+             (E == 0 || (fread(c, sizeof(int32_t), (size_t)E, f) == (size_t)E &&
+                         fread(ww, sizeof(uint32_t), (size_t)E, f) == (size_t)E));
+    fclose(f);
+    if (ok) { /* offsets must be a CSR of E arcs */
+        ok = o[0] == 0 && o[N] == E;
+        for (int64_t i = 0; ok && i < N; i++) ok = o[i] <= o[i + 1];
+    }
+    if (!ok) {
+        free(o);
+        free(c);
+        free(ww);
+        return DDP_ERR_IO;
+    }
+    *n = (int32_t)N;
+    *e = E;
+    *off = o;
+    *col = c;
+    *w = ww;
+    return DDP_OK;
 }
 
 int ddp_io_read_ints_text(const char *path, int64_t max, int32_t *out, int64_t *count) {

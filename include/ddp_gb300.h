@@ -288,6 +288,11 @@ int ddp_io_read_graph_text(const char *path, int32_t *n, int64_t *e, int32_t **o
 int ddp_io_write_graph_text(const char *path, int32_t n, int64_t e, const int32_t *off,
                             const int32_t *col, const uint32_t *w);
 /* Hx.txt: n whitespace-separated ints (bfs_hx.cu:158-172). */
+/* Binary graph file ("DDPG", version 1, n and e as int64, off[n+1], col[e],
+ * w[e], little-endian): loads without parsing.  No reference counterpart. */
+int ddp_io_write_graph_bin(const char *path, int32_t n, int64_t e, const int32_t *off, const int32_t *col,
+                           const uint32_t *w);
+int ddp_io_read_graph_bin(const char *path, int32_t *n, int64_t *e, int32_t **off, int32_t **col, uint32_t **w);
 int ddp_io_read_ints_text(const char *path, int64_t max, int32_t *out, int64_t *count);
 int ddp_io_write_ints_text(const char *path, int64_t n, const int32_t *vals);
 /* Updates.txt (DA_dyn_cpu.cu:1295-1326): batches of "count" then count

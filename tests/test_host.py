@@ -171,3 +171,20 @@ def test_maze_moves_are_consistent(ddp, oracle):
                 for i in range(rows * cols)]
 
     assert rows_of(off, col, ww) == rows_of(g1.off[:-1], g1.col, g1.w)
+
+
+def test_parallel_text_and_binary_io(ddp, tmp_path):
+    """A graph large enough for several parse threads round-trips through the
+    text format and the binary format; a truncated binary file is rejected."""
+    d = ddp
+    g = d.gen_random_chain(400_000, 8, 1, 1000, 77)  # ~30 MB of text: 4 chunks
+    pt, pb = str(tmp_path / "g.txt"), str(tmp_path / "g.bin")
+    d.write_graph_text(pt, g)
+    d.write_graph_bin(pb, g)
+    for r in (d.read_graph_text(pt), d.read_graph_bin(pb)):
+        assert r.n == g.n and np.array_equal(r.off, g.off) and np.array_equal(r.col, g.col)
+        assert np.array_equal(r.w, g.w)
+    data = open(pb, "rb").read()
+    open(pb, "wb").write(data[:-4])
+    with pytest.raises(d.DdpError):
+        d.read_graph_bin(pb)
