@@ -182,76 +182,97 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                 wr.u[lane] = u;
                 __syncwarp();
                 n_scan += (lane == 0) ? (unsigned long long)total : 0ull;
-                for (int kb = 0; kb < total; kb += 32) {
-                    const int k = kb + lane;
-                    bool to_near = false, to_far = false, first = false;
-                    int v = 0;
-                    uint32_t ng = 0, fpush = 0;
-                    if (k < total) {
-                        const int o = row_owner(wr, k);
-                        const uint2 a = row_arc(G, wr, o, k, true);
-                        v = (int)a.x;
-                        const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
-                        if (v >= 0 && ng64 < INF_G) {
-                            ng = (uint32_t)ng64;
-                            uint64_t cur = __ldcg(B.state + v);
-                            if (ng < st_g(cur)) {
-                                const uint32_t hv = H(v);
-                                const uint64_t fv = (uint64_t)ng + hv;
-                                fpush = fv >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)fv;
-                                if (P.keep ? hv < INF_G : fv < ft) {
-                                    const uint64_t nv = st_make(ng, wr.u[o]);
-                                    for (;;) {
-                                        const uint64_t got = atomicCAS(B.state + v, cur, nv);
-                                        if (got == cur) {
-                                            first = !P.no_touch_log && st_g(cur) >= INF_G;
-                                            if (fv < T) to_near = true;
-                                            else to_far = true;
-                                            break;
-                                        }
-                                        cur = got;
-                                        if (ng >= st_g(cur)) break;
-                                    }
-                                }
-                            }
+                // AA arcs per lane per step; each stage issues all of its
+                // loads / atomics before consuming any result
+#ifndef DDP_ASYNC_ARCS
+#define DDP_ASYNC_ARCS 2
+#endif
+                constexpr int AA = DDP_ASYNC_ARCS;
+                for (int kb = 0; kb < total; kb += 32 * AA) {
+                    int v[AA], o[AA];
+                    uint32_t ng[AA], hv[AA];
+                    uint64_t cur[AA];
+                    bool live[AA];
+#pragma unroll
+                    for (int r = 0; r < AA; r++) {
+                        const int k = kb + 32 * r + lane;
+                        live[r] = false;
+                        v[r] = 0;
+                        ng[r] = 0;
+                        o[r] = 0;
+                        if (k < total) {
+                            o[r] = row_owner(wr, k);
+                            const uint2 a = row_arc(G, wr, o[r], k, true);
+                            v[r] = (int)a.x;
+                            const uint64_t ng64 = (uint64_t)wr.g[o[r]] + a.y;
+                            live[r] = v[r] >= 0 && ng64 < INF_G;
+                            ng[r] = (uint32_t)ng64;
                         }
                     }
-                    if (to_near || to_far) n_rel++;
-                    // near pushes: counted in `pending` first, then kept as
-                    // this warp's own work, or spilled to the ring when full
-                    const unsigned mn = __ballot_sync(FULL, to_near);
-                    if (mn) {
-                        const int kn = __popc(mn);
-                        const int rank_in = __popc(mn & ((1u << lane) - 1u));
-                        if (lane == 0) atomicAdd(&sq->pending, kn);
-                        __syncwarp();
-                        if (c_loc + kn <= 64) {
-                            if (to_near) wr.sn[c_loc + rank_in] = make_uint2((uint32_t)v, ng);
-                            c_loc += kn;
-                        } else {
-                            int p0 = 0;
-                            if (lane == 0) p0 = ring_reserve(sq, kn, cap);
-                            p0 = __shfl_sync(FULL, p0, 0);
-                            if (p0 >= 0) {
-                                if (to_near) {
-                                    volatile uint2 *slot = reinterpret_cast<volatile uint2 *>(ring + p0 + rank_in);
-                                    // one 8-byte store: readers see the old
-                                    // empty marker or the whole entry
-                                    *reinterpret_cast<volatile unsigned long long *>(slot) =
-                                        ((unsigned long long)ng << 32) | (uint32_t)v;
+#pragma unroll
+                    for (int r = 0; r < AA; r++) cur[r] = live[r] ? __ldcg(B.state + v[r]) : 0ull;
+#pragma unroll
+                    for (int r = 0; r < AA; r++) {
+                        live[r] = live[r] && ng[r] < st_g(cur[r]);
+                        hv[r] = live[r] ? H(v[r]) : 0u;
+                    }
+#pragma unroll
+                    for (int r = 0; r < AA; r++) {
+                        bool to_near = false, to_far = false, first = false;
+                        const uint64_t fv = (uint64_t)ng[r] + hv[r];
+                        const uint32_t fpush = fv >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)fv;
+                        if (live[r] && (P.keep ? hv[r] < INF_G : fv < ft)) {
+                            const uint64_t nv = st_make(ng[r], wr.u[o[r]]);
+                            uint64_t c0 = cur[r];
+                            for (;;) {
+                                const uint64_t got = atomicCAS(B.state + v[r], c0, nv);
+                                if (got == c0) {
+                                    first = !P.no_touch_log && st_g(c0) >= INF_G;
+                                    if (fv < T) to_near = true;
+                                    else to_far = true;
+                                    break;
                                 }
+                                c0 = got;
+                                if (ng[r] >= st_g(c0)) break;
+                            }
+                        }
+                        if (to_near || to_far) n_rel++;
+                        // near pushes: counted in `pending` first, then kept as
+                        // this warp's own work, or spilled to the ring when full
+                        const unsigned mn = __ballot_sync(FULL, to_near);
+                        if (mn) {
+                            const int kn = __popc(mn);
+                            const int rank_in = __popc(mn & ((1u << lane) - 1u));
+                            if (lane == 0) atomicAdd(&sq->pending, kn);
+                            __syncwarp();
+                            if (c_loc + kn <= 64) {
+                                if (to_near) wr.sn[c_loc + rank_in] = make_uint2((uint32_t)v[r], ng[r]);
+                                c_loc += kn;
                             } else {
-                                // ring full: the entries go to far (the next
-                                // split brings them back) and leave the bucket
-                                if (lane == 0) atomicSub(&sq->pending, kn);
-                                to_far = to_far || to_near;
+                                int p0 = 0;
+                                if (lane == 0) p0 = ring_reserve(sq, kn, cap);
+                                p0 = __shfl_sync(FULL, p0, 0);
+                                if (p0 >= 0) {
+                                    if (to_near) {
+                                        volatile uint2 *slot = reinterpret_cast<volatile uint2 *>(ring + p0 + rank_in);
+                                        // one 8-byte store: readers see the old
+                                        // empty marker or the whole entry
+                                        *reinterpret_cast<volatile unsigned long long *>(slot) =
+                                            ((unsigned long long)ng[r] << 32) | (uint32_t)v[r];
+                                    }
+                                } else {
+                                    // ring full: the entries go to far (the next
+                                    // split brings them back) and leave the bucket
+                                    if (lane == 0) atomicSub(&sq->pending, kn);
+                                    to_far = to_far || to_near;
+                                }
                             }
+                            __syncwarp();
                         }
-                        __syncwarp();
+                        stage_push(to_far, make_uint4((uint32_t)v[r], ng[r], fpush, 0u), wr.sf, c_f, &sq->far_cnt,
+                                   fcur, nfar, B.cap_f, ctl, 0);
+                        stage_push(first, v[r], wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, 0);
                     }
-                    stage_push(to_far, make_uint4((uint32_t)v, ng, fpush, 0u), wr.sf, c_f, &sq->far_cnt, fcur, nfar,
-                               B.cap_f, ctl, 0);
-                    stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, (int64_t)G.n, ctl, 0);
                 }
                 __syncwarp();
                 // 3. retire the chunk (its children are already counted)
