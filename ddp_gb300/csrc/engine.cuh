@@ -412,7 +412,8 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     // independent loads issued together (speculatively for
                     // entries that turn out stale)
                     const uint64_t su = __ldcg(B.state + u);
-                    const uint32_t hu = H(u);
+                    // until t is reached (f(t) infinite) the pop test passes for any h
+                    const uint32_t hu = ft != 0xFFFFFFFFu ? H(u) : 0u;
                     const int r0 = row_begin(G.off, G.oend, u), r1 = row_end(G.off, G.oend, u);
                     int d0 = 0, d1 = 0;
                     if (has_diff) {

@@ -158,7 +158,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                     u = (int)en.x;
                     gu = en.y;
                     const uint64_t su = __ldcg(B.state + u);
-                    const uint32_t hu = H(u);
+                    // until t is reached (f(t) infinite) the pop test passes for any h
+                    const uint32_t hu = ft != 0xFFFFFFFFu ? H(u) : 0u;
                     const int r0 = row_begin(G.off, G.oend, u), r1 = row_end(G.off, G.oend, u);
                     if (st_g(su) == gu && u != P.t) {
                         if ((uint64_t)gu + hu < ft) {
