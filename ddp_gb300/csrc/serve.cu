@@ -9,8 +9,10 @@
 // at once, so requests that arrive while others run start as soon as a slot
 // (and its pre-allocated queue and state memory) frees up.  Results come back
 // the same way (cost, graph version, done flag) and are collected by polling.
-// Slots leave after a bounded idle period; submit and poll relaunch the
-// kernel when requests are pending and it is not running.
+// A slot with no work for ~2 ms votes to leave and keeps polling; the slots
+// leave together once all have voted, so a launch never thins out while
+// requests keep coming.  Submit and poll relaunch the kernel when requests
+// are pending and it is not running.
 //
 // Admission by memory: every slot owns a fixed footprint (state n x 8 B,
 // touched-log n x 4 B, four queues); the number of slots is what fits in the

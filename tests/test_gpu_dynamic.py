@@ -44,8 +44,9 @@ def _split(fl, u, v, w, per):
 
 
 def test_dynamic_random_batches(gpu, oracle):
-    """BASELINE config 3 shape at 1/50 scale: inserts of new arcs and
-    deletes of existing non-chain arcs, weights in [1,1000]."""
+    """The 1M-node update workload's shape at 1/50 scale (20k nodes, avg
+    out-degree 10): inserts of new arcs and deletes of existing non-chain
+    arcs, weights in [1,1000]."""
     d = gpu
     base = d.gen_random_chain(20000, 10, 1, 1000, 303)
     fl, u, v, w = d.gen_updates(base, 25, 200, 100, 1, 1000, 304)

@@ -217,8 +217,9 @@ def test_explicit_small_queue_reports_overflow(gpu):
 
 
 def test_config1_full_size(gpu, oracle):
-    """BASELINE config 1 at full size: N=100,000, avg out-degree 8, w in
-    [1,100], one seeded pair, h = reverse-BFS hops x min w, K = 1024."""
+    """The 100k-node single-query workload at full size: N=100,000, avg
+    out-degree 8, w in [1,100], one seeded pair, h = reverse-BFS hops x
+    min w, K = 1024."""
     d = gpu
     g = d.gen_random_chain(100000, 8, 1, 100, 2024)
     dg = d.DeviceGraph.from_csr(g)
