@@ -204,6 +204,27 @@ struct HeurEuclid {  // floor(rho * floor(dist)), rho <= w / length on every arc
     }
 };
 
+// Heuristics computed from registers and one small load (coordinates): the
+// one-CTA engine evaluates them speculatively, beside the relaxation's
+// atomic, instead of after it.  Table heuristics (hops, landmarks, arrays)
+// are read only for relaxations that improve g.
+template <class H>
+struct heur_cheap {
+    static constexpr bool value = false;
+};
+template <>
+struct heur_cheap<HeurZero> {
+    static constexpr bool value = true;
+};
+template <>
+struct heur_cheap<HeurManhattan> {
+    static constexpr bool value = true;
+};
+template <>
+struct heur_cheap<HeurEuclid> {
+    static constexpr bool value = true;
+};
+
 // ---- warp helpers ----------------------------------------------------------
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
@@ -263,6 +284,7 @@ struct WarpRows {
     uint32_t g[32];
     int u[32];
     uint2 sn[64];    // staged near/next pushes
+    int2 snr[64];    // one-CTA engine: row bounds of the staged own children
     uint4 sf[64];    // staged far pushes
     int st[64];      // staged first touches / BFS frontier pushes
 };

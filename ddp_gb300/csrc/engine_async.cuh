@@ -50,7 +50,8 @@ __device__ __forceinline__ int ring_reserve(CtaQ *sq, int k, int cap) {
 
 template <class Heur>
 __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, const Heur &H, const SearchParams &P,
-                                       WarpRows *wrows, CtaQ *sq) {
+                                       WarpRows *wrows, CtaQ *sq, bool latency) {
+    constexpr bool cheap = heur_cheap<Heur>::value;
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
@@ -103,9 +104,13 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                 // 1. take work: own children first, else claim from the ring
                 int n = 0;
                 uint2 en = make_uint2(RING_EMPTY, 0u);
+                int2 pre = make_int2(-1, -1);  // row bounds fetched when the child was pushed
                 if (c_loc > 0) {
                     n = min(32, c_loc);
-                    if (lane < n) en = wr.sn[c_loc - n + lane];
+                    if (lane < n) {
+                        en = wr.sn[c_loc - n + lane];
+                        if (cheap) pre = wr.snr[c_loc - n + lane];
+                    }
                     c_loc -= n;
                     __syncwarp();
                 } else {
@@ -160,7 +165,9 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                     const uint64_t su = __ldcg(B.state + u);
                     // until t is reached (f(t) infinite) the pop test passes for any h
                     const uint32_t hu = ft != 0xFFFFFFFFu ? H(u) : 0u;
-                    const int r0 = row_begin(G.off, G.oend, u), r1 = row_end(G.off, G.oend, u);
+                    const bool have = cheap && pre.x >= 0;
+                    const int r0 = have ? pre.x : row_begin(G.off, G.oend, u);
+                    const int r1 = have ? pre.y : row_end(G.off, G.oend, u);
                     if (st_g(su) == gu && u != P.t) {
                         if ((uint64_t)gu + hu < ft) {
                             rb = r0;
@@ -210,19 +217,52 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             ng[r] = (uint32_t)ng64;
                         }
                     }
+                    int2 rows[AA];
+                    if (!P.keep && latency) {
+                        // one atomic per arc: atomicMin on (g << 32 | parent)
+                        // installs a smaller g (or, at equal g, a smaller
+                        // parent id: an equal-cost alternative); cheap
+                        // heuristics and the child's row bounds load beside it
 #pragma unroll
-                    for (int r = 0; r < AA; r++) cur[r] = live[r] ? __ldcg(B.state + v[r]) : 0ull;
+                        for (int r = 0; r < AA; r++) {
+                            rows[r] = make_int2(-1, -1);
+                            if (cheap) {
+                                hv[r] = live[r] ? H(v[r]) : 0u;
+                                if (live[r]) rows[r] = make_int2(row_begin(G.off, G.oend, v[r]), row_end(G.off, G.oend, v[r]));
+                            }
+                            cur[r] = live[r] ? atomicMin(B.state + v[r], st_make(ng[r], wr.u[o[r]])) : 0ull;
+                        }
 #pragma unroll
-                    for (int r = 0; r < AA; r++) {
-                        live[r] = live[r] && ng[r] < st_g(cur[r]);
-                        hv[r] = live[r] ? H(v[r]) : 0u;
+                        for (int r = 0; r < AA; r++) {
+                            live[r] = live[r] && ng[r] < st_g(cur[r]);
+                            if (!cheap) hv[r] = live[r] ? H(v[r]) : 0u;
+                        }
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < AA; r++) cur[r] = live[r] ? __ldcg(B.state + v[r]) : 0ull;
+#pragma unroll
+                        for (int r = 0; r < AA; r++) {
+                            live[r] = live[r] && ng[r] < st_g(cur[r]);
+                            hv[r] = live[r] ? H(v[r]) : 0u;
+                            rows[r] = make_int2(-1, -1);
+                        }
                     }
 #pragma unroll
                     for (int r = 0; r < AA; r++) {
                         bool to_near = false, to_far = false, first = false;
                         const uint64_t fv = (uint64_t)ng[r] + hv[r];
                         const uint32_t fpush = fv >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)fv;
-                        if (live[r] && (P.keep ? hv[r] < INF_G : fv < ft)) {
+                        if (!P.keep && latency) {
+                            // the atomic already installed g: log a first touch even
+                            // when f >= f(t) prunes the push
+                            if (live[r]) {
+                                first = !P.no_touch_log && st_g(cur[r]) >= INF_G;
+                                if (fv < ft) {
+                                    if (fv < T) to_near = true;
+                                    else to_far = true;
+                                }
+                            }
+                        } else if (live[r] && (P.keep ? hv[r] < INF_G : fv < ft)) {
                             const uint64_t nv = st_make(ng[r], wr.u[o[r]]);
                             uint64_t c0 = cur[r];
                             for (;;) {
@@ -247,7 +287,10 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             if (lane == 0) atomicAdd(&sq->pending, kn);
                             __syncwarp();
                             if (c_loc + kn <= 64) {
-                                if (to_near) wr.sn[c_loc + rank_in] = make_uint2((uint32_t)v[r], ng[r]);
+                                if (to_near) {
+                                    wr.sn[c_loc + rank_in] = make_uint2((uint32_t)v[r], ng[r]);
+                                    if (cheap) wr.snr[c_loc + rank_in] = rows[r];
+                                }
                                 c_loc += kn;
                             } else {
                                 int p0 = 0;
