@@ -35,7 +35,7 @@ struct CtaQ {
     int alt_cnt;         // split: far entries kept
     unsigned int minf;   // split: min f kept
     int status;
-    int pad;
+    unsigned int tg;     // g(t) as this CTA installed it (the target's label, kept in shared memory)
 };
 
 // Reserves k ring slots (lane 0 only); returns the first position or -1 when
@@ -78,6 +78,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
             sq->tail = 1;
             sq->pending = 1;
         }
+        sq->tg = P.t >= 0 ? (unsigned int)st_g(__ldcg(B.state + P.t)) : 0xFFFFFFFFu;
     }
     const int64_t far_resume = P.resume ? (int64_t)(*(volatile int *)&ctl->far_n) : 0;
     const bool far_in_f1 = P.resume && (*(volatile int *)&ctl->far_sel) != 0;
@@ -85,6 +86,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
 
     uint4 *fcur = far_in_f1 ? B.f1 : B.f0, *falt = far_in_f1 ? B.f0 : B.f1;
     int64_t nfar = far_resume;
+    const uint32_t ht = P.t >= 0 ? H(P.t) : 0u;
     uint32_t T = sat_add(H(P.s), P.delta);
     uint32_t Tsplit = T;
     bool do_expand = !P.resume;
@@ -98,8 +100,8 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
             // ---- drain the bucket asynchronously -----------------------
             int c_f = 0, c_t = 0, c_loc = 0;  // staged far pushes, touches, own children
             for (;;) {
-                const uint64_t st_t = P.t >= 0 ? __ldcg(B.state + P.t) : ~0ull;
-                const uint64_t ft64 = (uint64_t)st_g(st_t) + (P.t >= 0 ? H(P.t) : 0u);
+                // f(t) from the shared-memory copy of g(t): only this CTA relaxes t
+                const uint64_t ft64 = (uint64_t)(*(volatile unsigned int *)&sq->tg) + ht;
                 const uint32_t ft = ft64 >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)ft64;
                 // 1. take work: own children first, else claim from the ring
                 int n = 0;
@@ -162,10 +164,15 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                 if (lane < n && en.x != RING_EMPTY) {
                     u = (int)en.x;
                     gu = en.y;
-                    const uint64_t su = __ldcg(B.state + u);
+                    const bool have = cheap && pre.x >= 0;
+                    // a child this warp just installed and chases at once is
+                    // expanded without re-reading its state (latency mode): if
+                    // another warp improved it meanwhile, the expansion with
+                    // the older g only relaxes worse labels, which the newer
+                    // entry corrects
+                    const uint64_t su = (have && latency) ? st_make(gu, 0) : __ldcg(B.state + u);
                     // until t is reached (f(t) infinite) the pop test passes for any h
                     const uint32_t hu = ft != 0xFFFFFFFFu ? H(u) : 0u;
-                    const bool have = cheap && pre.x >= 0;
                     const int r0 = have ? pre.x : row_begin(G.off, G.oend, u);
                     const int r1 = have ? pre.y : row_end(G.off, G.oend, u);
                     if (st_g(su) == gu && u != P.t) {
@@ -257,6 +264,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             // when f >= f(t) prunes the push
                             if (live[r]) {
                                 first = !P.no_touch_log && st_g(cur[r]) >= INF_G;
+                                if (v[r] == P.t) atomicMin(&sq->tg, ng[r]);
                                 if (fv < ft) {
                                     if (fv < T) to_near = true;
                                     else to_far = true;
@@ -269,6 +277,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                                 const uint64_t got = atomicCAS(B.state + v[r], c0, nv);
                                 if (got == c0) {
                                     first = !P.no_touch_log && st_g(c0) >= INF_G;
+                                    if (v[r] == P.t) atomicMin(&sq->tg, ng[r]);
                                     if (fv < T) to_near = true;
                                     else to_far = true;
                                     break;
