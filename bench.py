@@ -391,7 +391,7 @@ def bench_serving(a, c):
     g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
     dg = d.DeviceGraph.from_csr(g)
     dg.set_euclid(d.euclid_rho_fp(g))
-    srv = d.Server(dg, d.H_EUCLID, max_requests=1 << 22, grid=a.slots)
+    srv = d.Server(dg, d.H_EUCLID, max_requests=1 << 22, grid=a.slots, block=a.block)
     rng = np.random.default_rng(c["gseed"] + 1)
     src = np.repeat(np.arange(g.n, dtype=np.int32), np.diff(g.off))
     deleted = []

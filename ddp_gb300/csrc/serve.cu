@@ -473,7 +473,7 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
     graph_ref(g);
     s->hkind = hkind;
     if (opts) s->o = *opts;
-    s->block = s->o.block > 0 ? std::min(s->o.block, 512) : 256;
+    s->block = s->o.block > 0 ? std::min(s->o.block, 512) : 512;  // wider slots: lower latency, more per-query parallelism
     s->cap = max_requests;
     auto bail = [&](int rc) {
         ddp_serve_free(s);
