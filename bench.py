@@ -337,7 +337,7 @@ def bench_dynamic(a, c):
     g = base.with_sentinel()
     dg = d.DeviceGraph.from_csr(g)
     t0 = time.perf_counter()
-    dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS)
+    dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS, grid=a.slots)
     t_init = time.perf_counter() - t0
     nb = c["batches"]
     sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}

@@ -449,8 +449,7 @@ int dyn_upload(ddp_graph *g) {
         DDP_CUDA(cudaMemcpyAsync(d->d_slot, sl.data(), sizeof(long long) * k, cudaMemcpyHostToDevice, g->stream));
         DDP_CUDA(cudaMemcpyAsync(d->d_val, val.data(), sizeof(uint2) * k, cudaMemcpyHostToDevice, g->stream));
         k_scatter_arcs<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(dst, d->d_slot, d->d_val, (int)k);
-        DDP_CUDA(cudaGetLastError());
-        DDP_CUDA(cudaStreamSynchronize(g->stream));
+        DDP_CUDA(cudaGetLastError());  // stream-ordered; one synchronisation at the end
         dirty.clear();
         return DDP_OK;
     };
@@ -480,7 +479,6 @@ int dyn_upload(ddp_graph *g) {
         DDP_CUDA(cudaMemcpyAsync(d->d_rows, r.data(), sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
         k_scatter_rows<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(db, de, d->d_rows, (int)k);
         DDP_CUDA(cudaGetLastError());
-        DDP_CUDA(cudaStreamSynchronize(g->stream));
         drow.clear();
         return DDP_OK;
     };
@@ -488,6 +486,8 @@ int dyn_upload(ddp_graph *g) {
     if (!rc) rc = scatter(m->dirty_rarc, m->rarc, g->d_rarc);
     if (!rc) rc = rows(m->dirty_row, m->beg, m->end, g->d_off, g->d_oend);
     if (!rc) rc = rows(m->dirty_rrow, m->rbeg, m->rend, g->d_roff, g->d_roend);
+    // the device graph is current when this returns (other streams read it)
+    if (!rc) DDP_CUDA(cudaStreamSynchronize(g->stream));
     return rc;
 }
 
@@ -694,8 +694,12 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     cudaGetDevice(&dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dyn, 512, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    d->grid = std::max(1, per_sm) * std::max(1, sms);
-    if (d->o.grid > 0 && d->o.grid < d->grid) d->grid = d->o.grid;
+    // half the SMs by default: a batch repairs little, and fewer CTAs make
+    // the grid barriers between repair steps cheaper (measured best on 1M
+    // nodes with 1000-update batches)
+    const int coresident = std::max(1, per_sm) * std::max(1, sms);
+    d->grid = std::min(coresident, std::max(1, sms / 2));
+    if (d->o.grid > 0) d->grid = std::min(coresident, d->o.grid);
     if (hkind == DDP_H_BFS_HOPS) {
         // exact reverse BFS from the target into the dynamic hop array
         ddp_heuristic *h = nullptr;
@@ -729,7 +733,7 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
         DDP_CUDA(cudaMalloc(&d->d_upd, sizeof(int4) * std::max(k, 1)));
         d->upd_cap = k;
     }
-    if (k) DDP_CUDA(cudaMemcpy(d->d_upd, ups.data(), sizeof(int4) * k, cudaMemcpyHostToDevice));
+    if (k) DDP_CUDA(cudaMemcpyAsync(d->d_upd, ups.data(), sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
     rc = dyn_launch(d, 0, k);
     if (rc) return rc;
     if (out_cost) *out_cost = d->cost;
