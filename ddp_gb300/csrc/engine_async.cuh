@@ -207,11 +207,12 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                     int v[AA], o[AA];
                     uint32_t ng[AA], hv[AA];
                     uint64_t cur[AA];
-                    bool live[AA];
+                    bool live[AA], wpos[AA];
 #pragma unroll
                     for (int r = 0; r < AA; r++) {
                         const int k = kb + 32 * r + lane;
                         live[r] = false;
+                        wpos[r] = true;
                         v[r] = 0;
                         ng[r] = 0;
                         o[r] = 0;
@@ -219,17 +220,24 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             o[r] = row_owner(wr, k);
                             const uint2 a = row_arc(G, wr, o[r], k, true);
                             v[r] = (int)a.x;
+                            wpos[r] = a.y != 0;
                             const uint64_t ng64 = (uint64_t)wr.g[o[r]] + a.y;
                             live[r] = v[r] >= 0 && ng64 < INF_G;
                             ng[r] = (uint32_t)ng64;
                         }
                     }
                     int2 rows[AA];
+                    bool fresh[AA];  // latency mode: the atomic found v unreached
                     if (!P.keep && latency) {
-                        // one atomic per arc: atomicMin on (g << 32 | parent)
-                        // installs a smaller g (or, at equal g, a smaller
-                        // parent id: an equal-cost alternative); cheap
-                        // heuristics and the child's row bounds load beside it
+                        // one atomic per arc: over a positive-weight arc,
+                        // atomicMin on (g << 32 | parent) installs a smaller g
+                        // (or, at equal g, a smaller parent id: an equal-cost
+                        // alternative; parent chains still strictly decrease
+                        // in g, so no cycle).  A zero-weight arc must not
+                        // replace a parent on a tie (that could close a parent
+                        // cycle): it tries a CAS from "unreached", then a
+                        // strict-improvement CAS loop.  Cheap heuristics and
+                        // the child's row bounds load beside the atomic.
 #pragma unroll
                         for (int r = 0; r < AA; r++) {
                             rows[r] = make_int2(-1, -1);
@@ -237,11 +245,29 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                                 hv[r] = live[r] ? H(v[r]) : 0u;
                                 if (live[r]) rows[r] = make_int2(row_begin(G.off, G.oend, v[r]), row_end(G.off, G.oend, v[r]));
                             }
-                            cur[r] = live[r] ? atomicMin(B.state + v[r], st_make(ng[r], wr.u[o[r]])) : 0ull;
+                            const uint64_t nv = st_make(ng[r], wr.u[o[r]]);
+                            cur[r] = !live[r] ? 0ull
+                                     : wpos[r] ? atomicMin(B.state + v[r], nv)
+                                               : atomicCAS(B.state + v[r], ~0ull, nv);
                         }
 #pragma unroll
                         for (int r = 0; r < AA; r++) {
-                            live[r] = live[r] && ng[r] < st_g(cur[r]);
+                            fresh[r] = live[r] && cur[r] == ~0ull;
+                            bool inst = fresh[r] || (live[r] && wpos[r] && ng[r] < st_g(cur[r]));
+                            if (live[r] && !wpos[r] && !inst && ng[r] < st_g(cur[r])) {
+                                const uint64_t nv = st_make(ng[r], wr.u[o[r]]);
+                                uint64_t c0 = cur[r];
+                                for (;;) {
+                                    const uint64_t got = atomicCAS(B.state + v[r], c0, nv);
+                                    if (got == c0) {
+                                        inst = true;
+                                        break;
+                                    }
+                                    c0 = got;
+                                    if (ng[r] >= st_g(c0)) break;
+                                }
+                            }
+                            live[r] = inst;
                             if (!cheap) hv[r] = live[r] ? H(v[r]) : 0u;
                         }
                     } else {
@@ -252,6 +278,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             live[r] = live[r] && ng[r] < st_g(cur[r]);
                             hv[r] = live[r] ? H(v[r]) : 0u;
                             rows[r] = make_int2(-1, -1);
+                            fresh[r] = false;
                         }
                     }
 #pragma unroll
@@ -263,7 +290,7 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                             // the atomic already installed g: log a first touch even
                             // when f >= f(t) prunes the push
                             if (live[r]) {
-                                first = !P.no_touch_log && st_g(cur[r]) >= INF_G;
+                                first = !P.no_touch_log && fresh[r];
                                 if (v[r] == P.t) atomicMin(&sq->tg, ng[r]);
                                 if (fv < ft) {
                                     if (fv < T) to_near = true;

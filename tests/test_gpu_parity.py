@@ -87,12 +87,13 @@ def test_single_query_random(gpu, oracle):
             h.close()
 
 
-def test_zero_weights_and_edge_cases(gpu, oracle):
+@pytest.mark.parametrize("flags", [0, 2])  # 2 = OPT_ONE_CTA (latency mode of the one-CTA engine)
+def test_zero_weights_and_edge_cases(gpu, oracle, flags):
     d = gpu
     g = d.gen_random_chain(4000, 5, 0, 3, 8).with_sentinel()   # many zero-weight arcs
     dg = d.DeviceGraph.from_csr(g)
     for s, t in [(1, 2), (5, 3999), (7, 7), (0, g.n - 1)]:
-        r = dg.solve(s, t)
+        r = dg.solve(s, t, flags=flags)
         assert r.cost == _oracle_cost(oracle, g, None, s, t)
         if s == t:
             assert r.path.tolist() == [s]
@@ -105,6 +106,27 @@ def test_zero_weights_and_edge_cases(gpu, oracle):
         dg.solve(-1, 3)
     with pytest.raises(d.DdpError):
         dg.solve(0, g.n)
+
+
+def test_zero_weight_batches(gpu, oracle):
+    """Zero-weight arcs through the batch slots (one-CTA engine, both
+    relaxation modes: zero h runs the latency mode, BFS hops the throughput
+    mode): exact costs and valid paths (no parent cycles on equal g)."""
+    d = gpu
+    g = d.gen_random_chain(6000, 6, 0, 2, 18).with_sentinel()
+    dg = d.DeviceGraph.from_csr(g)
+    rng = np.random.default_rng(4)
+    S = rng.integers(0, g.n - 1, 64).astype(np.int32)
+    T = rng.integers(0, g.n - 1, 64).astype(np.int32)
+    want = np.array([_oracle_cost(oracle, g, None, int(s), int(t)) for s, t in zip(S, T)])
+    for hk in (d.H_ZERO, d.H_BFS_HOPS):
+        be = d.BatchEngine(dg, hk, group=1)
+        cost, _ = be.solve(S, T)
+        assert np.array_equal(cost, want), hk
+        for i in range(64):
+            if cost[i] != d.INF:
+                ok, why = oracle.check_path(g.off, g.col, g.w, be.path(i), int(S[i]), int(T[i]), int(cost[i]))
+                assert ok, (hk, i, why)
 
 
 def test_dead_arcs_are_skipped(gpu, oracle):
