@@ -74,9 +74,11 @@ namespace {
 
 // Lays rows out with slack: capacity = used + max(2, used / 4); reserves
 // room for relocations at the end.
+// extra: arcs still to be appended right after the layout (the reserve
+// holds them even if every one moves its row)
 void mirror_layout(const std::vector<int32_t> &used_b, const std::vector<int32_t> &used_e,
                    const std::vector<uint2> &src, std::vector<int32_t> &beg, std::vector<int32_t> &end,
-                   std::vector<int32_t> &cap, std::vector<uint2> &dst, int64_t &tail) {
+                   std::vector<int32_t> &cap, std::vector<uint2> &dst, int64_t &tail, int64_t extra = 0) {
     const size_t n = used_b.size();
     std::vector<int32_t> nb(n), ne(n), nc(n);
     int64_t total = 0;
@@ -87,7 +89,7 @@ void mirror_layout(const std::vector<int32_t> &used_b, const std::vector<int32_t
         nc[u] = live + std::max(2, live / 4);
         total += nc[u];
     }
-    const int64_t reserve = std::max<int64_t>(1 << 16, total / 4);
+    const int64_t reserve = std::max<int64_t>({(int64_t)1 << 16, total / 4, 4 * extra + 1024});
     std::vector<uint2> out((size_t)(total + reserve), make_uint2(0xFFFFFFFFu, 0u));
     int64_t k = 0;
     for (size_t u = 0; u < n; u++) {
@@ -103,6 +105,14 @@ void mirror_layout(const std::vector<int32_t> &used_b, const std::vector<int32_t
     cap.swap(nc);
     dst.swap(out);
     tail = k;
+}
+
+// Whether mirror_append(u) would succeed (room in the row or at the end).
+bool mirror_can_append(const std::vector<int32_t> &beg, const std::vector<int32_t> &end,
+                       const std::vector<int32_t> &cap, const std::vector<uint2> &arc, int64_t tail, int32_t u) {
+    if (end[(size_t)u] - beg[(size_t)u] < cap[(size_t)u]) return true;
+    const int32_t ncap = std::max(4, 2 * cap[(size_t)u]);
+    return tail + ncap <= (int64_t)arc.size() && tail + ncap <= INT32_MAX;
 }
 
 // Appends an arc to row u; moves the row to the end when it is full.
@@ -599,51 +609,38 @@ int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32
         m->dirty_arc.push_back(jf);
         if (jr >= 0) m->dirty_rarc.push_back(jr);
     }
-    // inserts, appended to their rows in batch order (createDiffGraph)
-    bool relayout = false;
-    for (int32_t i = 0; i < nupd && !relayout; i++) {
+    // inserts, appended to their rows in batch order (createDiffGraph).  When
+    // a row cannot grow, everything is laid out again with fresh slack and a
+    // reserve sized for the inserts still to come (larger on each retry).
+    int relayouts = 0;
+    for (int32_t i = 0; i < nupd; i++) {
         if (flag[i] != 1) continue;
         const int32_t a = u[i], b = v[i];
         if (a < 0 || a >= n || b < 0 || b >= n) continue;
-        if (!mirror_append(m->beg, m->end, m->cap, m->arc, m->tail, a, make_uint2((uint32_t)b, w[i]), m->dirty_arc,
-                           m->dirty_row) ||
-            !mirror_append(m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, b, make_uint2((uint32_t)a, w[i]),
-                           m->dirty_rarc, m->dirty_rrow)) {
-            relayout = true;
-            break;
+        // both directions or neither
+        while (!mirror_can_append(m->beg, m->end, m->cap, m->arc, m->tail, a) ||
+               !mirror_can_append(m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, b)) {
+            if (relayouts >= 8) return fail(DDP_ERR_OOM, "dynamic graph: no room for the insert batch");
+            int64_t remaining = 0;
+            for (int32_t j = i; j < nupd; j++)
+                if (flag[j] == 1) remaining++;
+            const int64_t extra = remaining << relayouts;
+            relayouts++;
+            std::vector<int32_t> b0 = m->beg, e0 = m->end, rb0 = m->rbeg, re0 = m->rend;
+            std::vector<uint2> a0 = m->arc, ra0 = m->rarc;
+            mirror_layout(b0, e0, a0, m->beg, m->end, m->cap, m->arc, m->tail, extra);
+            mirror_layout(rb0, re0, ra0, m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, extra);
+            m->full = true;
+            g->e = (int64_t)m->arc.size();
+            g->e_rev = (int64_t)m->rarc.size();
         }
+        mirror_append(m->beg, m->end, m->cap, m->arc, m->tail, a, make_uint2((uint32_t)b, w[i]), m->dirty_arc,
+                      m->dirty_row);
+        mirror_append(m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, b, make_uint2((uint32_t)a, w[i]), m->dirty_rarc,
+                      m->dirty_rrow);
         ups.push_back(make_int4(UPD_INS, a, b, (int)w[i]));
         if (w[i] < g->wmin) g->wmin = w[i];
         if (w[i] > g->wmax) g->wmax = w[i];
-    }
-    if (relayout) {
-        // the arc arrays are full: lay everything out again with fresh slack,
-        // then append the remaining inserts
-        std::vector<int32_t> b0 = m->beg, e0 = m->end, rb0 = m->rbeg, re0 = m->rend;
-        std::vector<uint2> a0 = m->arc, ra0 = m->rarc;
-        mirror_layout(b0, e0, a0, m->beg, m->end, m->cap, m->arc, m->tail);
-        mirror_layout(rb0, re0, ra0, m->rbeg, m->rend, m->rcap, m->rarc, m->rtail);
-        m->full = true;
-        size_t done = 0;
-        for (const int4 &x : ups)
-            if (x.x == UPD_INS) done++;
-        size_t seen = 0;
-        for (int32_t i = 0; i < nupd; i++) {
-            if (flag[i] != 1) continue;
-            const int32_t a = u[i], b = v[i];
-            if (a < 0 || a >= n || b < 0 || b >= n) continue;
-            if (seen++ < done) continue;
-            if (!mirror_append(m->beg, m->end, m->cap, m->arc, m->tail, a, make_uint2((uint32_t)b, w[i]),
-                               m->dirty_arc, m->dirty_row) ||
-                !mirror_append(m->rbeg, m->rend, m->rcap, m->rarc, m->rtail, b, make_uint2((uint32_t)a, w[i]),
-                               m->dirty_rarc, m->dirty_rrow))
-                return fail(DDP_ERR_OOM, "dynamic graph: insert batch larger than the arc reserve");
-            ups.push_back(make_int4(UPD_INS, a, b, (int)w[i]));
-            if (w[i] < g->wmin) g->wmin = w[i];
-            if (w[i] > g->wmax) g->wmax = w[i];
-        }
-        g->e = (int64_t)m->arc.size();
-        g->e_rev = (int64_t)m->rarc.size();
     }
     return dyn_upload(g);
 }

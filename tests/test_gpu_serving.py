@@ -103,3 +103,45 @@ def test_serving_with_updates(gpu, oracle, nver, rounds):
         assert costs[k] == want, (i, int(ver[k]))
     assert srv.stats()["version"] == rounds
     srv.close()
+
+
+def test_serving_through_relayouts(gpu, oracle):
+    """Insert batches large enough to exhaust the arc reserve: the master
+    graph is laid out again and the version buffers take full copies (on the
+    service CTA when the kernel runs).  Requests around the batches stay
+    exact for the version they report."""
+    d = gpu
+    g, dg = _geo(d, 5000, 43)
+    srv = d.Server(dg, d.H_EUCLID, max_requests=8192, versions=3, grid=16)
+    rng = np.random.default_rng(8)
+    versions = [(g.off.copy(), g.col.copy(), g.w.copy())]
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    submitted = []
+    for rnd in range(4):
+        S = rng.integers(0, g.n, 60).astype(np.int32)
+        T = rng.integers(0, g.n, 60).astype(np.int32)
+        srv.submit(S, T)
+        submitted += list(zip(S.tolist(), T.tolist()))
+        # 70k new arcs between random pairs, weights from the length scale (heavy, so
+        # the Euclidean scale stays) plus a few light ones (the scale drops)
+        k = 70_000
+        a = rng.integers(0, g.n, k)
+        b = rng.integers(0, g.n, k)
+        keep = a != b
+        a, b = a[keep], b[keep]
+        ww = rng.integers(5_000, 50_000, len(a)).astype(np.uint32)
+        ww[:20] = 1
+        fl = np.ones(len(a), np.int32)
+        srv.update(fl, a.astype(np.int32), b.astype(np.int32), ww)
+        off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, a, b, ww)
+        versions.append((np.append(off, len(col)).astype(np.int32), col.copy(), w.copy()))
+    ids, costs, lat, ver = srv.drain()
+    assert len(ids) == len(submitted)
+    for k in range(0, len(ids), 5):
+        i = int(ids[k])
+        s_, t_ = submitted[i]
+        vo, vc, vw = versions[int(ver[k])]
+        gv = d.CSR(g.n, vo, vc, vw, xy=g.xy)
+        assert costs[k] == _oracle(oracle, gv, s_, t_, 0), (i, int(ver[k]))
+    assert srv.stats()["version"] == 4
+    srv.close()
