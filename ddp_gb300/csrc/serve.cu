@@ -464,8 +464,10 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
         return fail(DDP_ERR_INVALID, "bad serving arguments");
     *out = nullptr;
     if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS && hkind != DDP_H_BFS_CAPPED && hkind != DDP_H_MANHATTAN &&
-        hkind != DDP_H_EUCLID)
+        hkind != DDP_H_EUCLID && hkind != DDP_H_LANDMARK)
         return fail(DDP_ERR_INVALID, "unsupported heuristic kind for serving");
+    if (hkind == DDP_H_LANDMARK && !graph_view(g).lm)
+        return fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)");
     if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID) && !g->d_xy)
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_server *s = new ddp_server();
@@ -618,6 +620,8 @@ int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int
 int ddp_serve_update(ddp_server *s, int32_t n, const int32_t *flag, const int32_t *u, const int32_t *v,
                      const uint32_t *w) {
     if (!s) return fail(DDP_ERR_INVALID, "null server");
+    if (s->hkind == DDP_H_LANDMARK)
+        return fail(DDP_ERR_INVALID, "a landmark server serves a fixed graph (updates would void the landmark bounds)");
     std::lock_guard<std::mutex> lk(s->mu);
     int rc = apply_and_publish(s, n, flag, u, v, w);
     if (rc) return rc;

@@ -240,7 +240,9 @@ typedef struct ddp_server ddp_server;
  * free device memory) serve requests published in a ring of max_requests
  * entries in pinned host memory mapped into the device.  The graph is kept
  * in `versions` (2..64) device copies so that updates never stop searches
- * in flight; the graph switches to the dynamic layout. */
+ * in flight; the graph switches to the dynamic layout.  hkind: ZERO,
+ * BFS_HOPS, BFS_CAPPED, MANHATTAN, EUCLID, or LANDMARK (a fixed graph:
+ * ddp_serve_update then fails with DDP_ERR_INVALID). */
 int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t max_requests,
                      int32_t versions, ddp_server **out);
 /* Publishes n requests; *first_id = id of the first.  Non-blocking. */

@@ -145,3 +145,27 @@ def test_serving_through_relayouts(gpu, oracle):
         assert costs[k] == _oracle(oracle, gv, s_, t_, 0), (i, int(ver[k]))
     assert srv.stats()["version"] == 4
     srv.close()
+
+
+def test_serving_with_landmarks_on_a_fixed_graph(gpu, oracle):
+    """Landmark serving (the 4M-node batch heuristic in continuous
+    batching): exact answers; updates are refused, since they would void
+    the landmark bounds."""
+    d = gpu
+    g = d.gen_random_chain(20000, 6, 1, 100, 57)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.build_landmarks(8, seed=1)
+    srv = d.Server(dg, d.H_LANDMARK, max_requests=4096, grid=32)
+    rng = np.random.default_rng(2)
+    S = rng.integers(0, g.n, 100).astype(np.int32)
+    T = rng.integers(0, g.n, 100).astype(np.int32)
+    first = srv.submit(S, T)
+    ids, costs, _, _ = srv.drain()
+    gs = g.with_sentinel()
+    for k in range(0, len(ids), 9):
+        i = int(ids[k]) - first
+        f, c, _, _, _ = oracle.astar(gs.n, gs.off[:-1], gs.col, gs.w, np.zeros(gs.n, np.int32), int(S[i]), int(T[i]))
+        assert costs[k] == (c if f else d.INF)
+    with pytest.raises(d.DdpError):
+        srv.update([1], [0], [5], [1])
+    srv.close()
