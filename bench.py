@@ -48,6 +48,8 @@ CONFIGS = {
     "c5-small": dict(n=500_000, k=6, side=1 << 20, wscale=100000, gseed=5005, rates=[5000, 20000, 50000],
                      seconds=0.5, update_ms=10, wchanges=500, deletes=100, inserts=100),
     "c2dyn": dict(rows=1024, cols=1024, wall=0.30, gseed=2202, useed=2303, batches=50, moves=200),
+    "c4serve": dict(n=4_000_000, deg=8, wmin=1, wmax=100, gseed=4004, rates=[2000, 5000, 8000, 12000],
+                    seconds=1.0),
     "c4-small": dict(n=400_000, deg=8, wmin=1, wmax=100, pairs=1024, hop_lo=4, hop_hi=400, gseed=4004,
                      pseed=4400),
 }
@@ -381,17 +383,26 @@ def bench_dynamic(a, c):
 
 def bench_serving(a, c):
     """Config 5: Poisson arrivals served by continuous batching on an 8M-node
-    geometric graph, with an update batch every 10 ms."""
+    geometric graph, with an update batch every 10 ms.  With c["deg"]: the
+    4M-node random digraph with the landmark heuristic and no updates (the
+    batch workload's graph under continuous batching)."""
     import torch  # noqa: F401
 
     from ddp_gb300 import build as B
     B.build()
     import ddp_gb300 as d
     from oracle import oracle as O
-    g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
-    dg = d.DeviceGraph.from_csr(g)
-    dg.set_euclid(d.euclid_rho_fp(g))
-    srv = d.Server(dg, d.H_EUCLID, max_requests=1 << 22, grid=a.slots, block=a.block)
+    fixed = "deg" in c
+    if fixed:
+        g = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
+        dg = d.DeviceGraph.from_csr(g)
+        dg.build_landmarks(a.landmarks, seed=c["gseed"])
+        srv = d.Server(dg, d.H_LANDMARK, max_requests=1 << 22, grid=a.slots, block=a.block)
+    else:
+        g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
+        dg = d.DeviceGraph.from_csr(g)
+        dg.set_euclid(d.euclid_rho_fp(g))
+        srv = d.Server(dg, d.H_EUCLID, max_requests=1 << 22, grid=a.slots, block=a.block)
     rng = np.random.default_rng(c["gseed"] + 1)
     src = np.repeat(np.arange(g.n, dtype=np.int32), np.diff(g.off))
     deleted = []
@@ -416,8 +427,9 @@ def bench_serving(a, c):
         deleted.extend(dl.tolist())
         srv.update(np.concatenate(fl), np.concatenate(uu), np.concatenate(vv), np.concatenate(ww))
 
-    # warm up: first update builds the dynamic mirror; a few queries
-    update_batch()
+    # warm up: a first update (if the workload has them); a few queries
+    if not fixed:
+        update_batch()
     srv.submit(rng.integers(0, g.n, 64).astype(np.int32), rng.integers(0, g.n, 64).astype(np.int32))
     srv.drain()
     rows = []
@@ -428,7 +440,7 @@ def bench_serving(a, c):
         T = rng.integers(0, g.n, nreq).astype(np.int32)
         lat, got, i, n_upd = [], 0, 0, 0
         t0 = time.perf_counter()
-        next_upd = c["update_ms"] / 1000.0
+        next_upd = c.get("update_ms", 0) / 1000.0
         last = t0
         while got < nreq:
             now = time.perf_counter() - t0
@@ -436,7 +448,7 @@ def bench_serving(a, c):
             if j > i:
                 srv.submit(S[i:j], T[i:j])
                 i = j
-            if now >= next_upd and i < nreq:
+            if not fixed and now >= next_upd and i < nreq:
                 update_batch()
                 n_upd += 1
                 next_upd += c["update_ms"] / 1000.0
@@ -462,7 +474,7 @@ def bench_serving(a, c):
     keep = ids >= first
     ids, costs = ids[keep], costs[keep]
     costs = costs[np.argsort(ids)]
-    r = dg.read_csr()
+    r = g if fixed else dg.read_csr()
     exact = True
     cpu_ms = []
     for k in range(len(Sx)):
@@ -475,11 +487,14 @@ def bench_serving(a, c):
     out = {"metric": "A* serving queries/sec + p50/p99 latency (exact)", "value": best["served_qps"],
            "unit": "queries/s", "higher_is_better": True, "n_gpus": 1, "dtype": "int32",
            "data": "synthetic (seeded generators)",
-           "config": {"workload": f"serving: {c['n']:,} points uniform on a {c['side']}^2 grid, symmetric "
-                                  f"{c['k']}-NN arcs, w = max(1, round({c['wscale']} x length / mean spacing)), "
-                                  f"h = floor(rho x floor(distance)), Poisson arrivals, every {c['update_ms']} ms "
-                                  f"{c['wchanges']} weight changes x U[0.5,2] + {c['deletes']} deletes + up to "
-                                  f"{c['inserts']} re-inserts", "n": g.n, "e": g.e, "slots": st["slots"]},
+           "config": {"workload": (f"serving: {c['n']:,}-node random digraph (chain + uniform arcs), avg out-degree "
+                                   f"{c['deg']}, w U[{c['wmin']},{c['wmax']}], landmark heuristic ({a.landmarks}), "
+                                   f"uniform random endpoints, Poisson arrivals, no updates") if fixed else
+                                  (f"serving: {c['n']:,} points uniform on a {c['side']}^2 grid, symmetric "
+                                   f"{c['k']}-NN arcs, w = max(1, round({c['wscale']} x length / mean spacing)), "
+                                   f"h = floor(rho x floor(distance)), Poisson arrivals, every {c['update_ms']} ms "
+                                   f"{c['wchanges']} weight changes x U[0.5,2] + {c['deletes']} deletes + up to "
+                                   f"{c['inserts']} re-inserts"), "n": g.n, "e": g.e, "slots": st["slots"]},
            "rates": rows, "exact_on_sample": bool(exact), "server": st,
            "cpu_baseline": {"value": float(np.mean(cpu_ms)), "unit": "ms/query (Dijkstra order, h = 0)",
                             "cores": 1, "kind": "port", "sample": f"{len(cpu_ms)} queries"}}
@@ -499,7 +514,7 @@ def main():
         if rank == 0:
             bench_dynamic(a, c)
         return
-    if a.config in ("c5", "c5-small"):
+    if a.config in ("c5", "c5-small", "c4serve"):
         if rank == 0:
             bench_serving(a, c)
         return

@@ -487,13 +487,25 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
     const int per_sm = std::max(1, slots_per_sm(hkind, s->block));
     int nslots = per_sm * device_sms();
     if (s->o.grid > 0) nslots = std::min(nslots, s->o.grid);
-    const int64_t capq = s->o.queue_cap > 0 ? s->o.queue_cap : std::max<int64_t>(1 << 16, g->n / 8);
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     const bool hops = hkind == DDP_H_BFS_HOPS || hkind == DDP_H_BFS_CAPPED;
-    const size_t per = slot_bytes(g->n, capq, capq, hops);
+    // queue capacities: what each slot's share of half the free memory
+    // holds after its state, up to the batch engine's sizes (n + 4096 near,
+    // 2n + 4096 far); at least 64k.  A request that still outgrows its slot
+    // is re-run on the single-query engine when it is polled.
+    int64_t capq = s->o.queue_cap, capf = s->o.queue_cap;
+    if (capq <= 0) {
+        const size_t fixed = slot_bytes(g->n, 0, 0, hops);
+        const size_t share = (freeb / 2) / (size_t)std::max(1, nslots);
+        const size_t per_entry = 2 * sizeof(uint2) + 2 * 2 * sizeof(uint4);  // q0/q1 + two far piles of 2x
+        const int64_t fit = share > fixed ? (int64_t)((share - fixed) / per_entry) : 0;
+        capq = std::min<int64_t>((int64_t)g->n + 4096, std::max<int64_t>(1 << 16, fit));
+        capf = std::min<int64_t>(2 * (int64_t)g->n + 4096, 2 * capq);
+    }
+    const size_t per = slot_bytes(g->n, capq, capf, hops);
     if ((size_t)nslots * per > freeb / 2) nslots = (int)std::max<size_t>(1, (freeb / 2) / per);
-    int rc = slots_alloc(s->sa, g->n, nslots, capq, capq, hops, s->stream);
+    int rc = slots_alloc(s->sa, g->n, nslots, capq, capf, hops, s->stream);
     if (rc) return bail(rc);
     const size_t R = (size_t)max_requests;
     unsigned flags = cudaHostAllocMapped;
