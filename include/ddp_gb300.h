@@ -158,7 +158,10 @@ int ddp_query_free(ddp_query *q);
 /* ---- batched multi-query engine (no reference counterpart: the
  *      reference solves one (s,t) per process, GA_v2.cu:301-305) --------- */
 /* hkind: DDP_H_ZERO, DDP_H_BFS_HOPS / DDP_H_BFS_CAPPED (per target, built
- * inside the batch kernel) or DDP_H_MANHATTAN.  A query whose search outgrew
+ * inside the batch kernel), DDP_H_MANHATTAN, DDP_H_EUCLID (coordinates) or
+ * DDP_H_LANDMARK (ddp_landmarks_build first).  opts: group = CTAs per slot
+ * (1 = the asynchronous one-CTA engine), block, K, delta, grid = slot cap;
+ * ddp_batch_tune picks them.  A query whose search outgrew
  * its slot's queues reports cost -1 from ddp_batch_solve_device;
  * ddp_batch_solve re-runs such queries on the single-query engine. */
 int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batch **out);
