@@ -43,7 +43,8 @@ CONFIGS = {
     "c2": dict(rows=2048, cols=2048, wall=0.30, gseed=2002),
     "c3": dict(n=1_000_000, deg=10, wmin=1, wmax=1000, gseed=3003, useed=3303, batches=100, per_batch=1000,
                inserts=500),
-    "c5": dict(n=8_000_000, k=6, side=1 << 20, wscale=100000, gseed=5005, rates=[5000, 20000, 50000, 100000, 200000],
+    "c5": dict(n=8_000_000, k=6, side=1 << 20, wscale=100000, gseed=5005,
+               rates=[500, 1000, 5000, 20000, 50000, 100000, 200000],  # 500, 1000: below capacity
                seconds=1.0, update_ms=10, wchanges=500, deletes=100, inserts=100),
     "c5-small": dict(n=500_000, k=6, side=1 << 20, wscale=100000, gseed=5005, rates=[5000, 20000, 50000],
                      seconds=0.5, update_ms=10, wchanges=500, deletes=100, inserts=100),
