@@ -4,7 +4,7 @@
 Workload (default, `--config c4`): 4,096 seeded source/target pairs on a
 4M-node random digraph (Hamiltonian chain + uniform arcs, average out-degree
 8, int32 weights uniform in [1,100]); heuristic h = the ALT landmark bound
-from 16 landmarks (the landmark table is built once per graph, outside the
+from 32 landmarks (the landmark table is built once per graph, outside the
 timed region; `--heuristic capped` restores the per-query reverse BFS built
 inside the batch kernel); slot shape, bucket width and K from the
 autotuner, run on random queries before timing.  One step = one batch of
@@ -85,7 +85,7 @@ def args_parse():
                    help="take group/block/delta/K from the flags instead of the autotuner")
     p.add_argument("--tune-sample", type=int, default=0,
                    help="random queries the autotuner times (0 = as many as the measured batch)")
-    p.add_argument("--landmarks", type=int, default=16, help="landmark count for --heuristic landmark")
+    p.add_argument("--landmarks", type=int, default=32, help="landmark count for --heuristic landmark (128-B rows)")
     p.add_argument("--heuristic", default="landmark", choices=["capped", "bfs", "zero", "landmark"],
                    help="landmark: ALT bound from --landmarks landmarks (table built once per graph); "
                         "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "

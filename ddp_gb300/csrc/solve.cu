@@ -828,8 +828,8 @@ extern "C" {
 
 int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out_ids) {
     if (!g) return fail(DDP_ERR_INVALID, "null graph");
-    if (count < 4 || count > 32 || count % 4)
-        return fail(DDP_ERR_INVALID, "landmark count must be 4, 8, ..., 32");
+    if (count < 4 || count > 64 || count % 4)
+        return fail(DDP_ERR_INVALID, "landmark count must be 4, 8, ..., 64");
     std::lock_guard<std::mutex> lk(g->mu);
     const int32_t n = g->n;
     const int32_t width = 2 * count;

@@ -118,7 +118,7 @@ int ddp_graph_free(ddp_graph *g);
 
 /* ---- heuristic: GA_star/bfs_hx.cu (program), LIB a_star.h:34
  *      set_huiristics(U*) ------------------------------------------------ */
-/* Landmark table for DDP_H_LANDMARK: `count` (4, 8, ..., 32) landmarks picked
+/* Landmark table for DDP_H_LANDMARK: `count` (4, 8, ..., 64) landmarks picked
  * farthest-first from a seeded start, with distances to and from every
  * node from 2 x count exhaustive searches on the device, stored as 16-bit
  * entries (count x 4 bytes per node): exact while every distance is below

@@ -48,7 +48,7 @@ def _oracle(O, g, s, t):
     return c if f else 2147483647
 
 
-@pytest.mark.parametrize("count", [4, 16])
+@pytest.mark.parametrize("count", [4, 16, 32])
 def test_landmark_table_and_values(gpu, count):
     d = gpu
     g = d.gen_random_chain(3000, 4, 1, 50, 71)
