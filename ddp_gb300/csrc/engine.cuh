@@ -173,11 +173,28 @@ struct HeurALT {
         const uint2 *rt = tab + (size_t)t * (2 * W);
         int32_t h = 0;
         bool cut = false;
-        for (int i = 0; i < W; i++) {
-            const uint2 fv = __ldg(rv + i), ft = __ldg(rt + i);
-            const uint2 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
-            terms(ft, fv, h, cut);
-            terms(bv, bt, h, cut);
+        if ((W & 1) == 0) {
+            // rows of 4L bytes with L % 8 == 0: both halves start on a
+            // 16-byte boundary, so each load takes 8 landmarks
+            const uint4 *qv = reinterpret_cast<const uint4 *>(rv), *qt = reinterpret_cast<const uint4 *>(rt);
+            const int W2 = W >> 1;
+            for (int i = 0; i < W2; i++) {
+                const uint4 fv = __ldg(qv + i), ft = __ldg(qt + i);
+                terms(make_uint2(ft.x, ft.y), make_uint2(fv.x, fv.y), h, cut);
+                terms(make_uint2(ft.z, ft.w), make_uint2(fv.z, fv.w), h, cut);
+            }
+            for (int i = W2; i < 2 * W2; i++) {
+                const uint4 bv = __ldg(qv + i), bt = __ldg(qt + i);
+                terms(make_uint2(bv.x, bv.y), make_uint2(bt.x, bt.y), h, cut);
+                terms(make_uint2(bv.z, bv.w), make_uint2(bt.z, bt.w), h, cut);
+            }
+        } else {
+            for (int i = 0; i < W; i++) {
+                const uint2 fv = __ldg(rv + i), ft = __ldg(rt + i);
+                const uint2 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
+                terms(ft, fv, h, cut);
+                terms(bv, bt, h, cut);
+            }
         }
         return cut ? INF_G : (uint32_t)h;
     }
@@ -434,8 +451,11 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                     // independent loads issued together (speculatively for
                     // entries that turn out stale)
                     const uint64_t su = __ldcg(B.state + u);
-                    // until t is reached (f(t) infinite) the pop test passes for any h
-                    const uint32_t hu = ft != 0xFFFFFFFFu ? H(u) : 0u;
+                    // every near entry was pushed with f = g + h(u) < T
+                    // (relaxations, split and compaction moves alike; T only
+                    // grows), so while f(t) >= T the pop test f < f(t)
+                    // passes without reading h again; keep mode re-derives it
+                    const uint32_t hu = (ft < T || (P.keep && ft != 0xFFFFFFFFu)) ? H(u) : 0u;
                     const int r0 = row_begin(G.off, G.oend, u), r1 = row_end(G.off, G.oend, u);
                     int d0 = 0, d1 = 0;
                     if (has_diff) {

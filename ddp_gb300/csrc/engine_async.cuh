@@ -171,8 +171,12 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                     // the older g only relaxes worse labels, which the newer
                     // entry corrects
                     const uint64_t su = (have && latency) ? st_make(gu, 0) : __ldcg(B.state + u);
-                    // until t is reached (f(t) infinite) the pop test passes for any h
-                    const uint32_t hu = ft != 0xFFFFFFFFu ? H(u) : 0u;
+                    // every entry of the current bucket was pushed with
+                    // f = g + h(u) < T (near pushes, split moves and the
+                    // source alike; T only grows), so while f(t) >= T the pop
+                    // test f < f(t) passes without reading h again; keep mode
+                    // re-derives it
+                    const uint32_t hu = (ft < T || (P.keep && ft != 0xFFFFFFFFu)) ? H(u) : 0u;
                     const int r0 = have ? pre.x : row_begin(G.off, G.oend, u);
                     const int r1 = have ? pre.y : row_end(G.off, G.oend, u);
                     if (st_g(su) == gu && u != P.t) {
