@@ -4,8 +4,8 @@
 Workload (default, `--config c4`): 4,096 seeded source/target pairs on a
 4M-node random digraph (Hamiltonian chain + uniform arcs, average out-degree
 8, int32 weights uniform in [1,100]); heuristic h = the ALT landmark bound
-from 32 landmarks (the landmark table is built once per graph, outside the
-timed region; `--heuristic capped` restores the per-query reverse BFS built
+from 64 landmarks stored as 8-bit entries (128-B rows; the table is built
+once per graph, outside the timed region; `--heuristic capped` restores the per-query reverse BFS built
 inside the batch kernel); slot shape, bucket width and K from the
 autotuner, run on random queries before timing.  One step = one batch of
 all pairs through the persistent batch kernel.
@@ -85,7 +85,9 @@ def args_parse():
                    help="take group/block/delta/K from the flags instead of the autotuner")
     p.add_argument("--tune-sample", type=int, default=0,
                    help="random queries the autotuner times (0 = as many as the measured batch)")
-    p.add_argument("--landmarks", type=int, default=32, help="landmark count for --heuristic landmark (128-B rows)")
+    p.add_argument("--landmarks", type=int, default=64, help="landmark count for --heuristic landmark")
+    p.add_argument("--landmark-bits", type=int, default=8, choices=[16, 8],
+                   help="landmark table entry width (rows of 2 x landmarks entries)")
     p.add_argument("--heuristic", default="landmark", choices=["capped", "bfs", "zero", "landmark"],
                    help="landmark: ALT bound from --landmarks landmarks (table built once per graph); "
                         "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
@@ -156,32 +158,39 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch(config_name, pairs, heuristic="capped"):
+def traffic_per_launch(config_name, pairs, heuristic="capped", table=None):
     """dram bytes of one k_batch launch from the committed ncu summary
     (profiles/k_batch_<config>[_<heuristic>].md, line
-    `traffic_bytes_per_query: X`), scaled to this launch's query count."""
+    `traffic_bytes_per_query: X`), scaled to this launch's query count.  A
+    summary with a `traffic_table: L x B-bit` line covers that landmark
+    table only (None for another)."""
     suffix = "" if heuristic == "capped" else f"_{heuristic}"
     p = os.path.join(ROOT, "profiles", f"k_batch_{config_name}{suffix}.md")
+    per_query, covers = None, None
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_query:"):
-                return float(line.split(":")[1]) * pairs
+                per_query = float(line.split(":")[1])
+            elif line.startswith("traffic_table:"):
+                covers = line.split(":", 1)[1].strip()
     except OSError:
-        pass
-    return None
+        return None
+    if per_query is None or (covers is not None and covers != table):
+        return None
+    return per_query * pairs
 
 
-def algorithmic_bytes(st, landmarks=0):
+def algorithmic_bytes(st, landmarks=0, bits=16):
     """Per-query bytes of the algorithm (graph-search accounting):
     12 B per expanded node (2 offsets + g), 16 B per scanned arc (head, w,
     h(head), g(head)), 16 B per successful relaxation (g, parent, queue
     push), and for the heuristic BFS 12 B per reached node + 8 B per scanned
     reverse arc.  With L landmarks h is read only for a relaxation that
-    improves g: 12 B per scanned arc and 16 + 4 L B per relaxation (the
-    node's row of 2 L 16-bit distances), no BFS."""
+    improves g: 12 B per scanned arc and 16 + 2 L bits / 8 B per relaxation
+    (the node's row of 2 L distances of `bits` bits), no BFS."""
     st = np.asarray(st, np.float64)
     if landmarks:
-        return 12 * st[:, 0] + 12 * st[:, 1] + (16 + 4 * landmarks) * st[:, 2]
+        return 12 * st[:, 0] + 12 * st[:, 1] + (16 + 2 * landmarks * bits // 8) * st[:, 2]
     return 12 * st[:, 0] + 16 * st[:, 1] + 16 * st[:, 2] + 12 * st[:, 4] + 8 * st[:, 5]
 
 
@@ -402,7 +411,7 @@ def bench_serving(a, c):
     if fixed:
         g = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
         dg = d.DeviceGraph.from_csr(g)
-        dg.build_landmarks(a.landmarks, seed=c["gseed"])
+        dg.build_landmarks(a.landmarks, seed=c["gseed"], bits=a.landmark_bits)
         srv = d.Server(dg, d.H_LANDMARK, max_requests=1 << 22, grid=a.slots, block=a.block)
     else:
         g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
@@ -554,7 +563,7 @@ def main():
         # per-graph preprocessing (2 x L exhaustive searches), outside the timed region
         torch.cuda.synchronize(dev)
         l0 = time.perf_counter()
-        dg.build_landmarks(lm, seed=c["gseed"])
+        dg.build_landmarks(lm, seed=c["gseed"], bits=a.landmark_bits)
         lm_s = time.perf_counter() - l0
     opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group)
     tuned = None
@@ -605,10 +614,11 @@ def main():
     launches = be.launches() * a.steps
     value = world * pairs * a.steps / tmax
     kernel_s = elapsed / a.steps
-    alg = float(algorithmic_bytes(st, lm).sum())
+    alg = float(algorithmic_bytes(st, lm, a.landmark_bits).sum())
     peak, peak_kind = peak_hbm()
     achieved = alg / kernel_s / 1e9
-    traffic = traffic_per_launch(a.config, pairs, a.heuristic)
+    traffic = traffic_per_launch(a.config, pairs, a.heuristic,
+                                 f"{lm} x {a.landmark_bits}-bit" if lm else None)
     lat_service = (t1 - t0) / 1e6
     lat_complete = (t1 - t0.min()) / 1e6
 
@@ -666,6 +676,7 @@ def main():
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)",
         "config": {"workload": workload_name(c), "n": g.n, "e": g.e, "pairs_per_gpu": pairs,
                    "heuristic": a.heuristic, "landmarks": lm or None,
+                   "landmark_bits": a.landmark_bits if lm else None,
                    "landmark_build_s": lm_s, "autotuner": tuned,
                    "slots": be.info()["slots"], "block": be.info()["block"], "K": opts["K"],
                    "group": be.info()["group"],

@@ -406,10 +406,11 @@ class DeviceGraph:
     def set_euclid(self, rho_fp: int) -> None:
         check(lib().ddp_graph_set_euclid(self.handle, int(rho_fp)))
 
-    def build_landmarks(self, count: int = 16, seed: int = 1) -> np.ndarray:
-        """Landmark table for H_LANDMARK; returns the landmark ids."""
+    def build_landmarks(self, count: int = 16, seed: int = 1, bits: int = 16) -> np.ndarray:
+        """Landmark table for H_LANDMARK with `bits` (16 or 8) per entry;
+        returns the landmark ids."""
         ids = np.empty(count, np.int32)
-        check(lib().ddp_landmarks_build(self.handle, int(count), int(seed), ptr(ids)))
+        check(lib().ddp_landmarks_build_bits(self.handle, int(count), int(bits), int(seed), ptr(ids)))
         return ids
 
     def info(self):

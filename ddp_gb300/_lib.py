@@ -33,6 +33,7 @@ SIGNATURES = {
     "ddp_graph_read_csr": (C.c_int, [vp, i32p, i32p, u32p]),
     "ddp_graph_free": (C.c_int, [vp]),
     "ddp_landmarks_build": (C.c_int, [vp, C.c_int32, C.c_uint64, C.POINTER(C.c_int32)]),
+    "ddp_landmarks_build_bits": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(C.c_int32)]),
     "ddp_heuristic_build": (C.c_int, [vp, C.c_int32, C.c_int32, i32p, i32p, C.POINTER(vp)]),
     "ddp_heuristic_free": (C.c_int, [vp]),
     "ddp_solve": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.POINTER(Opts), C.POINTER(vp)]),

@@ -70,15 +70,19 @@ struct DevGraph {
     const int32_t *oend;
     const int32_t *roend;
     // Landmark distances (ALT heuristic), null when not built: row v holds
-    // lm_L values q(L_i, v) then lm_L values q(v, L_i), 16 bits each, with
-    // q = floor(d / lm_scale) and LM_UNREACHED16 when there is no path.
-    // lm_L is a multiple of 4 (rows of 8-byte words).
+    // lm_L values q(L_i, v) then lm_L values q(v, L_i), lm_bits (16 or 8)
+    // each, with q = floor(d / lm_scale) and the all-ones entry
+    // (LM_UNREACHED16 / LM_UNREACHED8) when there is no path.  Each half row
+    // is a whole number of 8-byte words: lm_L is a multiple of 4 (16-bit)
+    // or of 8 (8-bit).
     const uint2 *lm;
     int32_t lm_L;
     int32_t lm_scale;
+    int32_t lm_bits;
 };
 constexpr int32_t LM_UNREACHED = 0x7FFFFFFF;  // exhaustive-search distances
-constexpr uint32_t LM_UNREACHED16 = 0xFFFFu;  // table entries
+constexpr uint32_t LM_UNREACHED16 = 0xFFFFu;  // 16-bit table entries
+constexpr uint32_t LM_UNREACHED8 = 0xFFu;     // 8-bit table entries
 
 __device__ __forceinline__ int row_end(const int32_t *off, const int32_t *oend, int u) {
     return oend ? __ldcg(oend + u) : __ldg(off + u + 1);

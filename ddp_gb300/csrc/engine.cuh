@@ -152,52 +152,61 @@ struct HeurManhattan {
 // exact difference when s = 1.  A landmark that reaches v but not t, or is
 // reached from t but not from v, proves that v cannot reach t.
 struct HeurALT {
-    const uint2 *tab;  // DevGraph::lm: rows of L / 2 words
-    int32_t L;         // landmarks, a multiple of 4
+    const uint2 *tab;  // DevGraph::lm: rows of 2L entries
+    int32_t L;         // landmarks, a multiple of 4 (16-bit) or 8 (8-bit)
     int32_t s;         // DevGraph::lm_scale
     int32_t t;
+    int32_t bits;      // DevGraph::lm_bits: 16 or 8
+    template <int B>
     __device__ __forceinline__ void term(uint32_t a, uint32_t b, int32_t &h, bool &cut) const {
         // a - b with a from the row that must be larger
-        if (a != LM_UNREACHED16 && b != LM_UNREACHED16) h = max(h, ((int32_t)a - (int32_t)b) * s - (s - 1));
-        else if (a == LM_UNREACHED16 && b != LM_UNREACHED16) cut = true;
+        constexpr uint32_t UNR = (1u << B) - 1u;
+        if (a != UNR && b != UNR) h = max(h, ((int32_t)a - (int32_t)b) * s - (s - 1));
+        else if (a == UNR && b != UNR) cut = true;
     }
+    template <int B>
+    __device__ __forceinline__ void word(uint32_t a, uint32_t b, int32_t &h, bool &cut) const {
+        constexpr uint32_t M = (1u << B) - 1u;
+#pragma unroll
+        for (int k = 0; k < 32; k += B) term<B>((a >> k) & M, (b >> k) & M, h, cut);
+    }
+    template <int B>
     __device__ __forceinline__ void terms(uint2 a, uint2 b, int32_t &h, bool &cut) const {
-        term(a.x & 0xFFFFu, b.x & 0xFFFFu, h, cut);
-        term(a.x >> 16, b.x >> 16, h, cut);
-        term(a.y & 0xFFFFu, b.y & 0xFFFFu, h, cut);
-        term(a.y >> 16, b.y >> 16, h, cut);
+        word<B>(a.x, b.x, h, cut);
+        word<B>(a.y, b.y, h, cut);
     }
-    __device__ uint32_t operator()(int32_t v) const {
-        const int W = L >> 2;  // 8-byte words per half row (4 landmarks each)
+    template <int B>
+    __device__ __forceinline__ uint32_t eval(int32_t v) const {
+        const int W = L / (64 / B);  // 8-byte words per half row
         const uint2 *rv = tab + (size_t)v * (2 * W);
         const uint2 *rt = tab + (size_t)t * (2 * W);
         int32_t h = 0;
         bool cut = false;
         if ((W & 1) == 0) {
-            // rows of 4L bytes with L % 8 == 0: both halves start on a
-            // 16-byte boundary, so each load takes 8 landmarks
+            // both halves start on a 16-byte boundary: 16-byte loads
             const uint4 *qv = reinterpret_cast<const uint4 *>(rv), *qt = reinterpret_cast<const uint4 *>(rt);
             const int W2 = W >> 1;
             for (int i = 0; i < W2; i++) {
                 const uint4 fv = __ldg(qv + i), ft = __ldg(qt + i);
-                terms(make_uint2(ft.x, ft.y), make_uint2(fv.x, fv.y), h, cut);
-                terms(make_uint2(ft.z, ft.w), make_uint2(fv.z, fv.w), h, cut);
+                terms<B>(make_uint2(ft.x, ft.y), make_uint2(fv.x, fv.y), h, cut);
+                terms<B>(make_uint2(ft.z, ft.w), make_uint2(fv.z, fv.w), h, cut);
             }
             for (int i = W2; i < 2 * W2; i++) {
                 const uint4 bv = __ldg(qv + i), bt = __ldg(qt + i);
-                terms(make_uint2(bv.x, bv.y), make_uint2(bt.x, bt.y), h, cut);
-                terms(make_uint2(bv.z, bv.w), make_uint2(bt.z, bt.w), h, cut);
+                terms<B>(make_uint2(bv.x, bv.y), make_uint2(bt.x, bt.y), h, cut);
+                terms<B>(make_uint2(bv.z, bv.w), make_uint2(bt.z, bt.w), h, cut);
             }
         } else {
             for (int i = 0; i < W; i++) {
                 const uint2 fv = __ldg(rv + i), ft = __ldg(rt + i);
                 const uint2 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
-                terms(ft, fv, h, cut);
-                terms(bv, bt, h, cut);
+                terms<B>(ft, fv, h, cut);
+                terms<B>(bv, bt, h, cut);
             }
         }
         return cut ? INF_G : (uint32_t)h;
     }
+    __device__ uint32_t operator()(int32_t v) const { return bits == 8 ? eval<8>(v) : eval<16>(v); }
 };
 
 // floor(sqrt(x)) for x < 2^62, exact: a float estimate, then integer fix-up

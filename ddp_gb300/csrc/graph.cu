@@ -72,6 +72,7 @@ DevGraph graph_view(const ddp_graph *g) {
     d.lm = lm_ok ? g->d_lm : nullptr;
     d.lm_L = lm_ok ? g->lm_L : 0;
     d.lm_scale = lm_ok ? g->lm_scale : 1;
+    d.lm_bits = lm_ok ? g->lm_bits : 16;
     return d;
 }
 

@@ -63,6 +63,7 @@ struct ddp_graph {
     uint2 *d_lm = nullptr;
     int32_t lm_L = 0;
     int32_t lm_scale = 1;
+    int32_t lm_bits = 16;
     int64_t lm_stamp = -1;
     std::vector<int32_t> lm_ids;
     // single-query workspace, allocated on first use

@@ -149,11 +149,12 @@ __global__ void k_put_column(int32_t *tab, int32_t width, int32_t c, const int32
     if (v < n) tab[v * width + c] = dist[v];
 }
 
-// 16-bit table entries from exhaustive-search distances: floor(d / scale)
-__global__ void k_pack_landmarks(const int32_t *tab32, uint16_t *tab16, int64_t count, int32_t scale) {
+// 16- or 8-bit table entries from exhaustive-search distances: floor(d / scale)
+template <class E>
+__global__ void k_pack_landmarks(const int32_t *tab32, E *tab, int64_t count, int32_t scale) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t d = tab32[i];
-        tab16[i] = d == LM_UNREACHED ? (uint16_t)LM_UNREACHED16 : (uint16_t)(d / scale);
+        tab[i] = d == LM_UNREACHED ? (E)~(E)0 : (E)(d / scale);
     }
 }
 
@@ -161,7 +162,7 @@ __global__ void k_pack_landmarks(const int32_t *tab32, uint16_t *tab16, int64_t 
 __global__ void k_alt_values(DevGraph G, int32_t t, int32_t *out) {
     const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= G.n) return;
-    const uint32_t h = HeurALT{G.lm, G.lm_L, G.lm_scale, t}(v);
+    const uint32_t h = HeurALT{G.lm, G.lm_L, G.lm_scale, t, G.lm_bits}(v);
     out[v] = h >= INF_G ? -1 : (int32_t)h;
 }
 
@@ -317,7 +318,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
             r = slot_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows, sq, async);
         } else if (HK == 4) {
-            r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, G.lm_scale, t}, P, wrows, sq, async);
+            r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, G.lm_scale, t, G.lm_bits}, P, wrows, sq, async);
         } else {
             r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
         }
@@ -827,9 +828,16 @@ static int sssp_into(ddp_graph *g, int32_t src, bool reverse, int32_t *dist) {
 extern "C" {
 
 int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out_ids) {
+    return ddp_landmarks_build_bits(g, count, 16, seed, out_ids);
+}
+
+int ddp_landmarks_build_bits(ddp_graph *g, int32_t count, int32_t bits, uint64_t seed, int32_t *out_ids) {
     if (!g) return fail(DDP_ERR_INVALID, "null graph");
-    if (count < 4 || count > 64 || count % 4)
-        return fail(DDP_ERR_INVALID, "landmark count must be 4, 8, ..., 64");
+    if (bits != 16 && bits != 8) return fail(DDP_ERR_INVALID, "landmark entries are 16 or 8 bits");
+    if (bits == 16 && (count < 4 || count > 64 || count % 4))
+        return fail(DDP_ERR_INVALID, "landmark count must be 4, 8, ..., 64 (16-bit entries)");
+    if (bits == 8 && (count < 8 || count > 128 || count % 8))
+        return fail(DDP_ERR_INVALID, "landmark count must be 8, 16, ..., 128 (8-bit entries)");
     std::lock_guard<std::mutex> lk(g->mu);
     const int32_t n = g->n;
     const int32_t width = 2 * count;
@@ -851,7 +859,7 @@ int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out
     // seeded random node
     std::vector<int64_t> score((size_t)n, INT64_MAX);
     std::vector<int32_t> fw((size_t)n), bw((size_t)n);
-    int32_t maxd = 0;  // largest finite landmark distance (sets the 16-bit scale)
+    int32_t maxd = 0;  // largest finite landmark distance (sets the table's scale)
     auto measure = [&](int32_t src, int col) -> int {
         int rc = sssp_into(g, src, false, dist);
         if (rc) return rc;
@@ -909,22 +917,27 @@ int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out
         rc = measure(ids.back(), i);
         if (rc) return done(rc);
     }
-    // 16-bit entries: q = floor(d / scale) with every finite q below the
-    // unreachable marker
-    const int32_t scale = std::max(1, (maxd + 65533) / 65534);
-    uint16_t *tab16 = nullptr;
-    e = cudaMalloc(&tab16, sizeof(uint16_t) * (size_t)n * width);
+    // entries q = floor(d / scale) with every finite q below the all-ones
+    // unreachable marker: the smallest scale with maxd / scale <= marker - 1
+    const int32_t top = bits == 16 ? 65534 : 254;
+    const int32_t scale = std::max(1, (int32_t)(((int64_t)maxd + top - 1) / top));
+    void *packed = nullptr;
+    e = cudaMalloc(&packed, (size_t)(bits / 8) * (size_t)n * width);
     if (e != cudaSuccess) return done(cuda_fail(e, "cudaMalloc(landmarks)"));
-    k_pack_landmarks<<<4 * device_sms(), 256, 0, g->stream>>>(tab, tab16, (int64_t)n * width, scale);
+    if (bits == 16)
+        k_pack_landmarks<<<4 * device_sms(), 256, 0, g->stream>>>(tab, (uint16_t *)packed, (int64_t)n * width, scale);
+    else
+        k_pack_landmarks<<<4 * device_sms(), 256, 0, g->stream>>>(tab, (uint8_t *)packed, (int64_t)n * width, scale);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) {
-        cudaFree(tab16);
+        cudaFree(packed);
         return done(cuda_fail(e, "landmark table packing"));
     }
     cudaFree(g->d_lm);
-    g->d_lm = reinterpret_cast<uint2 *>(tab16);
+    g->d_lm = reinterpret_cast<uint2 *>(packed);
     g->lm_scale = scale;
+    g->lm_bits = bits;
     g->lm_L = count;
     g->lm_stamp = g->update_count;
     g->lm_ids = ids;
@@ -975,7 +988,7 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             HeurManhattan Hm{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->wmin};
             HeurEuclid He{g->d_xy, h ? h->tx : 0, h ? h->ty : 0, g->rho_fp};
             HeurArray Ha{h ? h->d_h : nullptr};
-            HeurALT Hl{G.lm, G.lm_L, G.lm_scale, target};
+            HeurALT Hl{G.lm, G.lm_L, G.lm_scale, target, G.lm_bits};
             HeurZero Hz{};
             const void *fn;
             if (kind == DDP_H_BFS_HOPS || kind == DDP_H_BFS_CAPPED) { fn = (const void *)k_solve_cta<HeurHops>; hp = &Hh; }
@@ -1007,7 +1020,7 @@ int ddp_solve(ddp_graph *g, const ddp_heuristic *h, int32_t source, int32_t targ
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurArray>, grid, block, args, st);
         } else if (kind == DDP_H_LANDMARK) {
-            HeurALT H{G.lm, G.lm_L, G.lm_scale, target};
+            HeurALT H{G.lm, G.lm_L, G.lm_scale, target, G.lm_bits};
             int grid = coop_grid(k_solve_single<HeurALT>, block, o.grid);
             void *args[] = {&G, &w->sa, &H, &P, &w->d_out, &w->d_path, &g->n};
             e = coop_launch(k_solve_single<HeurALT>, grid, block, args, st);

@@ -129,6 +129,13 @@ int ddp_graph_free(ddp_graph *g);
  * reference counterpart. */
 int ddp_landmarks_build(ddp_graph *g, int32_t count, uint64_t seed, int32_t *out_ids);
 
+/* ddp_landmarks_build with the entry width chosen: bits = 16 (as above) or
+ * 8 (count = 8, 16, ..., 128; count x 2 bytes per node; exact while every
+ * distance is below 255, else floor(d / s) with the smallest such s).
+ * Halving the row halves the bytes each heuristic evaluation reads, for a
+ * bound that is up to s - 1 weaker per term.  No reference counterpart. */
+int ddp_landmarks_build_bits(ddp_graph *g, int32_t count, int32_t bits, uint64_t seed, int32_t *out_ids);
+
 /* Builds h for `target` on the device.  user_h (DDP_H_USER only) holds n
  * values; negative values mean "target unreachable from here".  out_h
  * (optional, n values) receives h, -1 for nodes that cannot reach target. */

@@ -27,17 +27,27 @@ def _scipy_dists(g, ids):
     return conv(fw), conv(bw)
 
 
-def _alt(fw, bw, t):
-    """h(v) for target t from landmark distances (rows: landmarks); -1 = cut."""
+def _scale(fw, bw, bits):
+    """Smallest s with every finite floor(d / s) below the all-ones marker."""
+    fin = np.concatenate([fw[fw != UNR], bw[bw != UNR]])
+    top = (1 << bits) - 2
+    return max(1, -(-int(fin.max()) // top)) if fin.size else 1
+
+
+def _alt(fw, bw, t, s=1):
+    """h(v) for target t from landmark distances (rows: landmarks) stored as
+    q = floor(d / s): each term s (q_a - q_b) - (s - 1); -1 = cut."""
     n = fw.shape[1]
     h = np.zeros(n, np.int64)
     cut = np.zeros(n, bool)
     for F, B in zip(fw, bw):
+        qF = np.where(F != UNR, F // s, UNR)
+        qB = np.where(B != UNR, B // s, UNR)
         ok = (F[t] != UNR) & (F != UNR)
-        h = np.where(ok, np.maximum(h, F[t] - F), h)
+        h = np.where(ok, np.maximum(h, (qF[t] - qF) * s - (s - 1)), h)
         cut |= (F[t] == UNR) & (F != UNR)
         ok = (B != UNR) & (B[t] != UNR)
-        h = np.where(ok, np.maximum(h, B - B[t]), h)
+        h = np.where(ok, np.maximum(h, (qB - qB[t]) * s - (s - 1)), h)
         cut |= (B == UNR) & (B[t] != UNR)
     return np.where(cut, -1, h)
 
@@ -48,26 +58,31 @@ def _oracle(O, g, s, t):
     return c if f else 2147483647
 
 
-@pytest.mark.parametrize("count", [4, 16, 32])
-def test_landmark_table_and_values(gpu, count):
+@pytest.mark.parametrize("count,bits", [(4, 16), (16, 16), (32, 16), (8, 8), (32, 8), (64, 8)])
+def test_landmark_table_and_values(gpu, count, bits):
     d = gpu
-    g = d.gen_random_chain(3000, 4, 1, 50, 71)
+    # heavier arcs for 8-bit entries, so that the table needs a scale > 1
+    g = d.gen_random_chain(3000, 4, 1, 50 if bits == 16 else 400, 71)
     dg = d.DeviceGraph.from_csr(g)
-    ids = dg.build_landmarks(count, seed=3)
+    ids = dg.build_landmarks(count, seed=3, bits=bits)
     assert len(set(ids.tolist())) == count
     fw, bw = _scipy_dists(g, ids)
+    s = _scale(fw, bw, bits)
+    if bits == 8:
+        assert s > 1
     rng = np.random.default_rng(2)
     for t in rng.integers(0, g.n, 6):
         h = dg.heuristic(int(t), d.H_LANDMARK, want_values=True)
-        assert np.array_equal(h.values.astype(np.int64), _alt(fw, bw, int(t)))
+        assert np.array_equal(h.values.astype(np.int64), _alt(fw, bw, int(t), s))
         assert h.values[t] == 0
 
 
-def test_landmark_single_and_batch_exact(gpu, oracle):
+@pytest.mark.parametrize("bits", [16, 8])
+def test_landmark_single_and_batch_exact(gpu, oracle, bits):
     d = gpu
     g = d.gen_random_chain(20000, 6, 1, 100, 72)
     dg = d.DeviceGraph.from_csr(g)
-    dg.build_landmarks(8, seed=5)
+    dg.build_landmarks(8, seed=5, bits=bits)
     rng = np.random.default_rng(9)
     S = rng.integers(0, g.n, 48).astype(np.int32)
     T = rng.integers(0, g.n, 48).astype(np.int32)
@@ -87,7 +102,8 @@ def test_landmark_single_and_batch_exact(gpu, oracle):
             assert ok, why
 
 
-def test_landmark_disconnected(gpu, oracle):
+@pytest.mark.parametrize("bits", [16, 8])
+def test_landmark_disconnected(gpu, oracle, bits):
     """Sparse random arcs (no chain): many pairs have no path; the cut rule
     must prune only nodes that cannot reach t."""
     d = gpu
@@ -105,7 +121,7 @@ def test_landmark_disconnected(gpu, oracle):
     w = rng.integers(1, 30, len(b)).astype(np.uint32)
     g = d.CSR(n, off, b.astype(np.int32), w)
     dg = d.DeviceGraph.from_csr(g)
-    dg.build_landmarks(8, seed=1)
+    dg.build_landmarks(8, seed=1, bits=bits)
     S = rng.integers(0, n, 64).astype(np.int32)
     T = rng.integers(0, n, 64).astype(np.int32)
     # plus pairs two arcs apart (reachable)
@@ -135,14 +151,15 @@ def test_landmark_table_goes_stale(gpu):
     dg.heuristic(5, d.H_LANDMARK).close()
 
 
-def test_landmark_scaled_table_admissible(gpu, oracle):
-    """Weights up to 60,000 push distances past 16 bits: the table stores
-    floor(d / s); h must stay a lower bound of the true distance to t and
-    costs stay exact."""
+@pytest.mark.parametrize("bits", [16, 8])
+def test_landmark_scaled_table_admissible(gpu, oracle, bits):
+    """Weights up to 60,000 push distances past 16 (and 8) bits: the table
+    stores floor(d / s); h must stay a lower bound of the true distance to t
+    and costs stay exact."""
     d = gpu
     g = d.gen_random_chain(3000, 4, 20000, 60000, 74)
     dg = d.DeviceGraph.from_csr(g)
-    ids = dg.build_landmarks(8, seed=4)
+    ids = dg.build_landmarks(8, seed=4, bits=bits)
     lfw, _ = _scipy_dists(g, ids)
     assert lfw[lfw != UNR].max() > 65534  # the table needs a scale > 1
     rng = np.random.default_rng(6)
