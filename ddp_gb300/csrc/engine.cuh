@@ -147,9 +147,10 @@ struct HeurManhattan {
 };
 
 // ALT lower bound: max over landmarks L of d(L,t) - d(L,v) and d(v,L) - d(t,L)
-// (triangle inequality, so admissible and consistent).  The table holds
-// q = floor(d / s); d(a) - d(b) >= s (q_a - q_b) - (s - 1), which is the
-// exact difference when s = 1.  A landmark that reaches v but not t, or is
+// (triangle inequality, so admissible, and consistent when s = 1).  The
+// table holds q = floor(d / s); d(a) - d(b) >= s (q_a - q_b) - (s - 1),
+// which is the exact difference when s = 1.  The engines need
+// admissibility only: a node reached again with a smaller g is re-expanded.  A landmark that reaches v but not t, or is
 // reached from t but not from v, proves that v cannot reach t.
 struct HeurALT {
     const uint2 *tab;  // DevGraph::lm: rows of 2L entries

@@ -62,8 +62,9 @@ enum ddp_heuristic_kind {
                             not reached get (last level + 1) x min weight,
                             which stays admissible and consistent            */
     DDP_H_LANDMARK = 6   /* ALT: max over landmarks L of d(L,t) - d(L,v) and
-                            d(v,L) - d(t,L) (triangle inequality: admissible
-                            and consistent); needs ddp_landmarks_build.  No
+                            d(v,L) - d(t,L) (triangle inequality: admissible;
+                            consistent while the table is unscaled); needs
+                            ddp_landmarks_build.  No
                             reference counterpart (the reference only has
                             bfs_hx.cu hop counts, which carry little on random
                             graphs)                                           */
