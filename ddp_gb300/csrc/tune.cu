@@ -5,7 +5,7 @@
 // No reference counterpart (the reference hard-codes K per run and has no
 // batched form).  Search: the (group, block) grid first, since it decides
 // how many queries run at once and dominates throughput; then delta around
-// the automatic choice; then K for multi-CTA slots (one-CTA slots run the
+// the automatic choice, walking on in the direction that wins; then K for multi-CTA slots (one-CTA slots run the
 // asynchronous engine, which has no K).  Every trial must return the same
 // costs as the first one: a mismatch is reported as an error, never tuned
 // around.
@@ -81,15 +81,30 @@ int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *source
         int rc = run(o);
         if (rc) return rc;
     }
-    // 2. bucket width around the automatic one
+    // 2. bucket width: half and twice the automatic one, then further steps
+    //    of 2/3 (or 3/2) while the winning direction keeps winning
     const uint32_t d0 = auto_delta(g);
     const ddp_opts shape = top_o;
+    uint32_t best_d = d0;
     for (uint32_t dv : {d0 / 2, d0 * 2}) {
         if (dv < 1 || dv == d0) continue;
         ddp_opts o = shape;
         o.delta = (int32_t)dv;
+        const double before = top;
         int rc = run(o);
         if (rc) return rc;
+        if (top > before) best_d = dv;
+    }
+    for (int step = 0; step < 3 && best_d != d0; step++) {
+        const uint32_t nd = best_d < d0 ? best_d * 2 / 3 : best_d * 3 / 2;
+        if (nd < 1 || nd == best_d) break;
+        ddp_opts o = shape;
+        o.delta = (int32_t)nd;
+        const double before = top;
+        int rc = run(o);
+        if (rc) return rc;
+        if (top <= before) break;
+        best_d = nd;
     }
     // 3. expansion cap per iteration (phase-synchronous groups only)
     if (top_o.group > 1) {

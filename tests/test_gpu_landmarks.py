@@ -175,3 +175,24 @@ def test_landmark_scaled_table_admissible(gpu, oracle, bits):
     want = np.array([_oracle(oracle, g, int(s), int(t)) for s, t in zip(S, T)])
     cost, _ = d.BatchEngine(dg, d.H_LANDMARK, group=1).solve(S, T)
     assert np.array_equal(cost, want)
+
+
+@pytest.mark.parametrize("n", [4003, 4002, 4001])
+def test_slot_reuse_after_reset(gpu, oracle, n):
+    """Few slots, many queries: every slot runs ~16 searches back to back, so
+    each search starts from the reset of the previous one.  n % 4 != 0 puts
+    the slots' state arrays off 32-byte boundaries, where the reset writes
+    single words at the array ends and whole sectors inside."""
+    d = gpu
+    g = d.gen_random_chain(n, 5, 1, 60, 75)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.build_landmarks(16, seed=2, bits=8)
+    rng = np.random.default_rng(n)
+    S = rng.integers(0, g.n, 64).astype(np.int32)
+    T = rng.integers(0, g.n, 64).astype(np.int32)
+    want = np.array([_oracle(oracle, g, int(s), int(t)) for s, t in zip(S, T)])
+    be = d.BatchEngine(dg, d.H_LANDMARK, group=1, grid=4)
+    for _ in range(2):
+        cost, _ = be.solve(S, T)
+        assert np.array_equal(cost, want)
+    be.close()
