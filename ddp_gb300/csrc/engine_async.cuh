@@ -48,10 +48,14 @@ __device__ __forceinline__ int ring_reserve(CtaQ *sq, int k, int cap) {
     }
 }
 
-template <class Heur>
+// LATENCY picks the relaxation form: one atomic per arc (single queries and
+// cheap heuristics) or a load, then h and a CAS on improving arcs only
+// (table heuristics in batches).
+template <class Heur, bool LATENCY>
 __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, const Heur &H, const SearchParams &P,
-                                       WarpRows *wrows, CtaQ *sq, bool latency) {
+                                       WarpRows *wrows, CtaQ *sq) {
     constexpr bool cheap = heur_cheap<Heur>::value;
+    constexpr bool latency = LATENCY;
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
@@ -202,11 +206,17 @@ __device__ SearchResult run_search_cta(const DevGraph &G, const SlotBufs &B, con
                 __syncwarp();
                 n_scan += (lane == 0) ? (unsigned long long)total : 0ull;
                 // AA arcs per lane per step; each stage issues all of its
-                // loads / atomics before consuming any result
-#ifndef DDP_ASYNC_ARCS
-#define DDP_ASYNC_ARCS 2
+                // loads / atomics before consuming any result.  Two in
+                // latency mode; one in throughput mode, whose heuristic row
+                // loads already fill the warp's memory pipeline (landmark
+                // batches: 17.1k -> 19.0k q/s)
+#ifndef DDP_ASYNC_ARCS_LATENCY
+#define DDP_ASYNC_ARCS_LATENCY 2
 #endif
-                constexpr int AA = DDP_ASYNC_ARCS;
+#ifndef DDP_ASYNC_ARCS_THROUGHPUT
+#define DDP_ASYNC_ARCS_THROUGHPUT 1
+#endif
+                constexpr int AA = latency ? DDP_ASYNC_ARCS_LATENCY : DDP_ASYNC_ARCS_THROUGHPUT;
                 for (int kb = 0; kb < total; kb += 32 * AA) {
                     int v[AA], o[AA];
                     uint32_t ng[AA], hv[AA];

@@ -179,7 +179,7 @@ __device__ SearchResult slot_search(const Grp &grp, const DevGraph &G, const Slo
                                     const SearchParams &P, WarpRows *wrows, CtaQ *sq, bool async) {
     // throughput (many slots): load + CAS on improving arcs only, unless
     // the heuristic is cheap enough that one atomic per arc wins
-    if (async) return run_search_cta(G, B, H, P, wrows, sq, heur_cheap<Heur>::value);
+    if (async) return run_search_cta<Heur, heur_cheap<Heur>::value>(G, B, H, P, wrows, sq);
     return run_search(grp, G, B, H, P, wrows);
 }
 
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(512, 2)
     __shared__ WarpRows wrows[MAX_WARPS];
     __shared__ CtaQ sq;
     SlotBufs B = slot_of(sa, 0);
-    SearchResult r = run_search_cta(G, B, H, P, wrows, &sq, true);  // one query: latency first
+    SearchResult r = run_search_cta<Heur, true>(G, B, H, P, wrows, &sq);  // one query: latency first
     if (threadIdx.x == 0) {
         out[0] = r.cost >= INF_G ? DDP_INF : (int32_t)r.cost;
         out[1] = (B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) ? 0 : write_path(B, P.s, P.t, path, path_cap, G.n, &B.ctl->status);
