@@ -152,60 +152,76 @@ struct HeurManhattan {
 // which is the exact difference when s = 1.  The engines need
 // admissibility only: a node reached again with a smaller g is re-expanded.  A landmark that reaches v but not t, or is
 // reached from t but not from v, proves that v cannot reach t.
+// unroll factor of the landmark row loops (row loads issued ahead of use)
+#ifndef DDP_ALT_UNROLL
+#define DDP_ALT_UNROLL 8
+#endif
+constexpr int ALT_UNROLL = DDP_ALT_UNROLL;
 struct HeurALT {
     const uint2 *tab;  // DevGraph::lm: rows of 2L entries
     int32_t L;         // landmarks, a multiple of 4 (16-bit) or 8 (8-bit)
     int32_t s;         // DevGraph::lm_scale
     int32_t t;
     int32_t bits;      // DevGraph::lm_bits: 16 or 8
+    // One packed word of B-bit entries, a from the row that must be larger:
+    // the lanes' a - b, saturated at 0 and zeroed where either side is the
+    // unreachable marker, fold into the lane-wise maximum m; lanes where a
+    // is the marker and b is not (the landmark relates v and t one way
+    // only, so v cannot reach t) fold into the cut mask cm.  Since s >= 1,
+    // the maximum over terms of s (a - b) - (s - 1), floored at 0, is
+    // s max(a - b) - (s - 1) when that maximum is positive, else 0.
     template <int B>
-    __device__ __forceinline__ void term(uint32_t a, uint32_t b, int32_t &h, bool &cut) const {
-        // a - b with a from the row that must be larger
-        constexpr uint32_t UNR = (1u << B) - 1u;
-        if (a != UNR && b != UNR) h = max(h, ((int32_t)a - (int32_t)b) * s - (s - 1));
-        else if (a == UNR && b != UNR) cut = true;
+    __device__ __forceinline__ void word(uint32_t a, uint32_t b, uint32_t &m, uint32_t &cm) const {
+        if (B == 8) {
+            const uint32_t ea = __vcmpeq4(a, 0xFFFFFFFFu), eb = __vcmpeq4(b, 0xFFFFFFFFu);
+            cm |= ea & ~eb;
+            m = __vmaxu4(m, __vsubus4(a, b) & ~(ea | eb));
+        } else {
+            const uint32_t ea = __vcmpeq2(a, 0xFFFFFFFFu), eb = __vcmpeq2(b, 0xFFFFFFFFu);
+            cm |= ea & ~eb;
+            m = __vmaxu2(m, __vsubus2(a, b) & ~(ea | eb));
+        }
     }
     template <int B>
-    __device__ __forceinline__ void word(uint32_t a, uint32_t b, int32_t &h, bool &cut) const {
-        constexpr uint32_t M = (1u << B) - 1u;
-#pragma unroll
-        for (int k = 0; k < 32; k += B) term<B>((a >> k) & M, (b >> k) & M, h, cut);
-    }
-    template <int B>
-    __device__ __forceinline__ void terms(uint2 a, uint2 b, int32_t &h, bool &cut) const {
-        word<B>(a.x, b.x, h, cut);
-        word<B>(a.y, b.y, h, cut);
+    __device__ __forceinline__ void terms(uint2 a, uint2 b, uint32_t &m, uint32_t &cm) const {
+        word<B>(a.x, b.x, m, cm);
+        word<B>(a.y, b.y, m, cm);
     }
     template <int B>
     __device__ __forceinline__ uint32_t eval(int32_t v) const {
         const int W = L / (64 / B);  // 8-byte words per half row
         const uint2 *rv = tab + (size_t)v * (2 * W);
         const uint2 *rt = tab + (size_t)t * (2 * W);
-        int32_t h = 0;
-        bool cut = false;
+        uint32_t m = 0, cm = 0;
         if ((W & 1) == 0) {
             // both halves start on a 16-byte boundary: 16-byte loads
             const uint4 *qv = reinterpret_cast<const uint4 *>(rv), *qt = reinterpret_cast<const uint4 *>(rt);
             const int W2 = W >> 1;
+#pragma unroll ALT_UNROLL
             for (int i = 0; i < W2; i++) {
                 const uint4 fv = __ldg(qv + i), ft = __ldg(qt + i);
-                terms<B>(make_uint2(ft.x, ft.y), make_uint2(fv.x, fv.y), h, cut);
-                terms<B>(make_uint2(ft.z, ft.w), make_uint2(fv.z, fv.w), h, cut);
+                terms<B>(make_uint2(ft.x, ft.y), make_uint2(fv.x, fv.y), m, cm);
+                terms<B>(make_uint2(ft.z, ft.w), make_uint2(fv.z, fv.w), m, cm);
             }
+#pragma unroll ALT_UNROLL
             for (int i = W2; i < 2 * W2; i++) {
                 const uint4 bv = __ldg(qv + i), bt = __ldg(qt + i);
-                terms<B>(make_uint2(bv.x, bv.y), make_uint2(bt.x, bt.y), h, cut);
-                terms<B>(make_uint2(bv.z, bv.w), make_uint2(bt.z, bt.w), h, cut);
+                terms<B>(make_uint2(bv.x, bv.y), make_uint2(bt.x, bt.y), m, cm);
+                terms<B>(make_uint2(bv.z, bv.w), make_uint2(bt.z, bt.w), m, cm);
             }
         } else {
             for (int i = 0; i < W; i++) {
                 const uint2 fv = __ldg(rv + i), ft = __ldg(rt + i);
                 const uint2 bv = __ldg(rv + W + i), bt = __ldg(rt + W + i);
-                terms<B>(ft, fv, h, cut);
-                terms<B>(bv, bt, h, cut);
+                terms<B>(ft, fv, m, cm);
+                terms<B>(bv, bt, m, cm);
             }
         }
-        return cut ? INF_G : (uint32_t)h;
+        if (cm) return INF_G;
+        const uint32_t mx = B == 8 ? max(max(m & 0xFFu, (m >> 8) & 0xFFu), max((m >> 16) & 0xFFu, m >> 24))
+                                   : max(m & 0xFFFFu, m >> 16);
+        // mx s <= q s <= the largest table distance, below INF_G
+        return mx ? mx * (uint32_t)s - (uint32_t)(s - 1) : 0u;
     }
     __device__ uint32_t operator()(int32_t v) const { return bits == 8 ? eval<8>(v) : eval<16>(v); }
 };
