@@ -147,14 +147,15 @@ def test_serving_through_relayouts(gpu, oracle):
     srv.close()
 
 
-def test_serving_with_landmarks_on_a_fixed_graph(gpu, oracle):
+@pytest.mark.parametrize("count,bits", [(8, 16), (16, 8)])
+def test_serving_with_landmarks_on_a_fixed_graph(gpu, oracle, count, bits):
     """Landmark serving (the 4M-node batch heuristic in continuous
-    batching): exact answers; updates are refused, since they would void
-    the landmark bounds."""
+    batching), 16- and 8-bit tables: exact answers; updates are refused,
+    since they would void the landmark bounds."""
     d = gpu
     g = d.gen_random_chain(20000, 6, 1, 100, 57)
     dg = d.DeviceGraph.from_csr(g)
-    dg.build_landmarks(8, seed=1)
+    dg.build_landmarks(count, seed=1, bits=bits)
     srv = d.Server(dg, d.H_LANDMARK, max_requests=4096, grid=32)
     rng = np.random.default_rng(2)
     S = rng.integers(0, g.n, 100).astype(np.int32)
