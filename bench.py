@@ -15,9 +15,15 @@ all pairs through the persistent batch kernel.
 Prints one JSON line (rank 0).  `value` = queries/sec with inputs resident in
 HBM, timed with CUDA events on the launching stream; `e2e` = the same metric
 through the C-ABI call with host buffers (H2D + D2H inside the timed region).
-N > 1 (torchrun) runs independent replicas, each on its own pairs (weak
-scaling, no data-path collective).  `--impl reference` times the reference's
-serial CPU A* (the oracle restatement) on the host cores instead.
+After the timed batches: every cost against the oracle's fixture for the same
+inputs (`exact_vs_oracle_all`), plain single-query GA* on 256 of the pairs,
+and a serving leg (`serving`): Poisson arrivals at several offered rates
+through the continuous-batching server, p50/p99 from submission to
+completion.  N > 1 (torchrun) runs independent replicas, each on its own
+pairs (weak scaling, no data-path collective).  `--impl reference` times the
+reference's serial CPU A* (the oracle restatement) on the host cores
+instead, over the same pairs, with graph and pairs from the oracle's own
+generators (no product library loaded).
 """
 from __future__ import annotations
 
@@ -93,7 +99,10 @@ def args_parse():
                         "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
                         "get last level + 1); bfs: full reverse BFS; zero: h = 0")
     p.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
-    p.add_argument("--plain-sample", type=int, default=16, help="queries timed on plain single-query GA*")
+    p.add_argument("--plain-sample", type=int, default=256, help="queries timed on plain single-query GA*")
+    p.add_argument("--serve-rates", default="5000,10000,20000",
+                   help="offered Poisson rates (requests/s) of the serving leg ('' = skip)")
+    p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per serving rate")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -158,26 +167,89 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch(config_name, pairs, heuristic="capped", table=None):
-    """dram bytes of one k_batch launch from the committed ncu summary
-    (profiles/k_batch_<config>[_<heuristic>].md, line
-    `traffic_bytes_per_query: X`), scaled to this launch's query count.  A
-    summary with a `traffic_table: L x B-bit` line covers that landmark
-    table only (None for another)."""
-    suffix = "" if heuristic == "capped" else f"_{heuristic}"
-    p = os.path.join(ROOT, "profiles", f"k_batch_{config_name}{suffix}.md")
-    per_query, covers = None, None
-    try:
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_query:"):
-                per_query = float(line.split(":")[1])
-            elif line.startswith("traffic_table:"):
-                covers = line.split(":", 1)[1].strip()
-    except OSError:
+# DRAM bytes per query of k_batch (dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture, divided by the launch's query count), keyed by
+# (workload, heuristic, table).  Each figure comes from the capture named
+# beside it (profiles/ holds its summary and command); None where no capture
+# covers the kernel as built.
+TRAFFIC_PER_QUERY = {
+    # profiles/k_batch_c4_landmark.md: full-size one-pass capture, 4,096 pairs
+    ("c4", "landmark", 64, 8): 143.77e6,
+}
+
+
+def traffic_per_launch(config_name, pairs, heuristic, landmarks, bits):
+    """Measured DRAM bytes of one k_batch launch: the per-query figure of
+    TRAFFIC_PER_QUERY scaled to this launch's query count, or None."""
+    per_query = TRAFFIC_PER_QUERY.get((config_name.replace("-small", ""), heuristic, landmarks or 0,
+                                       bits if landmarks else 0))
+    return None if per_query is None else per_query * pairs
+
+
+FIXTURES = os.path.join(ROOT, "tests", "golden")
+
+
+def _digest(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for x in arrays:
+        h.update(np.ascontiguousarray(x).tobytes())
+    return h.hexdigest()
+
+
+def check_fixture(c, pairs, rank, g, S, T, costs):
+    """All costs against the oracle's (tests/golden/c4_costs.npz, made on
+    the CPU by tests/golden/make_fixtures.py), when the digests say the
+    fixture covers exactly these inputs.  Returns a summary dict or None."""
+    p = os.path.join(FIXTURES, "c4_costs.npz")
+    if not os.path.exists(p) or rank != 0:
         return None
-    if per_query is None or (covers is not None and covers != table):
-        return None
-    return per_query * pairs
+    z = np.load(p)
+    if len(z["costs"]) != pairs or str(z["graph_digest"]) != _digest(g.off, g.col, g.w) \
+            or str(z["pairs_digest"]) != _digest(S, T):
+        return {"exact": None, "note": "fixture does not cover these inputs"}
+    want = z["costs"]
+    bad = np.flatnonzero(costs != want)
+    return {"exact": bool(bad.size == 0), "checked": int(pairs), "mismatches": int(bad.size),
+            "first_mismatch": int(bad[0]) if bad.size else None,
+            "source": "tests/golden/c4_costs.npz (oracle A*, every pair, CPU)"}
+
+
+def serve_leg(d, dg, hkind, S, T, costs, fixture, a):
+    """Continuous batching on the measured graph: Poisson arrivals at each
+    offered rate, endpoints drawn from the measured pairs, so that each
+    answer has a known cost (the oracle's where the fixture covers the
+    pairs, else the batch run's)."""
+    rates = [float(x) for x in a.serve_rates.split(",") if x.strip()]
+    srv = d.Server(dg, hkind, max_requests=1 << 22, grid=a.slots, block=a.block)
+    rng = np.random.default_rng(99173)
+    pick = {}
+
+    def endpoints(k):
+        idx = rng.integers(0, len(S), k)
+        pick["idx"] = idx
+        return S[idx], T[idx]
+
+    srv.submit(S[:64], T[:64])  # warm-up
+    srv.drain()
+    rows, served, wrong = [], 0, 0
+    for rate in rates:
+        row, _, _, ids, got, first = poisson_run(srv, rate, a.serve_seconds, rng, endpoints)
+        mine = (ids >= first) & (ids < first + len(pick["idx"]))  # this rate's requests
+        ids, got = ids[mine], got[mine]
+        idx = pick["idx"][ids - first]
+        bad = int((got != costs[idx]).sum())
+        row["exact"] = bad == 0
+        served += len(ids)
+        wrong += bad
+        rows.append(row)
+    st = srv.stats()
+    srv.close()
+    oracle_backed = bool(fixture and fixture.get("exact"))
+    return {"rates": rows, "slots": st["slots"], "launches": st["launches"], "reruns": st["reruns"],
+            "answers_checked": served, "answers_wrong": wrong,
+            "checked_against": "oracle costs of the pairs (fixture)" if oracle_backed else "the batch run's costs",
+            "latency": "submission to completion, per request"}
 
 
 def algorithmic_bytes(st, landmarks=0, bits=16):
@@ -212,16 +284,31 @@ def max_over_ranks(x, world, dev):
     return float(t.item())
 
 
+def shared_config(c, pairs, world, n, e):
+    """The workload half of `config`, identical in both arms."""
+    return {"workload": workload_name(c), "n": n, "e": e, "pairs_per_gpu": pairs,
+            "graph_seed": c["gseed"], "pair_seed": c["pseed"],
+            "l2": "inputs larger than L2 (graph ~%d MB + per-query state)" % ((e * 16 + n * 8) >> 20),
+            "parallelism": f"replicas x{world} (queries sharded, no collective)"}
+
+
 def run_reference(a, c, world, rank):
-    """The reference's CPU A* (oracle restatement of GA_star/A_star_cpu.cpp)
-    on all host cores: each step = one bounded sample of the workload."""
+    """The reference's CPU A* (GA_star/A_star_cpu.cpp restated in the
+    oracle, its reverse-BFS heuristic of GA_star/bfs_hx.cu) on all host
+    cores, over the same pairs as the GPU arm.  Graph and pairs come from the
+    oracle's own generators (byte-identical to the product's, a tested
+    equality), so this arm loads no product library.  Each step is a bounded
+    sample: one query per host thread, taken in order from the pair list."""
     if rank != 0:
         return
     from oracle import oracle as O
     pairs = a.pairs or c["pairs"]
-    g, S, T, _ = make_workload(c, pairs, 0)
+    off, col, w, _ = O.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
+    S, T, _ = O.gen_pairs(c["n"], off, col, pairs, c["hop_lo"], c["hop_hi"], c["pseed"])
+    n, e = c["n"], int(off[-1])
     threads = os.cpu_count() or 1
-    off = g.off[:-1]
+    # reference layout with an isolated sentinel node n: offsets = off (n + 1
+    # entries), so the reference's last-row bound (E - 1) drops no arc
     # heap with the position map: the same pops and result as the reference's
     # linear-scan decrease-key, strictly faster (an upper bound on its speed)
     mode = O.HEAP_POSMAP
@@ -231,7 +318,7 @@ def run_reference(a, c, world, rank):
         idx = [(q + i) % pairs for i in range(per_step)]
         q += per_step
         t0 = time.perf_counter()
-        cost, ss, hs, done = O.astar_many(g.n, off, g.col, g.w, S[idx], T[idx], hkind=1, wmin=c["wmin"],
+        cost, ss, hs, done = O.astar_many(n + 1, off, col, w, S[idx], T[idx], hkind=1, wmin=c["wmin"],
                                           mode=mode, threads=threads, budget_s=1e9)
         dt = time.perf_counter() - t0
         if step >= a.warmup:
@@ -239,17 +326,17 @@ def run_reference(a, c, world, rank):
             done_total += done
     total = sum(times)
     value = done_total / total if total > 0 else 0.0
+    sample = (f"{per_step} of the {pairs} pairs per step (one per host thread, in pair order; "
+              f"{done_total} queries timed): reverse BFS + serial A* per query, position-map "
+              "decrease-key (same pops as the reference's linear scan, faster)")
     out = {
         "impl": "reference",
         "metric": METRIC,
-        "value": value, "unit": "queries/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "value": value, "unit": "queries/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1000 * total / max(1, a.steps), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)",
-        "config": {"workload": workload_name(c), "pairs_per_step": per_step},
-        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} queries per step (one per core), heuristic BFS + serial A* "
-                                   "per query; position-map decrease-key (same pops as the reference's "
-                                   "linear scan, faster)"},
+        "config": shared_config(c, pairs, world, n, e),
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -306,12 +393,20 @@ def bench_single(a, c):
     hh = np.concatenate([np.maximum(h.values, 0), [0]]).astype(np.int32)
     f, oc, _, _, osec = O.astar(gs.n, gs.off[:-1], gs.col, gs.w, hh, s, t, mode=O.HEAP_POSMAP)
     ok, why = O.check_path(g.off, g.col, g.w, r.path, s, t, r.cost)
+    # the maze query's cost made by the oracle on the CPU (tests/golden/c2_cost.npz)
+    fixture_ok = None
+    fp = os.path.join(FIXTURES, "c2_cost.npz")
+    if a.config == "c2" and os.path.exists(fp):
+        z = np.load(fp)
+        if str(z["graph_digest"]) == _digest(g.off, g.col, g.w):
+            fixture_ok = bool(int(z["cost"]) == cost)
     out = {"metric": "single-query GA* latency (exact)", "value": 1000 * best_t, "unit": "ms/query",
            "higher_is_better": False, "n_gpus": 1, "steps": a.steps, "warmup": max(3, a.warmup),
            "dtype": "int32", "data": "synthetic (seeded generators)",
            "config": {"workload": workload, "n": g.n, "e": g.e, "best": bestK,
                       "sweep_ms": {str(k): 1000 * v[0] for k, v in res.items()}},
            "cost": cost, "exact_vs_oracle": bool(f and oc == cost), "path_valid": ok,
+           "exact_vs_fixture": fixture_ok,
            "work": {"expanded": int(r.stats[0]), "scanned": int(r.stats[1]), "phases": int(r.stats[3])},
            "cpu_baseline": {"value": 1000 * osec, "unit": "ms/query", "cores": 1, "kind": "port",
                             "sample": "the same query, search loop only, position-map heap"}}
@@ -356,6 +451,7 @@ def bench_dynamic(a, c):
     t0 = time.perf_counter()
     dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS, grid=a.slots)
     t_init = time.perf_counter() - t0
+    cost0 = dyn.cost()
     nb = c["batches"]
     sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}
     off, col, ww = g.off[:-1].copy(), g.col.copy(), g.w.copy()
@@ -380,6 +476,21 @@ def bench_dynamic(a, c):
             cpu_t.append(osec)
             want = oc if f else d.INF
             exact = exact and cost == want and r.cost == want
+    # the cost before the first batch and after every batch against the
+    # oracle's from-scratch costs (tests/golden/c3_costs.npz, checked by
+    # input digest)
+    fx = None
+    fp = os.path.join(FIXTURES, "c3_costs.npz")
+    if "rows" not in c and os.path.exists(fp):
+        z = np.load(fp)
+        if str(z["graph_digest"]) == _digest(base.off, base.col, base.w) and \
+                str(z["updates_digest"]) == _digest(fl, u, v, w) and len(z["costs"]) == nb + 1:
+            got = np.array([cost0] + costs, np.int64)
+            bad = np.flatnonzero(got != z["costs"])
+            fx = {"exact": bool(bad.size == 0), "checked": int(nb + 1), "mismatches": int(bad.size),
+                  "source": "tests/golden/c3_costs.npz (oracle A* from scratch after every batch, CPU)"}
+        else:
+            fx = {"exact": None, "note": "fixture does not cover these inputs"}
     out = {"metric": "dynamic A* update batch latency (exact)", "value": 1000 * float(np.mean(dyn_t)),
            "unit": "ms/batch", "higher_is_better": False, "n_gpus": 1, "steps": nb, "warmup": 0,
            "dtype": "int32", "data": "synthetic (seeded generators)",
@@ -391,9 +502,55 @@ def bench_dynamic(a, c):
            "cpu_from_scratch_ms_per_batch": {"value": 1000 * float(np.mean(cpu_t)), "cores": 1, "kind": "port",
                                              "sample": f"{len(cpu_t)} sampled batches, search loop only"},
            "exact_on_sampled_batches": exact, "sampled_batches": sorted(sample),
+           "exact_vs_oracle_all": fx["exact"] if fx else None, "oracle_fixture": fx,
            "invalidated_nodes_mean": float(np.mean(inval)), "costs_first_last": [costs[0], costs[-1]]}
     print(json.dumps(out), flush=True)
     dyn.close()
+
+
+def poisson_run(srv, rate, seconds, rng, endpoints, update_fn=None, update_ms=0):
+    """Offers Poisson arrivals at `rate` requests/s for `seconds` to a server
+    (continuous batching), with update_fn() every update_ms when given, and
+    collects every answer.  endpoints(k) -> (S, T) of the next k requests.
+    Returns (row, S, T, ids, costs, first id): p50/p99 are latencies from
+    submission to completion as the server measures them."""
+    nreq = max(1, int(rate * seconds))
+    arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    S, T = endpoints(nreq)
+    lat, ids_all, costs_all, got, i, n_upd = [], [], [], 0, 0, 0
+    first = None
+    t0 = time.perf_counter()
+    next_upd = update_ms / 1000.0
+    last = t0
+    while got < nreq:
+        now = time.perf_counter() - t0
+        j = int(np.searchsorted(arr, now, side="right"))
+        if j > i:
+            f = srv.submit(S[i:j], T[i:j])
+            first = f if first is None else first
+            i = j
+        if update_fn is not None and now >= next_upd and i < nreq:
+            update_fn()
+            n_upd += 1
+            next_upd += update_ms / 1000.0
+        ids, costs, l, v = srv.poll()
+        if len(ids):
+            got += len(ids)
+            lat.append(l)
+            ids_all.append(ids)
+            costs_all.append(costs)
+            last = time.perf_counter()
+        elif j == i and i >= nreq:
+            time.sleep(0.0001)
+        if time.perf_counter() - t0 > 60 * seconds + 60:
+            break
+    lat = np.concatenate(lat) / 1e6 if lat else np.zeros(0)
+    wall = last - t0
+    row = {"offered_qps": rate, "served_qps": got / wall if wall > 0 else 0.0, "requests": nreq,
+           "completed": got, "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "updates": n_upd}
+    ids = np.concatenate(ids_all) if ids_all else np.zeros(0, np.int64)
+    costs = np.concatenate(costs_all) if costs_all else np.zeros(0, np.int32)
+    return row, S, T, ids, costs, first
 
 
 def bench_serving(a, c):
@@ -447,39 +604,11 @@ def bench_serving(a, c):
         update_batch()
     srv.submit(rng.integers(0, g.n, 64).astype(np.int32), rng.integers(0, g.n, 64).astype(np.int32))
     srv.drain()
-    rows = []
-    for rate in c["rates"]:
-        nreq = int(rate * c["seconds"])
-        arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
-        S = rng.integers(0, g.n, nreq).astype(np.int32)
-        T = rng.integers(0, g.n, nreq).astype(np.int32)
-        lat, got, i, n_upd = [], 0, 0, 0
-        t0 = time.perf_counter()
-        next_upd = c.get("update_ms", 0) / 1000.0
-        last = t0
-        while got < nreq:
-            now = time.perf_counter() - t0
-            j = int(np.searchsorted(arr, now, side="right"))
-            if j > i:
-                srv.submit(S[i:j], T[i:j])
-                i = j
-            if not fixed and now >= next_upd and i < nreq:
-                update_batch()
-                n_upd += 1
-                next_upd += c["update_ms"] / 1000.0
-            ids, costs, l, v = srv.poll()
-            if len(ids):
-                got += len(ids)
-                lat.append(l)
-                last = time.perf_counter()
-            elif j == i and i >= nreq:
-                time.sleep(0.0001)
-            if time.perf_counter() - t0 > 60 * c["seconds"] + 60:
-                break
-        lat = np.concatenate(lat) / 1e6 if lat else np.zeros(0)
-        wall = last - t0
-        rows.append({"offered_qps": rate, "served_qps": got / wall if wall > 0 else 0.0, "requests": nreq,
-                     "completed": got, "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "updates": n_upd})
+    def endpoints(k):
+        return rng.integers(0, g.n, k).astype(np.int32), rng.integers(0, g.n, k).astype(np.int32)
+
+    rows = [poisson_run(srv, rate, c["seconds"], rng, endpoints, None if fixed else update_batch,
+                        c.get("update_ms", 0))[0] for rate in c["rates"]]
     # exactness on a sample (against the current graph version: no updates now)
     Sx = rng.integers(0, g.n, 8).astype(np.int32)
     Tx = rng.integers(0, g.n, 8).astype(np.int32)
@@ -611,16 +740,19 @@ def main():
     clocks = ck.summary()
     costs = dcost.cpu().numpy()
     st, t0, t1 = be.stats()
+    be_info = be.info()
     launches = be.launches() * a.steps
     value = world * pairs * a.steps / tmax
     kernel_s = elapsed / a.steps
     alg = float(algorithmic_bytes(st, lm, a.landmark_bits).sum())
     peak, peak_kind = peak_hbm()
     achieved = alg / kernel_s / 1e9
-    traffic = traffic_per_launch(a.config, pairs, a.heuristic,
-                                 f"{lm} x {a.landmark_bits}-bit" if lm else None)
+    traffic = traffic_per_launch(a.config, pairs, a.heuristic, lm, a.landmark_bits)
     lat_service = (t1 - t0) / 1e6
     lat_complete = (t1 - t0.min()) / 1e6
+    # every answer against the oracle's costs for the same inputs (committed
+    # fixture, checked by input digest)
+    fixture = check_fixture(c, pairs, rank, g, S, T, costs)
 
     # end to end through the C-ABI with host buffers (H2D + D2H inside)
     e2e_times = []
@@ -634,31 +766,46 @@ def main():
     e2e_qps = world * pairs * len(e2e_times) / sum(e2e_times)
     exact_vs_batch = bool(np.array_equal(hc, costs))
 
-    # plain single-query GA* looped one query at a time (heuristic + solve)
+    # plain single-query GA* looped one query at a time (heuristic + solve,
+    # one query on the whole GPU), CUDA events on the same stream
     plain = None
     if a.plain_sample > 0:
         ps = min(a.plain_sample, pairs)
         for i in range(2):  # warm the single-query workspace
             h = dg.heuristic(int(T[i]), hkind)
-            dg.solve(int(S[i]), int(T[i]), h)
+            dg.solve(int(S[i]), int(T[i]), h, stream=stream.cuda_stream)
             h.close()
         torch.cuda.synchronize(dev)
-        p0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         pc = []
         for i in range(ps):
             h = dg.heuristic(int(T[i]), hkind)
-            r = dg.solve(int(S[i]), int(T[i]), h)
+            r = dg.solve(int(S[i]), int(T[i]), h, stream=stream.cuda_stream)
             h.close()
             pc.append(r.cost)
-        pt = time.perf_counter() - p0
-        plain = {"qps": ps / pt, "sample": ps, "costs_match_batch": bool(np.array_equal(pc, costs[:ps]))}
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        pt = e0.elapsed_time(e1) / 1000.0
+        plain = {"qps": ps / pt, "sample": ps, "timing": "CUDA events on the launching stream",
+                 "costs_match_batch": bool(np.array_equal(pc, costs[:ps]))}
+    be.close()
+
+    # serving: the same graph and heuristic under continuous batching,
+    # Poisson arrivals drawn from the measured pairs (so every answer has an
+    # oracle cost), p50/p99 from submission to completion
+    serving = None
+    if a.serve_rates and rank == 0:
+        serving = serve_leg(d, dg, hkind, S, T, costs, fixture, a)
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         from oracle import oracle as O
         threads = os.cpu_count() or 1
         k = min(pairs, threads)
-        cst, ss, hs, done = O.astar_many(g.n, g.off[:-1], g.col, g.w, S[:k], T[:k], hkind=1, wmin=c["wmin"],
+        # sentinel node n: the reference's last-row bound (E - 1) drops no arc
+        cst, ss, hs, done = O.astar_many(g.n + 1, g.off, g.col, g.w, S[:k], T[:k], hkind=1, wmin=c["wmin"],
                                          mode=O.HEAP_POSMAP, threads=threads, budget_s=a.cpu_budget)
         ok = cst[:k] >= 0
         if done:
@@ -669,24 +816,26 @@ def main():
                              f"{1000 * ss[ok].mean():.0f} ms, heuristic {1000 * hs[ok].mean():.0f} ms per query",
                    "costs_match_gpu": bool(np.array_equal(cst[ok], costs[:k][ok]))}
 
+    info = be_info
     out = {
         "metric": METRIC,
         "value": value, "unit": "queries/s", "n_gpus": world, "steps": a.steps, "warmup": max(3, a.warmup),
         "ms_per_step": 1000 * tmax / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)",
-        "config": {"workload": workload_name(c), "n": g.n, "e": g.e, "pairs_per_gpu": pairs,
-                   "heuristic": a.heuristic, "landmarks": lm or None,
+        "config": shared_config(c, pairs, world, g.n, g.e),
+        "engine": {"heuristic": a.heuristic, "landmarks": lm or None,
                    "landmark_bits": a.landmark_bits if lm else None,
                    "landmark_build_s": lm_s, "autotuner": tuned,
-                   "slots": be.info()["slots"], "block": be.info()["block"], "K": opts["K"],
-                   "group": be.info()["group"],
-                   "delta": opts["delta"] or "auto",
-                   "l2": "inputs larger than L2 (graph ~%d MB + per-slot state)" % ((g.e * 16 + g.n * 8) >> 20),
-                   "parallelism": f"replicas x{world} (queries sharded, no collective)"},
+                   "slots": info["slots"], "block": info["block"], "K": opts["K"], "group": info["group"],
+                   "queue_cap": info["queue_cap"], "delta": opts["delta"] or "auto"},
+        "exact_vs_oracle_all": fixture["exact"] if fixture else None,
+        "oracle_fixture": fixture,
         "latency_ms": {"p50": float(np.percentile(lat_complete, 50)), "p99": float(np.percentile(lat_complete, 99)),
                        "service_p50": float(np.percentile(lat_service, 50)),
                        "service_p99": float(np.percentile(lat_service, 99)),
-                       "note": "completion time from batch start (all queries submitted at once); service = on-slot time"},
+                       "note": "batch: completion time from batch start (all queries submitted at once); "
+                               "service = on-slot time.  Serving latencies under arrivals: `serving`"},
+        "serving": serving,
         "plain_ga": plain,
         "speedup_vs_plain": (value / world / plain["qps"]) if plain else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -706,7 +855,6 @@ def main():
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
-    be.close()
     dg.close()
     if world > 1:
         torch.distributed.destroy_process_group()

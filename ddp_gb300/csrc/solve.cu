@@ -1117,10 +1117,17 @@ struct ddp_batch {
     int32_t launches = 0;
     int group = 1;  // CTAs per query slot
     bool no_graph = false;
-    // CUDA graph of the last device-pointer solve
+    // CUDA graph of the last device-pointer solve and the kernel arguments
+    // it was captured with: a replay is valid only while a fresh launch
+    // would pass exactly the same arguments (graph arrays, landmark table,
+    // batch buffers, options)
     cudaGraphExec_t gexec = nullptr;
-    const void *gkey[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    int32_t gkey_n = -1;
+    bool gkey_valid = false;
+    DevGraph gkey_G{};
+    BatchArgs gkey_A{};
+    // arrays of the last solve that path reads go back to: the batch's own
+    // after ddp_batch_solve, the caller's after ddp_batch_solve_device
+    const int32_t *last_S = nullptr, *last_T = nullptr, *last_plen = nullptr;
     // paths of queries re-run on the single-query engine
     std::map<int32_t, std::vector<int32_t>> overflow_paths;
 };
@@ -1129,6 +1136,7 @@ namespace ddp {
 
 static int batch_grow(ddp_batch *b, int32_t n) {
     if (n <= b->cap_q_n) return DDP_OK;
+    b->last_n = 0;  // the last solve's paths go with the old buffers
     cudaFree(b->d_S);
     cudaFree(b->d_T);
     cudaFree(b->d_cost);
@@ -1152,9 +1160,12 @@ static int batch_grow(ddp_batch *b, int32_t n) {
     return DDP_OK;
 }
 
-static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, const int32_t *dT,
-                                int32_t *dcost, int32_t *dplen) {
-    BatchArgs A;
+// Kernel arguments of one batch launch.  Returns false when the landmark
+// table the heuristic needs is stale (the graph changed since it was built).
+static bool batch_args(ddp_batch *b, int32_t n, const int32_t *dS, const int32_t *dT, int32_t *dcost,
+                       int32_t *dplen, DevGraph *G, BatchArgs *A0) {
+    BatchArgs &A = *A0;
+    std::memset(&A, 0, sizeof(A));
     A.S = dS;
     A.T = dT;
     A.nq = n;
@@ -1170,26 +1181,14 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     A.status = b->d_status;
     A.delta = b->o.delta > 0 ? (uint32_t)b->o.delta : auto_delta(b->g);
     A.bfs_budget = b->hkind == DDP_H_BFS_CAPPED ? bfs_budget(b->g->n) : 0;
-    A.serve = 0;
-    A.pub = nullptr;
-    A.pause = nullptr;
-    A.idle_limit = 0;
-    A.idle_votes = nullptr;
-    A.closing = nullptr;
-    A.serve_slots = 0;
-    A.svc = nullptr;
-    A.done = nullptr;
-    A.ver = nullptr;
-    A.version = 0;
-    A.vtab = nullptr;
-    A.nver = 0;
-    A.cur_ver = nullptr;
-    A.inflight = nullptr;
     A.K = b->o.K;
     A.group = b->group;
     A.sync_engine = (b->o.flags & DDP_OPT_SYNC) != 0;
-    DevGraph G = graph_view(b->g);
-    if (b->hkind == DDP_H_LANDMARK && !G.lm) return cudaErrorInvalidValue;  // stale table
+    *G = graph_view(b->g);
+    return !(b->hkind == DDP_H_LANDMARK && !G->lm);
+}
+
+static cudaError_t batch_launch_args(ddp_batch *b, DevGraph G, BatchArgs A) {
     cudaError_t e = cudaMemsetAsync(b->d_work, 0, sizeof(int) * 2, b->stream);
     if (e != cudaSuccess) return e;
     // fresh control blocks (barrier counters included) for every launch
@@ -1202,6 +1201,24 @@ static cudaError_t batch_launch(ddp_batch *b, int32_t n, const int32_t *dS, cons
     if (b->group > 1)
         return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
     return cudaLaunchKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
+}
+
+// Field-by-field equality of the by-value kernel arguments (padding bytes
+// are not compared).
+static bool same_view(const DevGraph &x, const DevGraph &y) {
+    return x.n == y.n && x.e == y.e && x.off == y.off && x.arc == y.arc && x.roff == y.roff &&
+           x.rarc == y.rarc && x.xy == y.xy && x.wmin == y.wmin && x.rho_fp == y.rho_fp && x.doff == y.doff &&
+           x.darc == y.darc && x.droff == y.droff && x.drarc == y.drarc && x.oend == y.oend &&
+           x.roend == y.roend && x.lm == y.lm && x.lm_L == y.lm_L && x.lm_scale == y.lm_scale &&
+           x.lm_bits == y.lm_bits;
+}
+
+static bool same_args(const BatchArgs &x, const BatchArgs &y) {
+    return x.S == y.S && x.T == y.T && x.nq == y.nq && x.cost == y.cost && x.plen == y.plen &&
+           x.paths == y.paths && x.path_cap == y.path_cap && x.qstatus == y.qstatus && x.stats == y.stats &&
+           x.tstart == y.tstart && x.tend == y.tend && x.work == y.work && x.status == y.status &&
+           x.delta == y.delta && x.K == y.K && x.bfs_budget == y.bfs_budget && x.group == y.group &&
+           x.sync_engine == y.sync_engine;
 }
 
 }  // namespace ddp
@@ -1271,45 +1288,52 @@ int ddp_batch_solve_device(ddp_batch *b, int32_t n, const int32_t *d_sources,
     int rc = batch_grow(b, n);
     if (rc) return rc;
     if (n == 0) return DDP_OK;
-    const void *key[5] = {d_sources, d_targets, d_cost, d_path_len, nullptr};
-    bool hit = b->gexec && b->gkey_n == n;
-    for (int i = 0; i < 4 && hit; i++) hit = key[i] == b->gkey[i];
-    if (b->no_graph) {
-        // capture was refused once (e.g. a cooperative launch): launch directly
-        cudaError_t e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
-        if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
-        b->overflow_paths.clear();
-        b->last_n = n;
-        b->launches = 1;
-        return DDP_OK;
-    }
-    if (!hit) {
-        if (b->gexec) {
-            cudaGraphExecDestroy(b->gexec);
-            b->gexec = nullptr;
-        }
-        cudaGraph_t graph = nullptr;
-        DDP_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
-        cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
-        if (e == cudaSuccess && e2 == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            (void)cudaGetLastError();
-            b->gexec = nullptr;
-            b->no_graph = true;
-            e = batch_launch(b, n, d_sources, d_targets, d_cost, d_path_len);
-            if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
-            b->overflow_paths.clear();
-            b->last_n = n;
-            b->launches = 1;
-            return DDP_OK;
-        }
-        for (int i = 0; i < 4; i++) b->gkey[i] = key[i];
-        b->gkey_n = n;
-    }
-    DDP_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    // path lengths go to the batch's own array when the caller wants none,
+    // so that ddp_batch_path can still size the paths
+    int32_t *plen = d_path_len ? d_path_len : b->d_plen;
+    DevGraph G;
+    BatchArgs A;
+    if (!batch_args(b, n, d_sources, d_targets, d_cost, plen, &G, &A))
+        return fail(DDP_ERR_INVALID, "landmark table is stale (graph updated since ddp_landmarks_build)");
     b->overflow_paths.clear();
+    b->last_n = 0;  // no paths to read until this launch is queued
+    if (!b->no_graph) {
+        const bool hit = b->gexec && b->gkey_valid && same_view(G, b->gkey_G) && same_args(A, b->gkey_A);
+        if (!hit) {
+            if (b->gexec) {
+                cudaGraphExecDestroy(b->gexec);
+                b->gexec = nullptr;
+            }
+            b->gkey_valid = false;
+            cudaGraph_t graph = nullptr;
+            DDP_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = batch_launch_args(b, G, A);
+            cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+            if (e == cudaSuccess && e2 == cudaSuccess) e = cudaGraphInstantiate(&b->gexec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                // capture was refused (e.g. a cooperative launch): launch
+                // directly from now on
+                (void)cudaGetLastError();
+                if (b->gexec) cudaGraphExecDestroy(b->gexec);
+                b->gexec = nullptr;
+                b->no_graph = true;
+            } else {
+                b->gkey_G = G;
+                b->gkey_A = A;
+                b->gkey_valid = true;
+            }
+        }
+    }
+    if (b->no_graph) {
+        cudaError_t e = batch_launch_args(b, G, A);
+        if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
+    } else {
+        DDP_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+    }
+    b->last_S = d_sources;
+    b->last_T = d_targets;
+    b->last_plen = plen;
     b->last_n = n;
     b->launches = 1;
     return DDP_OK;
@@ -1329,8 +1353,15 @@ int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32
                                  cudaMemcpyHostToDevice, b->stream));
         DDP_CUDA(cudaMemcpyAsync(b->d_T, targets, sizeof(int32_t) * (size_t)n,
                                  cudaMemcpyHostToDevice, b->stream));
-        cudaError_t e = batch_launch(b, n, b->d_S, b->d_T, b->d_cost, b->d_plen);
+        DevGraph G;
+        BatchArgs A;
+        if (!batch_args(b, n, b->d_S, b->d_T, b->d_cost, b->d_plen, &G, &A))
+            return fail(DDP_ERR_INVALID, "landmark table is stale (graph updated since ddp_landmarks_build)");
+        cudaError_t e = batch_launch_args(b, G, A);
         if (e != cudaSuccess) return cuda_fail(e, "k_batch launch");
+        b->last_S = b->d_S;
+        b->last_T = b->d_T;
+        b->last_plen = b->d_plen;
         b->last_n = n;
         b->launches = 1;
         DDP_CUDA(cudaMemcpyAsync(out_cost, b->d_cost, sizeof(int32_t) * (size_t)n,
@@ -1385,15 +1416,15 @@ int ddp_batch_path(ddp_batch *b, int32_t i, int32_t *buf, int32_t cap, int32_t *
     }
     int32_t l = 0;
     DDP_CUDA(cudaStreamSynchronize(b->stream));
-    DDP_CUDA(cudaMemcpy(&l, b->d_plen + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(&l, b->last_plen + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
     *len = l;
     if (l > b->path_cap) {
         // the slot buffer kept only a prefix; recompute the path on the
         // single-query engine
         ddp_heuristic *h = nullptr;
         int32_t s, t;
-        DDP_CUDA(cudaMemcpy(&s, b->d_S + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
-        DDP_CUDA(cudaMemcpy(&t, b->d_T + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        DDP_CUDA(cudaMemcpy(&s, b->last_S + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        DDP_CUDA(cudaMemcpy(&t, b->last_T + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
         int rc = ddp_heuristic_build(b->g, t, b->hkind, nullptr, nullptr, &h);
         if (rc) return rc;
         ddp_query *q = nullptr;

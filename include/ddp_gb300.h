@@ -177,7 +177,13 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
 int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32_t *targets,
                     int32_t *out_cost, int32_t *out_path_len);
 /* Same with device pointers and no host synchronisation (stream-ordered on
- * the batch's stream); d_cost / d_path_len are device arrays of n. */
+ * the batch's stream); d_cost / d_path_len are device arrays of n
+ * (d_path_len may be NULL).  Repeated calls replay a CUDA graph of the
+ * launch while its arguments are unchanged; any change (other arrays, a
+ * rebuilt landmark table, a re-laid-out dynamic graph) captures it again.
+ * Fails with DDP_ERR_INVALID when the landmark table is stale.  Paths of
+ * such a solve are read back from the caller's d_sources / d_targets: keep
+ * them unchanged until ddp_batch_path is done. */
 int ddp_batch_solve_device(ddp_batch *b, int32_t n, const int32_t *d_sources,
                            const int32_t *d_targets, int32_t *d_cost, int32_t *d_path_len);
 /* Waits for the batch stream. */
@@ -282,8 +288,8 @@ int ddp_serve_free(ddp_server *s);
  * (about 8 MiB, held on every GPU that loads the library until exit).
  *   d_rev_offsets: n+1 int32, reverse CSR offsets (row v = arcs into v)
  *   d_rev_sources: int32 sources of those arcs (negative = absent arc)
- *   d_hops: n int32 out, hops from v to target, -1 when target is
- *           unreachable (the Hx.txt convention of GA_star/bfs_hx.cu)
+ *   d_hops: n int32 out, hops from v to target, -1 when v cannot reach
+ *           the target
  * n is limited to DDP_NOALLOC_MAX_NODES; larger graphs are rejected with
  * DDP_ERR_INVALID.  The first call on a device looks up the scratch address
  * (make it before any stream capture).  The call is synchronous on `stream`

@@ -38,7 +38,8 @@ def build() -> str:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "astar_oracle.c")):
+        srcs = [os.path.join(HERE, f) for f in ("astar_oracle.c", "gen_oracle.c")]
+        if not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(f) for f in srcs):
             build()
         L = C.CDLL(LIB)
         L.oracle_astar.restype = C.c_int
@@ -55,6 +56,12 @@ def lib():
         L.oracle_astar_many.argtypes = [C.c_int, C.c_int, i32p, i32p, u32p, i32p, i32p, C.c_int, C.c_int, C.c_int,
                                         i32p, i32p, C.c_int, C.c_int, C.c_double, i32p, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double)]
+        L.oracle_gen_random_chain.restype = C.c_int
+        L.oracle_gen_random_chain.argtypes = [C.c_int32, C.c_int64, C.c_uint32, C.c_uint32, C.c_uint64, i32p, i32p,
+                                              u32p, i32p]
+        L.oracle_gen_pairs.restype = C.c_int
+        L.oracle_gen_pairs.argtypes = [C.c_int32, i32p, i32p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_uint64, C.c_int32, i32p, i32p, i32p]
         _lib = L
     return _lib
 
@@ -220,3 +227,33 @@ def check_path(off_full, col, w, path, s, t, cost, h_t=0):
     if total + h_t != cost:
         return False, f"weight {total}+{h_t} != cost {cost}"
     return True, ""
+
+
+def gen_random_chain(n, avg_deg, wmin, wmax, seed):
+    """Seeded random digraph (Hamiltonian chain + uniform arcs, no
+    self-loops or duplicates, n * avg_deg arcs) from gen_oracle.c.  Returns
+    (off[n+1], col, w, perm)."""
+    e = int(n) * int(avg_deg)
+    off = np.empty(n + 1, np.int32)
+    col = np.empty(e, np.int32)
+    w = np.empty(e, np.uint32)
+    perm = np.empty(n, np.int32)
+    rc = lib().oracle_gen_random_chain(int(n), e, int(wmin), int(wmax), int(seed), _p(off), _p(col),
+                                       _p(w, C.c_uint32), _p(perm))
+    if rc:
+        raise ValueError(f"oracle_gen_random_chain failed ({rc})")
+    return off, col, w, perm
+
+
+def gen_pairs(n, off, col, npairs, hop_lo, hop_hi, seed, bfs_cap_level=6, threads=0):
+    """Seeded (S, T, wanted hops) from gen_oracle.c; off has n+1 entries."""
+    off, col = _i(off), _i(col)
+    S = np.empty(npairs, np.int32)
+    T = np.empty(npairs, np.int32)
+    want = np.empty(npairs, np.int32)
+    threads = threads or min(16, os.cpu_count() or 1)
+    rc = lib().oracle_gen_pairs(int(n), _p(off), _p(col), int(npairs), int(hop_lo), int(hop_hi),
+                                int(bfs_cap_level), int(seed), int(threads), _p(S), _p(T), _p(want))
+    if rc:
+        raise ValueError(f"oracle_gen_pairs failed ({rc})")
+    return S, T, want

@@ -18,17 +18,29 @@ def test_algorithmic_bytes_accounting():
     assert bench.algorithmic_bytes(hops)[0] == 12 * 10 + 16 * 80 + 16 * 60 + 12 * 500 + 8 * 4000
 
 
-def test_traffic_read_from_profile_for_its_table_only():
+def test_traffic_figure_covers_its_table_only():
     import bench
-    per_query = None
-    covers = None
-    for line in open(f"{bench.ROOT}/profiles/k_batch_c4_landmark.md"):
-        if line.startswith("traffic_bytes_per_query:"):
-            per_query = float(line.split(":")[1])
-        elif line.startswith("traffic_table:"):
-            covers = line.split(":", 1)[1].strip()
-    assert per_query and covers
-    assert bench.traffic_per_launch("c4", 4096, "landmark", covers) == per_query * 4096
-    assert bench.traffic_per_launch("c4", 4096, "landmark", "16 x 16-bit") is None
-    assert bench.traffic_per_launch("c4", 100, "capped") > 0  # summary without a table line
-    assert bench.traffic_per_launch("nonexistent", 100, "landmark", covers) is None
+    per_query = bench.TRAFFIC_PER_QUERY[("c4", "landmark", 64, 8)]
+    assert bench.traffic_per_launch("c4", 4096, "landmark", 64, 8) == per_query * 4096
+    assert bench.traffic_per_launch("c4-small", 10, "landmark", 64, 8) == per_query * 10
+    assert bench.traffic_per_launch("c4", 4096, "landmark", 16, 16) is None
+    assert bench.traffic_per_launch("nonexistent", 100, "landmark", 64, 8) is None
+
+
+def test_fixture_check_needs_matching_inputs(tmp_path, monkeypatch):
+    import bench
+    g = type("G", (), {})()
+    g.off = np.arange(5, dtype=np.int32)
+    g.col = np.arange(4, dtype=np.int32)
+    g.w = np.ones(4, np.uint32)
+    S = np.array([0, 1], np.int32)
+    T = np.array([2, 3], np.int32)
+    np.savez(tmp_path / "c4_costs.npz", costs=np.array([5, 7], np.int32),
+             graph_digest=bench._digest(g.off, g.col, g.w), pairs_digest=bench._digest(S, T))
+    monkeypatch.setattr(bench, "FIXTURES", str(tmp_path))
+    ok = bench.check_fixture({}, 2, 0, g, S, T, np.array([5, 7], np.int32))
+    assert ok["exact"] is True and ok["checked"] == 2
+    bad = bench.check_fixture({}, 2, 0, g, S, T, np.array([5, 8], np.int32))
+    assert bad["exact"] is False and bad["first_mismatch"] == 1
+    other = bench.check_fixture({}, 2, 0, g, T, S, np.array([5, 7], np.int32))
+    assert other["exact"] is None

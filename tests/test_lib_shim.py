@@ -11,7 +11,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIBDIR = os.path.join(ROOT, "ddp_gb300")
-REF_MAIN = "/root/reference/LIB/main.cpp"
+# the read-only reference tree, where present (DDP_REFERENCE_TREE overrides)
+REF_MAIN = os.path.join(os.environ.get("DDP_REFERENCE_TREE", "/root/reference"), "LIB", "main.cpp")
 KAT8 = "8 12\n1 2 3 3 4 4 5 5 6 7 7 0\n0 2 3 5 7 9 10 11\n4 1 2 6 3 1 2 5 1 3 1 9\n"
 
 

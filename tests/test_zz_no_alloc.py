@@ -3,8 +3,9 @@
 It exists for callers that cannot let the library call cudaMalloc; it keeps
 its scratch in a fixed array inside the library.  This file is named to be
 collected last.  It checks, through the C-ABI, that two calls in a row give
-the same hop counts as the allocating heuristic build (ddp_heuristic_build
-with DDP_H_BFS_HOPS on a graph whose minimum weight is 1, so h = hops)."""
+the same hop counts as the oracle's reverse BFS and as the allocating
+heuristic build (ddp_heuristic_build with DDP_H_BFS_HOPS on a graph whose
+minimum weight is 1, so h = hops)."""
 import ctypes as C
 
 import numpy as np
@@ -13,7 +14,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_bfs_matches_allocating_build(gpu):
+def test_noalloc_bfs_matches_oracle_and_allocating_build(gpu, oracle):
     torch = pytest.importorskip("torch")
     d = gpu
     L = d.lib()
@@ -31,9 +32,12 @@ def test_noalloc_bfs_matches_allocating_build(gpu):
                                     C.c_void_p(hops.data_ptr()), None)
         assert rc == 0, L.ddp_last_error()
         got = hops.cpu().numpy()
-        want = dg.heuristic(target, d.H_BFS_HOPS, want_values=True).values
+        # the oracle's reverse BFS (hops, -1 = cannot reach the target)
+        want = oracle.bfs_heuristic(g.n, g.off[:-1], g.col, g.w, target, wmin=1)
         bad = np.flatnonzero(got != want)
         assert bad.size == 0, f"{bad.size} mismatches, first {bad[:5]}: {got[bad[:5]]} vs {want[bad[:5]]}"
+        alloc = dg.heuristic(target, d.H_BFS_HOPS, want_values=True).values
+        assert np.array_equal(got, alloc)
         assert got[target] == 0 and got[g.n - 1] == -1
 
 
