@@ -94,10 +94,11 @@ def args_parse():
     p.add_argument("--landmarks", type=int, default=64, help="landmark count for --heuristic landmark")
     p.add_argument("--landmark-bits", type=int, default=8, choices=[16, 8],
                    help="landmark table entry width (rows of 2 x landmarks entries)")
-    p.add_argument("--heuristic", default="landmark", choices=["capped", "bfs", "zero", "landmark"],
+    p.add_argument("--heuristic", default="landmark", choices=["capped", "bfs", "zero", "landmark", "bidir"],
                    help="landmark: ALT bound from --landmarks landmarks (table built once per graph); "
                         "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
-                        "get last level + 1); bfs: full reverse BFS; zero: h = 0")
+                        "get last level + 1); bfs: full reverse BFS; zero: h = 0; bidir: no heuristic, "
+                        "forward and reverse searches meet in the middle")
     p.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
     p.add_argument("--plain-sample", type=int, default=256, help="queries timed on plain single-query GA*")
     p.add_argument("--serve-rates", default="5000,10000,20000",
@@ -259,7 +260,10 @@ def algorithmic_bytes(st, landmarks=0, bits=16):
     push), and for the heuristic BFS 12 B per reached node + 8 B per scanned
     reverse arc.  With L landmarks h is read only for a relaxation that
     improves g: 12 B per scanned arc and 16 + 2 L bits / 8 B per relaxation
-    (the node's row of 2 L distances of `bits` bits), no BFS."""
+    (the node's row of 2 L distances of `bits` bits), no BFS.  The
+    bidirectional search counts the same 12 / 16 / 16 B, the 4 B of h(head)
+    standing for the other direction's g(head), read beside g(head) for the
+    meeting test."""
     st = np.asarray(st, np.float64)
     if landmarks:
         return 12 * st[:, 0] + 12 * st[:, 1] + (16 + 2 * landmarks * bits // 8) * st[:, 2]
@@ -685,7 +689,7 @@ def main():
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     hkind = {"capped": d.H_BFS_CAPPED, "bfs": d.H_BFS_HOPS, "zero": d.H_ZERO,
-             "landmark": d.H_LANDMARK}[a.heuristic]
+             "landmark": d.H_LANDMARK, "bidir": d.H_BIDIR}[a.heuristic]
     lm = a.landmarks if a.heuristic == "landmark" else 0
     lm_s = None
     if lm:
@@ -840,7 +844,8 @@ def main():
         "speedup_vs_plain": (value / world / plain["qps"]) if plain else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": {"landmark": "k_batch<4>", "zero": "k_batch<0>"}.get(a.heuristic, "k_batch<1>"),
+                     "kernel": {"landmark": "k_batch<4>", "zero": "k_batch<0>",
+                                "bidir": "k_batch<5>"}.get(a.heuristic, "k_batch<1>"),
                      "algorithmic_bytes_per_launch": alg,
                      "kernel_ms": 1000 * kernel_s},
         "work_per_query": {"phases_mean": float(st[:, 3].mean()), "expanded_mean": float(st[:, 0].mean()), "arcs_scanned_mean": float(st[:, 1].mean()),

@@ -1,0 +1,459 @@
+// Bidirectional one-CTA search: a forward search from s over the CSR and a
+// reverse search from t over the reverse CSR, run together by one CTA until
+// they meet.  No heuristic and no per-graph table: both searches are keyed
+// by g, so on graphs of small hop diameter two balls of half the radius
+// replace one ball of the full radius (orders of magnitude fewer nodes on
+// random digraphs).
+//
+// Layout: two state words per node, side by side (state[2v] forward
+// (g << 32 | parent), state[2v + 1] reverse (g << 32 | successor)), so one
+// 16-byte load of v's pair gives the label being relaxed and the other
+// side's label for the meeting test.  Entries carry their direction in the
+// top bit of the node id: ring {v | dir << 31, g}, far {v | dir << 31, g,
+// g, 0}.  The touched log holds a node once per direction that reached it
+// (capacity 2n); a reset clears both words.
+//
+// Work distribution is the asynchronous engine's (engine_async.cuh): the
+// current bucket (keys < T) is a pool that warps drain concurrently, chasing
+// their own children first and spilling to the ring; a `pending` count in
+// shared memory ends the bucket.  Between buckets the far pile is split at
+// T + delta.
+//
+// Meeting: relaxing arc (u, v) in direction dir with v's other-side label
+// finite offers mu = g(u) + w + g_other(v), kept with the arc's forward-side
+// tail x (u forward, v reverse) in one 64-bit atomicMin (mu << 32 | x).
+// Labels only decrease, so at the end some arc (x, y) of x's forward row
+// has g_f(x) + w + g_r(y) == mu, and the path is s .. x (forward parents),
+// y .. t (reverse successors).
+//
+// Stop rule (bidirectional Dijkstra): after a bucket is drained, every node
+// with a forward distance below the smallest open forward key a is final
+// and expanded, and likewise below b in reverse.  When a + b >= mu, a
+// shorter s-t path P would hold an arc (x, y) with d_s(x) < a and
+// d_t(y) < b; both ends were expanded with final labels, and whichever
+// expansion read the other's word second saw it final (labels are
+// installed by an atomic that completes before the entry is pushed, and
+// the pair is read from L2), so mu <= len(P): no shorter path exists.  An
+// empty direction (a or b infinite) also ends the search.  Relaxations and
+// far entries with g >= mu are dropped: no path through them is shorter.
+#pragma once
+
+#include "engine_async.cuh"
+
+namespace ddp {
+
+constexpr uint32_t DIR_BIT = 0x80000000u;
+constexpr uint32_t NODE_MASK = 0x7FFFFFFFu;
+
+struct BiQ {
+    int head, tail;     // ring positions of the current bucket
+    int pending;        // entries pushed to the bucket and not yet retired
+    int far_cnt;        // far pushes appended this bucket
+    int alt_cnt;        // split: far entries kept
+    int status;
+    unsigned int minkey[2];  // split: smallest key left open, per direction
+    unsigned long long mu;   // (best s-t length << 32) | forward-side tail of its arc
+};
+
+// Reserves k ring slots (lane 0 only); returns the first position or -1 when
+// the ring would overflow (the caller then sends the entries to far).
+__device__ __forceinline__ int bi_ring_reserve(BiQ *sq, int k, int cap) {
+    for (;;) {
+        const int t = *(volatile int *)&sq->tail;
+        if (t + k > cap) return -1;
+        if (atomicCAS(&sq->tail, t, t + k) == t) return t;
+    }
+}
+
+__device__ __forceinline__ ulonglong2 ld_pair(const unsigned long long *st2, int v) {
+    return __ldcg(reinterpret_cast<const ulonglong2 *>(st2) + v);
+}
+
+// Path s..t from the meeting word; returns its length (0 when no path).
+__device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B, int32_t s, int32_t t,
+                                           unsigned long long mu, int32_t *path, int32_t cap, int *status) {
+    const uint32_t cost = uint32_t(mu >> 32);
+    if (cost >= INF_G) return 0;
+    if (s == t) {
+        if (cap > 0) path[0] = s;
+        return 1;
+    }
+    const int32_t x = int32_t(uint32_t(mu));
+    const uint32_t gx = st_g(__ldcg(B.state + 2 * (size_t)x));
+    int32_t y = -1;
+    const int r1 = row_end(G.off, G.oend, x);
+    for (int k = row_begin(G.off, G.oend, x); k < r1 && y < 0; k++) {
+        const uint2 a = G.oend ? __ldcg(G.arc + k) : __ldg(G.arc + k);
+        if ((int)a.x < 0) continue;
+        const uint32_t gr = st_g(__ldcg(B.state + 2 * (size_t)a.x + 1));
+        if (gr < INF_G && (uint64_t)gx + a.y + gr == cost) y = (int32_t)a.x;
+    }
+    if (y < 0) {
+        atomicOr(status, ST_TIMEOUT);  // no meeting arc: report the query failed
+        return 0;
+    }
+    // lengths of s..x and y..t
+    int32_t lf = 0, lr = 0;
+    for (int32_t c = x; c >= 0 && lf <= G.n; c = st_parent(__ldcg(B.state + 2 * (size_t)c))) {
+        lf++;
+        if (c == s) break;
+    }
+    for (int32_t c = y; c >= 0 && lr <= G.n; c = st_parent(__ldcg(B.state + 2 * (size_t)c + 1))) {
+        lr++;
+        if (c == t) break;
+    }
+    const int32_t len = lf + lr;
+    if (len > cap) atomicOr(status, ST_PATH_TRUNC);
+    int32_t i = lf - 1;
+    for (int32_t c = x; c >= 0 && i >= 0; c = st_parent(__ldcg(B.state + 2 * (size_t)c)), i--)
+        if (i < cap) path[i] = c;
+    i = lf;
+    for (int32_t c = y; c >= 0 && i < len; c = st_parent(__ldcg(B.state + 2 * (size_t)c + 1)), i++)
+        if (i < cap) path[i] = c;
+    return len;
+}
+
+__device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, const SearchParams &P,
+                                      WarpRows *wrows, BiQ *sq) {
+    SearchCtl *ctl = B.ctl;
+    const int lane = lane_id();
+    const int warp = threadIdx.x >> 5;
+    WarpRows &wr = wrows[warp];
+    uint2 *ring = B.q0;
+    unsigned long long *st2 = B.state;
+    const int cap = (int)min(B.cap_q, (int64_t)0x3FFFFFFF);
+    const int64_t cap_t = 2 * (int64_t)G.n;
+
+    if (threadIdx.x == 0) {
+        ctl->iters = 0;
+        ctl->expanded = ctl->scanned = ctl->relaxed = 0;
+        ctl->far_scanned = 0;
+        sq->head = 0;
+        sq->tail = 0;
+        sq->pending = 0;
+        sq->far_cnt = 0;
+        sq->alt_cnt = 0;
+        sq->status = 0;
+        sq->minkey[0] = sq->minkey[1] = 0xFFFFFFFFu;
+        if (P.s == P.t) {
+            sq->mu = (unsigned long long)(uint32_t)P.s;  // length 0
+            ctl->touched = 0;
+        } else {
+            sq->mu = ~0ull;
+            st2[2 * (size_t)P.s] = st_make(0, -1);
+            st2[2 * (size_t)P.t + 1] = st_make(0, -1);
+            B.touched[0] = P.s;
+            B.touched[1] = P.t;
+            ctl->touched = 2;
+            ring[0] = make_uint2((uint32_t)P.s, 0u);
+            ring[1] = make_uint2((uint32_t)P.t | DIR_BIT, 0u);
+            sq->tail = 2;
+            sq->pending = 2;
+        }
+    }
+    __syncthreads();
+    if (P.s == P.t) {
+        SearchResult r0;
+        r0.cost = 0;
+        r0.iters = 0;
+        return r0;
+    }
+
+    uint4 *fcur = B.f0, *falt = B.f1;
+    int64_t nfar = 0;
+    uint32_t T = P.delta;  // the current bucket holds keys < T
+    uint32_t Tsplit = T;
+    bool do_expand = true;
+    unsigned long long n_exp = 0, n_scan = 0, n_rel = 0;
+    int phases = 0;
+    const int64_t max_phases = 4 * (int64_t)G.n + (1 << 22);
+
+    for (;;) {
+        if (do_expand) {
+            int c_f = 0, c_t = 0, c_loc = 0;  // staged far pushes, touches, own children
+            for (;;) {
+                const uint32_t mu = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
+                // 1. take work: own children first, else claim from the ring
+                int n = 0;
+                uint2 en = make_uint2(RING_EMPTY, 0u);
+                if (c_loc > 0) {
+                    n = min(32, c_loc);
+                    if (lane < n) en = wr.sn[c_loc - n + lane];
+                    c_loc -= n;
+                    __syncwarp();
+                } else {
+                    int h0 = 0;
+                    if (lane == 0) {
+                        n = -1;
+                        for (uint32_t spins = 0;; spins++) {
+                            const int h = *(volatile int *)&sq->head, t = *(volatile int *)&sq->tail;
+                            if (h < t) {
+                                const int k = min(32, t - h);
+                                if (atomicCAS(&sq->head, h, h + k) == h) {
+                                    n = k;
+                                    h0 = h;
+                                    break;
+                                }
+                                continue;
+                            }
+                            if (*(volatile int *)&sq->pending == 0) break;  // bucket done
+                            if (spins > SPIN_LIMIT) {
+                                atomicOr(&sq->status, ST_TIMEOUT);
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
+                    }
+                    n = __shfl_sync(FULL, n, 0);
+                    h0 = __shfl_sync(FULL, h0, 0);
+                    if (n < 0) break;
+                    if (lane < n) {
+                        volatile uint2 *slot = reinterpret_cast<volatile uint2 *>(ring + h0 + lane);
+                        uint2 x = make_uint2(slot->x, slot->y);
+                        for (uint32_t spins = 0; x.x == RING_EMPTY; spins++) {
+                            // reserved by a producer that has not written yet
+                            if (spins > SPIN_LIMIT) {
+                                atomicOr(&sq->status, ST_TIMEOUT);
+                                break;
+                            }
+                            __nanosleep(32);
+                            x = make_uint2(slot->x, slot->y);
+                        }
+                        en = x;
+                        slot->x = RING_EMPTY;  // clean for the next bucket
+                    }
+                }
+                // 2. entry stage: live entries below mu expand
+                int rb = 0, deg = 0;
+                uint32_t gu = 0, ud = 0;
+                if (lane < n && en.x != RING_EMPTY) {
+                    ud = en.x;
+                    gu = en.y;
+                    const int u = (int)(ud & NODE_MASK);
+                    const uint32_t dir = ud >> 31;
+                    const uint64_t su = __ldcg(st2 + 2 * (size_t)u + dir);
+                    if (st_g(su) == gu && gu < mu) {
+                        const int r0 = dir ? row_begin(G.roff, G.roend, u) : row_begin(G.off, G.oend, u);
+                        const int r1 = dir ? row_end(G.roff, G.roend, u) : row_end(G.off, G.oend, u);
+                        rb = r0;
+                        deg = r1 - r0;
+                        n_exp++;
+                    }
+                }
+                int total;
+                const int ex = warp_excl_scan(deg, &total);
+                wr.excl[lane] = ex;
+                wr.rb[lane] = rb;
+                wr.bdeg[lane] = deg;
+                wr.drb[lane] = 0;
+                wr.g[lane] = gu;
+                wr.u[lane] = (int)ud;
+                __syncwarp();
+                n_scan += (lane == 0) ? (unsigned long long)total : 0ull;
+                for (int kb = 0; kb < total; kb += 32) {
+                    const int k = kb + lane;
+                    bool live = false, first = false;
+                    int v = 0;
+                    uint32_t ng = 0, dir = 0;
+                    uint32_t uo = 0;
+                    ulonglong2 pr = make_ulonglong2(0ull, 0ull);
+                    if (k < total) {
+                        const int o = row_owner(wr, k);
+                        uo = (uint32_t)wr.u[o];
+                        dir = uo >> 31;
+                        const uint2 a = row_arc(G, wr, o, k, dir == 0);
+                        v = (int)a.x;
+                        const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
+                        live = v >= 0 && ng64 < (uint64_t)min(mu, INF_G);
+                        ng = (uint32_t)ng64;
+                        if (live) pr = ld_pair(st2, v);
+                    }
+                    if (live) {
+                        const uint64_t mine = dir ? pr.y : pr.x;
+                        const uint32_t go = st_g(dir ? pr.x : pr.y);
+                        if (go < INF_G) {
+                            // the two searches meet over this arc
+                            const uint64_t c = (uint64_t)ng + go;
+                            if (c < mu) {
+                                const uint32_t x = dir ? (uint32_t)v : (uo & NODE_MASK);
+                                atomicMin(&sq->mu, (c << 32) | x);
+                            }
+                        }
+                        live = ng < st_g(mine);
+                        if (live) {
+                            const uint64_t nv = st_make(ng, (int32_t)(uo & NODE_MASK));
+                            unsigned long long *w = st2 + 2 * (size_t)v + dir;
+                            uint64_t c0 = mine;
+                            live = false;
+                            for (;;) {
+                                const uint64_t got = atomicCAS(w, c0, nv);
+                                if (got == c0) {
+                                    live = true;
+                                    first = st_g(c0) >= INF_G;
+                                    break;
+                                }
+                                c0 = got;
+                                if (ng >= st_g(c0)) break;
+                            }
+                        }
+                    }
+                    bool to_near = live && ng < T;
+                    bool to_far = live && !to_near;
+                    if (live) n_rel++;
+                    const uint32_t vd = (uint32_t)v | (dir << 31);
+                    // near pushes: counted in `pending` first, then kept as
+                    // this warp's own work, or spilled to the ring when full
+                    const unsigned mn = __ballot_sync(FULL, to_near);
+                    if (mn) {
+                        const int kn = __popc(mn);
+                        const int rank_in = __popc(mn & ((1u << lane) - 1u));
+                        if (lane == 0) atomicAdd(&sq->pending, kn);
+                        __syncwarp();
+                        if (c_loc + kn <= 64) {
+                            if (to_near) wr.sn[c_loc + rank_in] = make_uint2(vd, ng);
+                            c_loc += kn;
+                        } else {
+                            int p0 = 0;
+                            if (lane == 0) p0 = bi_ring_reserve(sq, kn, cap);
+                            p0 = __shfl_sync(FULL, p0, 0);
+                            if (p0 >= 0) {
+                                if (to_near) {
+                                    volatile unsigned long long *slot =
+                                        reinterpret_cast<volatile unsigned long long *>(ring + p0 + rank_in);
+                                    *slot = ((unsigned long long)ng << 32) | vd;
+                                }
+                            } else {
+                                if (lane == 0) atomicSub(&sq->pending, kn);
+                                to_far = to_far || to_near;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                    stage_push(to_far, make_uint4(vd, ng, ng, 0u), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
+                               ctl, 0);
+                    stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
+                }
+                __syncwarp();
+                // 3. retire the chunk (its children are already counted)
+                if (lane == 0 && n > 0) atomicSub(&sq->pending, n);
+                if (*(volatile int *)&sq->status & ST_TIMEOUT) break;
+            }
+            stage_flush(wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
+            stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
+            __syncthreads();
+            phases++;
+            nfar += *(volatile int *)&sq->far_cnt;
+            const int st = *(volatile int *)&sq->status | *(volatile int *)&ctl->status;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                sq->far_cnt = 0;
+                sq->head = 0;
+                sq->tail = 0;
+                sq->pending = 0;
+            }
+            if (st & (ST_OVERFLOW | ST_TIMEOUT)) {
+                if (threadIdx.x == 0) atomicOr(&ctl->status, st & (ST_OVERFLOW | ST_TIMEOUT));
+                break;
+            }
+            if (nfar > B.cap_f) {
+                if (threadIdx.x == 0) atomicOr(&ctl->status, ST_OVERFLOW);
+                break;
+            }
+            Tsplit = sat_add(T, P.delta);
+            __syncthreads();
+        }
+        // ---- split the far pile at Tsplit, and the stop test ---------------
+        {
+            const uint32_t mu = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
+            unsigned int kmin0 = 0xFFFFFFFFu, kmin1 = 0xFFFFFFFFu;
+            int c_n = 0, c_f = 0;
+            if (threadIdx.x == 0) ctl->far_scanned += (unsigned long long)nfar;
+            for (int64_t base = (int64_t)warp * 32; base < nfar; base += (int64_t)(blockDim.x >> 5) * 32) {
+                const int64_t idx = base + lane;
+                bool to_near = false, keep = false;
+                uint4 en = make_uint4(0u, 0u, 0u, 0u);
+                if (idx < nfar) {
+                    en = __ldcg(fcur + idx);
+                    if (en.z < mu) {
+                        if (en.z < Tsplit) to_near = true;
+                        else keep = true;
+                        if (en.x >> 31) kmin1 = min(kmin1, en.z);
+                        else kmin0 = min(kmin0, en.z);
+                    }
+                }
+                stage_push(to_near, make_uint2(en.x, en.y), wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
+                stage_push(keep, en, wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
+            }
+            stage_flush(wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
+            stage_flush(wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                kmin0 = min(kmin0, __shfl_xor_sync(FULL, kmin0, o));
+                kmin1 = min(kmin1, __shfl_xor_sync(FULL, kmin1, o));
+            }
+            if (lane == 0) {
+                if (kmin0 != 0xFFFFFFFFu) atomicMin(&sq->minkey[0], kmin0);
+                if (kmin1 != 0xFFFFFFFFu) atomicMin(&sq->minkey[1], kmin1);
+            }
+            __syncthreads();
+            const int m = min(*(volatile int *)&sq->tail, cap);
+            const int kept = *(volatile int *)&sq->alt_cnt;
+            const unsigned int a = *(volatile unsigned int *)&sq->minkey[0];
+            const unsigned int b = *(volatile unsigned int *)&sq->minkey[1];
+            const uint32_t mu2 = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
+            const int st = *(volatile int *)&ctl->status;
+            phases++;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                sq->alt_cnt = 0;
+                sq->minkey[0] = sq->minkey[1] = 0xFFFFFFFFu;
+                sq->head = 0;
+                sq->pending = m;
+            }
+            uint4 *t2 = fcur;
+            fcur = falt;
+            falt = t2;
+            nfar = kept;
+            if (st & (ST_OVERFLOW | ST_TIMEOUT)) break;
+            if (phases > max_phases) {
+                if (threadIdx.x == 0) atomicOr(&ctl->status, ST_TIMEOUT);
+                break;
+            }
+            // an empty direction, or a + b >= mu: mu is the distance.  The
+            // ring entries just moved hold the direction minima too.
+            if (a == 0xFFFFFFFFu || b == 0xFFFFFFFFu || (uint64_t)a + b >= (uint64_t)mu2) {
+                // the ring may hold moved entries nobody will pop: clear it
+                for (int i = threadIdx.x; i < m; i += blockDim.x) ring[i].x = RING_EMPTY;
+                break;
+            }
+            if (m > 0) {
+                T = Tsplit;
+                do_expand = true;
+            } else {
+                Tsplit = sat_add(min(a, b), P.delta);
+                do_expand = false;
+            }
+            __syncthreads();
+        }
+    }
+
+    if (lane == 0 && n_scan) atomicAdd(&ctl->scanned, n_scan);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_exp += __shfl_xor_sync(FULL, n_exp, o);
+        n_rel += __shfl_xor_sync(FULL, n_rel, o);
+    }
+    if (lane == 0) {
+        if (n_exp) atomicAdd(&ctl->expanded, n_exp);
+        if (n_rel) atomicAdd(&ctl->relaxed, n_rel);
+    }
+    if (threadIdx.x == 0) ctl->iters = phases;
+    __syncthreads();
+    SearchResult r;
+    const unsigned long long mw = *(volatile unsigned long long *)&sq->mu;
+    r.cost = uint32_t(mw >> 32) >= INF_G ? 0xFFFFFFFFu : uint32_t(mw >> 32);
+    r.iters = phases;
+    return r;
+}
+
+}  // namespace ddp

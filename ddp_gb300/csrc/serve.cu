@@ -464,7 +464,7 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
         return fail(DDP_ERR_INVALID, "bad serving arguments");
     *out = nullptr;
     if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS && hkind != DDP_H_BFS_CAPPED && hkind != DDP_H_MANHATTAN &&
-        hkind != DDP_H_EUCLID && hkind != DDP_H_LANDMARK)
+        hkind != DDP_H_EUCLID && hkind != DDP_H_LANDMARK && hkind != DDP_H_BIDIR)
         return fail(DDP_ERR_INVALID, "unsupported heuristic kind for serving");
     if (hkind == DDP_H_LANDMARK && !graph_view(g).lm)
         return fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)");
@@ -489,7 +489,8 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
     if (s->o.grid > 0) nslots = std::min(nslots, s->o.grid);
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    const bool hops = hkind == DDP_H_BFS_HOPS || hkind == DDP_H_BFS_CAPPED;
+    const int hops = (hkind == DDP_H_BFS_HOPS || hkind == DDP_H_BFS_CAPPED ? SLOT_HOPS : 0) |
+                     (hkind == DDP_H_BIDIR ? SLOT_PAIR : 0);  // slot layout
     // queue capacities: what each slot's share of half the free memory
     // holds after its state, up to the batch engine's sizes (n + 4096 near,
     // 2n + 4096 far); at least 64k.  A request that still outgrows its slot
@@ -601,7 +602,9 @@ int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int
             // the search outgrew its slot: re-run it on the single-query engine
             // over the master copy, which is the latest version
             ddp_heuristic *h = nullptr;
-            const int hk = s->hkind;
+            // (the bidirectional kind has no single-query form: Dijkstra
+            // order gives the same cost)
+            const int hk = s->hkind == DDP_H_BIDIR ? DDP_H_ZERO : s->hkind;
             int rc = ddp_heuristic_build(s->g, s->h_T[i], hk, nullptr, nullptr, &h);
             if (rc) return rc;
             ddp_query *q = nullptr;

@@ -12,6 +12,9 @@
 
 #include "engine.cuh"
 #include "engine_async.cuh"
+#include "engine_bidir.cuh"
+
+#include <type_traits>
 #include "graph.cuh"
 #include "solve.cuh"
 
@@ -20,34 +23,38 @@ namespace ddp {
 constexpr int MAX_WARPS = 16;  // blocks of at most 512 threads
 
 // ---- slot arrays -------------------------------------------------------------
-size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops) {
+size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind) {
+    const size_t words = (kind & SLOT_PAIR) ? 2 : 1;
     size_t b = 0;
-    b += sizeof(unsigned long long) * (size_t)n;  // state
-    b += sizeof(int32_t) * (size_t)n;             // touched
-    if (hops) b += sizeof(uint32_t) * (size_t)n;
+    b += sizeof(unsigned long long) * (size_t)n * words;  // state
+    b += sizeof(int32_t) * (size_t)n * words;             // touched
+    if (kind & SLOT_HOPS) b += sizeof(uint32_t) * (size_t)n;
     b += 2 * sizeof(uint2) * (size_t)cap_q;
     b += 2 * sizeof(uint4) * (size_t)cap_f;
     b += sizeof(SearchCtl);
     return b;
 }
 
-int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, bool hops,
+int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, int kind,
                 cudaStream_t st) {
     sa = SlotArrays();
+    const bool hops = (kind & SLOT_HOPS) != 0;
+    const size_t words = (kind & SLOT_PAIR) ? 2 : 1;
     sa.n = n;
+    sa.words = (int)words;
     sa.nslots = nslots;
     sa.cap_q = cap_q;
     sa.cap_f = cap_f;
     const size_t S = (size_t)nslots;
-    DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)n * S));
-    DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * S));
+    DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)n * words * S));
+    DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * words * S));
     if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
     DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.f, sizeof(uint4) * (size_t)cap_f * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
     DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
-    DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * S, st));
+    DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * words * S, st));
     if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
     // queue slots start as "empty" (the asynchronous engine's ring marker)
     DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * 2 * S, st));
@@ -69,8 +76,8 @@ void slots_free(SlotArrays &sa) {
 __device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
     SlotBufs b;
     const size_t n = (size_t)sa.n;
-    b.state = sa.state + n * i;
-    b.touched = sa.touched + n * i;
+    b.state = sa.state + n * sa.words * i;
+    b.touched = sa.touched + n * sa.words * i;
     b.hops = sa.hops ? sa.hops + n * i : nullptr;
     b.q0 = sa.q + (size_t)sa.cap_q * 2 * i;
     b.q1 = b.q0 + sa.cap_q;
@@ -185,7 +192,7 @@ __device__ SearchResult slot_search(const Grp &grp, const DevGraph &G, const Slo
 
 template <int HK, class Grp>
 __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B, const BatchArgs &A,
-                           uint32_t *epoch, WarpRows *wrows, CtaQ *sq, bool async) {
+                           uint32_t *epoch, WarpRows *wrows, CtaQ *sq, BiQ *bq, bool async) {
     SearchCtl *ctl = B.ctl;
     long long t0 = 0;
     int vbuf = -1;  // versioned serving: graph buffer the current search holds
@@ -319,10 +326,14 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             r = slot_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows, sq, async);
         } else if (HK == 4) {
             r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, G.lm_scale, t, G.lm_bits}, P, wrows, sq, async);
+        } else if (HK == 5) {
+            // bidirectional: one-CTA slots only (the host never launches
+            // this kind with wider slots)
+            if constexpr (std::is_same<Grp, CtaGroup>::value) r = run_bidir_cta(G, B, P, wrows, bq);
         } else {
             r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
         }
-        if (async && (*(volatile int *)&ctl->status & (ST_OVERFLOW | ST_TIMEOUT))) {
+        if ((async || HK == 5) && (*(volatile int *)&ctl->status & (ST_OVERFLOW | ST_TIMEOUT))) {
             // an aborted asynchronous search may leave ring slots written:
             // clear the ring so the slot's next search starts clean
             for (int64_t i = grp.rank(); i < B.cap_q; i += grp.size()) B.q0[i].x = RING_EMPTY;
@@ -331,10 +342,17 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         if (grp.rank() == 0) {
             const int st = ctl->status;
             int32_t len = 0;
-            if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths)
-                len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
-                                 &ctl->status);
-            A.cost[q] = (st & (ST_OVERFLOW | ST_TIMEOUT)) ? -1
+            if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths) {
+                if (HK == 5)
+                    len = write_path_bidir(G, B, s, t, bq->mu, A.paths + (size_t)q * A.path_cap, A.path_cap,
+                                           &ctl->status);
+                else
+                    len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
+                                     &ctl->status);
+            }
+            // a bidirectional search that found no meeting arc failed
+            const int stf = ctl->status;
+            A.cost[q] = ((st | stf) & (ST_OVERFLOW | ST_TIMEOUT)) ? -1
                         : (r.cost >= INF_G)                ? DDP_INF
                                                            : (int32_t)r.cost;
             if (A.plen) A.plen[q] = len;
@@ -363,7 +381,13 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         }
         grp.sync();
         const int cnt = *(volatile int *)&ctl->touched;
-        for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
+        if (HK == 5) {
+            // both words of each logged node (one 16-byte store)
+            for (int i = grp.rank(); i < cnt; i += grp.size())
+                reinterpret_cast<ulonglong2 *>(B.state)[B.touched[i]] = make_ulonglong2(~0ull, ~0ull);
+        } else {
+            for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
+        }
         grp.sync();
         if (grp.rank() == 0) {
             if (A.tstart) A.tstart[q] = t0;
@@ -500,6 +524,7 @@ template <int HK>
 __global__ void __launch_bounds__(512, 2) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
     __shared__ WarpRows wrows[MAX_WARPS];
     __shared__ CtaQ sq;
+    __shared__ BiQ bq;
     if (A.svc && (int)blockIdx.x == A.serve_slots) {
         service_loop(A);
         return;
@@ -507,12 +532,12 @@ __global__ void __launch_bounds__(512, 2) k_batch(DevGraph G, SlotArrays sa, Bat
     if (A.group <= 1) {
         SlotBufs B = slot_of(sa, blockIdx.x);
         CtaGroup grp{&B.ctl->status};
-        batch_loop<HK>(grp, G, B, A, sa.epoch + blockIdx.x, wrows, &sq, !A.sync_engine);
+        batch_loop<HK>(grp, G, B, A, sa.epoch + blockIdx.x, wrows, &sq, &bq, !A.sync_engine);
     } else {
         const int slot = blockIdx.x / A.group;
         SlotBufs B = slot_of(sa, slot);
         SubGridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status, A.group};
-        batch_loop<HK>(grp, G, B, A, sa.epoch + slot, wrows, &sq, false);
+        batch_loop<HK>(grp, G, B, A, sa.epoch + slot, wrows, &sq, &bq, false);
     }
 }
 
@@ -561,12 +586,23 @@ static cudaError_t coop_launch(K kernel, int grid, int block, void **args, cudaS
 
 static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CAPPED; }
 
+// Slot layout a batch heuristic kind needs.
+static int slot_kind(int hkind) {
+    return (is_bfs_kind(hkind) ? SLOT_HOPS : 0) | (hkind == DDP_H_BIDIR ? SLOT_PAIR : 0);
+}
+
+// Heuristic kind of the single-query engine that re-runs a batch query
+// (the bidirectional form has no single-query counterpart: plain Dijkstra
+// order gives the same cost).
+static int rerun_kind(int hkind) { return hkind == DDP_H_BIDIR ? DDP_H_ZERO : hkind; }
+
 // The batch kernel instance for a heuristic kind.
 static const void *batch_kernel(int hkind) {
     if (is_bfs_kind(hkind)) return (const void *)k_batch<1>;
     if (hkind == DDP_H_MANHATTAN) return (const void *)k_batch<2>;
     if (hkind == DDP_H_EUCLID) return (const void *)k_batch<3>;
     if (hkind == DDP_H_LANDMARK) return (const void *)k_batch<4>;
+    if (hkind == DDP_H_BIDIR) return (const void *)k_batch<5>;
     return (const void *)k_batch<0>;
 }
 
@@ -1229,9 +1265,9 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
     *out = nullptr;
     if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN && hkind != DDP_H_EUCLID &&
-        hkind != DDP_H_LANDMARK)
+        hkind != DDP_H_LANDMARK && hkind != DDP_H_BIDIR)
         return fail(DDP_ERR_INVALID,
-                    "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED, MANHATTAN, EUCLID or LANDMARK");
+                    "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED, MANHATTAN, EUCLID, LANDMARK or BIDIR");
     if (hkind == DDP_H_LANDMARK && !graph_view(g).lm)
         return fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)");
     if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID) && !g->d_xy)
@@ -1252,7 +1288,7 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     // slots: occupancy-limited, then memory-limited (half of free memory)
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(hkind), b->block, 0);
-    b->group = std::max(1, b->o.group);
+    b->group = hkind == DDP_H_BIDIR ? 1 : std::max(1, b->o.group);  // bidirectional slots are one CTA
     const int coresident = std::max(1, per_sm) * sm_count();
     if (b->group > coresident) b->group = coresident;
     int nslots = coresident / b->group;
@@ -1263,10 +1299,10 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     // the far pile holds every open node beyond the current bucket: twice the
     // node count leaves room for stale copies between compactions
     const int64_t cap_f = b->o.queue_cap > 0 ? b->o.queue_cap : 2 * (int64_t)g->n + 4096;
-    const size_t per = slot_bytes(g->n, cap, cap_f, is_bfs_kind(hkind));
+    const size_t per = slot_bytes(g->n, cap, cap_f, slot_kind(hkind));
     const size_t budget = freeb / 2;
     if ((size_t)nslots * per > budget) nslots = (int)std::max<size_t>(1, budget / per);
-    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap_f, is_bfs_kind(hkind), b->stream);
+    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap_f, slot_kind(hkind), b->stream);
     if (rc == DDP_OK) {
         cudaError_t e1 = cudaMalloc(&b->d_work, sizeof(int) * 2);
         if (e1 != cudaSuccess) rc = cuda_fail(e1, "cudaMalloc(work)");
@@ -1381,7 +1417,7 @@ int ddp_batch_solve(ddp_batch *b, int32_t n, const int32_t *sources, const int32
             if (sources[i] < 0 || sources[i] >= b->g->n || targets[i] < 0 || targets[i] >= b->g->n)
                 return fail(DDP_ERR_INVALID, "query endpoint out of range");
             ddp_heuristic *h = nullptr;
-            int rc = ddp_heuristic_build(b->g, targets[i], b->hkind, nullptr, nullptr, &h);
+            int rc = ddp_heuristic_build(b->g, targets[i], rerun_kind(b->hkind), nullptr, nullptr, &h);
             if (rc) return rc;
             ddp_query *q = nullptr;
             ddp_opts so = b->o;
@@ -1425,7 +1461,7 @@ int ddp_batch_path(ddp_batch *b, int32_t i, int32_t *buf, int32_t cap, int32_t *
         int32_t s, t;
         DDP_CUDA(cudaMemcpy(&s, b->last_S + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
         DDP_CUDA(cudaMemcpy(&t, b->last_T + i, sizeof(int32_t), cudaMemcpyDeviceToHost));
-        int rc = ddp_heuristic_build(b->g, t, b->hkind, nullptr, nullptr, &h);
+        int rc = ddp_heuristic_build(b->g, t, rerun_kind(b->hkind), nullptr, nullptr, &h);
         if (rc) return rc;
         ddp_query *q = nullptr;
         ddp_opts so = b->o;

@@ -11,9 +11,10 @@ struct SearchCtl;
 struct SlotArrays {
     int32_t n = 0;
     int nslots = 0;
+    int words = 1;  // state words per node: 1, or 2 (forward and reverse, side by side)
     int64_t cap_q = 0, cap_f = 0;
-    unsigned long long *state = nullptr;  // nslots x n
-    int32_t *touched = nullptr;           // nslots x n
+    unsigned long long *state = nullptr;  // nslots x n x words
+    int32_t *touched = nullptr;           // nslots x n x words
     uint32_t *hops = nullptr;             // nslots x n (per-target heuristic) or null
     uint2 *q = nullptr;                   // nslots x 2 x cap_q
     uint4 *f = nullptr;                   // nslots x 2 x cap_f {node, g, f, 0}
@@ -76,10 +77,12 @@ struct BatchArgs {
     int *inflight;                // per buffer: searches running on it (host memory)
 };
 
-size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, bool hops);
+// Slot kinds (bits): a per-target hop array; paired forward/reverse state.
+enum { SLOT_HOPS = 1, SLOT_PAIR = 2 };
+size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind);
 // Runs maintenance subs with ordinary launches on st (no serving kernel runs).
 cudaError_t svc_run_direct(const SvcSub *subs, int nsub, cudaStream_t st);
-int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, bool hops,
+int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, int kind,
                 cudaStream_t st);
 void slots_free(SlotArrays &sa);
 uint32_t *heuristic_hops_ptr(const ddp_heuristic *h);

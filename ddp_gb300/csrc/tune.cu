@@ -6,7 +6,7 @@
 // batched form).  Search: the (group, block) grid first, since it decides
 // how many queries run at once and dominates throughput; then delta around
 // the automatic choice, walking on in the direction that wins; then K for multi-CTA slots (one-CTA slots run the
-// asynchronous engine, which has no K).  Every trial must return the same
+// asynchronous engine, which has no K); then the queue capacity per slot.  Every trial must return the same
 // costs as the first one: a mismatch is reported as an error, never tuned
 // around.
 #include <chrono>
@@ -70,9 +70,11 @@ int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *source
         }
         return DDP_OK;
     };
-    // 1. slot shape
+    // 1. slot shape (bidirectional slots are one CTA)
     const int shapes[][2] = {{1, 512}, {1, 256}, {2, 512}, {4, 512}, {8, 512}, {19, 512}};
-    for (const auto &sh : shapes) {
+    const int nshapes = hkind == DDP_H_BIDIR ? 2 : 6;
+    for (int si = 0; si < nshapes; si++) {
+        const auto &sh = shapes[si];
         ddp_opts o = b0;
         o.group = sh[0];
         o.block = sh[1];
@@ -114,6 +116,21 @@ int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *source
             o.K = k;
             int rc = run(o);
             if (rc) return rc;
+        }
+    }
+    // 4. queue capacity per slot: smaller queues leave memory for more
+    //    slots where memory, not occupancy, limits them; a query that
+    //    outgrows its slot is re-run on the single-query engine, so a cap
+    //    that is too small loses on time and is not taken
+    {
+        const ddp_opts capped = top_o;
+        for (int64_t div : {4, 16}) {
+            ddp_opts o = capped;
+            o.queue_cap = (int64_t)g->n / div + 4096;
+            const double before = top;
+            int rc = run(o);
+            if (rc) return rc;
+            if (top <= before) break;
         }
     }
     *best = top_o;

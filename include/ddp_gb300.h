@@ -61,13 +61,18 @@ enum ddp_heuristic_kind {
                             where it has reached max(4096, n/32) nodes; nodes
                             not reached get (last level + 1) x min weight,
                             which stays admissible and consistent            */
-    DDP_H_LANDMARK = 6   /* ALT: max over landmarks L of d(L,t) - d(L,v) and
+    DDP_H_LANDMARK = 6,  /* ALT: max over landmarks L of d(L,t) - d(L,v) and
                             d(v,L) - d(t,L) (triangle inequality: admissible;
                             consistent while the table is unscaled); needs
                             ddp_landmarks_build.  No
                             reference counterpart (the reference only has
                             bfs_hx.cu hop counts, which carry little on random
                             graphs)                                           */
+    DDP_H_BIDIR = 7      /* batch and serving only: no heuristic; a forward
+                            search from s and a reverse search from t meet
+                            in the middle (bidirectional Dijkstra).  No
+                            table, so it stays valid under updates.  No
+                            reference counterpart                             */
 };
 
 typedef struct ddp_graph ddp_graph;         /* device-resident CSR + reverse CSR */
@@ -166,8 +171,9 @@ int ddp_query_free(ddp_query *q);
 /* ---- batched multi-query engine (no reference counterpart: the
  *      reference solves one (s,t) per process, GA_v2.cu:301-305) --------- */
 /* hkind: DDP_H_ZERO, DDP_H_BFS_HOPS / DDP_H_BFS_CAPPED (per target, built
- * inside the batch kernel), DDP_H_MANHATTAN, DDP_H_EUCLID (coordinates) or
- * DDP_H_LANDMARK (ddp_landmarks_build first).  opts: group = CTAs per slot
+ * inside the batch kernel), DDP_H_MANHATTAN, DDP_H_EUCLID (coordinates),
+ * DDP_H_LANDMARK (ddp_landmarks_build first) or DDP_H_BIDIR (one-CTA
+ * slots, twice the per-slot state).  opts: group = CTAs per slot
  * (1 = the asynchronous one-CTA engine), block, K, delta, grid = slot cap;
  * ddp_batch_tune picks them.  A query whose search outgrew
  * its slot's queues reports cost -1 from ddp_batch_solve_device;
