@@ -14,10 +14,10 @@
 // (capacity 2n); a reset clears both words.
 //
 // Work distribution is the asynchronous engine's (engine_async.cuh): the
-// current bucket (keys < T) is a pool that warps drain concurrently, chasing
-// their own children first and spilling to the ring; a `pending` count in
-// shared memory ends the bucket.  Between buckets the far pile is split at
-// T + delta.
+// current bucket (keys below the thresholds) is a pool that warps drain
+// concurrently, chasing their own children first and spilling to the ring;
+// a `pending` count in shared memory ends the bucket.  Between buckets the
+// far pile is split at each advancing direction's threshold + delta.
 //
 // Meeting: relaxing arc (u, v) in direction dir with v's other-side label
 // finite offers mu = g(u) + w + g_other(v), kept with the arc's forward-side
@@ -25,6 +25,13 @@
 // Labels only decrease, so at the end some arc (x, y) of x's forward row
 // has g_f(x) + w + g_r(y) == mu, and the path is s .. x (forward parents),
 // y .. t (reverse successors).
+//
+// Balance: each direction keeps its own threshold T_d, and a split advances
+// direction d only while its open set is at most twice the other's (plus a
+// little), so the search grows the smaller ball, as bidirectional Dijkstra
+// expands the side with the smaller queue.  A query whose source has only
+// heavy out-arcs then advances the forward side alone instead of letting the
+// reverse ball grow far past the meeting radius.
 //
 // Stop rule (bidirectional Dijkstra): after a bucket is drained, every node
 // with a forward distance below the smallest open forward key a is final
@@ -52,6 +59,8 @@ struct BiQ {
     int alt_cnt;        // split: far entries kept
     int status;
     unsigned int minkey[2];  // split: smallest key left open, per direction
+    int open_dir[2];         // far entries per direction (kept by the last split + pushed since)
+    int moved_dir[2];        // split: entries moved to the ring, per direction
     unsigned long long mu;   // (best s-t length << 32) | forward-side tail of its arc
 };
 
@@ -135,6 +144,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
         sq->alt_cnt = 0;
         sq->status = 0;
         sq->minkey[0] = sq->minkey[1] = 0xFFFFFFFFu;
+        sq->open_dir[0] = sq->open_dir[1] = 0;
+        sq->moved_dir[0] = sq->moved_dir[1] = 0;
         if (P.s == P.t) {
             sq->mu = (unsigned long long)(uint32_t)P.s;  // length 0
             ctl->touched = 0;
@@ -161,8 +172,11 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
 
     uint4 *fcur = B.f0, *falt = B.f1;
     int64_t nfar = 0;
-    uint32_t T = P.delta;  // the current bucket holds keys < T
-    uint32_t Tsplit = T;
+    // the current bucket holds keys < T0 (forward) and < T1 (reverse); lo_d
+    // is a lower bound of direction d's open keys when its last advance
+    // moved nothing (the next advance jumps there)
+    uint32_t T0 = P.delta, T1 = P.delta;
+    uint32_t lo0 = 0, lo1 = 0;
     bool do_expand = true;
     unsigned long long n_exp = 0, n_scan = 0, n_rel = 0;
     int phases = 0;
@@ -171,6 +185,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
     for (;;) {
         if (do_expand) {
             int c_f = 0, c_t = 0, c_loc = 0;  // staged far pushes, touches, own children
+            int nf0 = 0, nf1 = 0;             // far pushes per direction (this lane)
             for (;;) {
                 const uint32_t mu = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
                 // 1. take work: own children first, else claim from the ring
@@ -297,7 +312,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                             }
                         }
                     }
-                    bool to_near = live && ng < T;
+                    bool to_near = live && ng < (dir ? T1 : T0);
                     bool to_far = live && !to_near;
                     if (live) n_rel++;
                     const uint32_t vd = (uint32_t)v | (dir << 31);
@@ -329,6 +344,10 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         }
                         __syncwarp();
                     }
+                    if (to_far) {
+                        if (dir) nf1++;
+                        else nf0++;
+                    }
                     stage_push(to_far, make_uint4(vd, ng, ng, 0u), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
                                ctl, 0);
                     stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
@@ -340,6 +359,15 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             }
             stage_flush(wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
             stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                nf0 += __shfl_xor_sync(FULL, nf0, o);
+                nf1 += __shfl_xor_sync(FULL, nf1, o);
+            }
+            if (lane == 0) {
+                if (nf0) atomicAdd(&sq->open_dir[0], nf0);
+                if (nf1) atomicAdd(&sq->open_dir[1], nf1);
+            }
             __syncthreads();
             phases++;
             nfar += *(volatile int *)&sq->far_cnt;
@@ -359,13 +387,19 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 if (threadIdx.x == 0) atomicOr(&ctl->status, ST_OVERFLOW);
                 break;
             }
-            Tsplit = sat_add(T, P.delta);
             __syncthreads();
         }
-        // ---- split the far pile at Tsplit, and the stop test ---------------
+        // ---- split the far pile, and the stop test -------------------------
         {
             const uint32_t mu = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
+            // advance the direction(s) whose open set is not much larger
+            const int o0 = *(volatile int *)&sq->open_dir[0], o1 = *(volatile int *)&sq->open_dir[1];
+            const bool adv0 = (int64_t)o0 <= 2 * (int64_t)o1 + 64;
+            const bool adv1 = (int64_t)o1 <= 2 * (int64_t)o0 + 64;
+            const uint32_t Ts0 = adv0 ? sat_add(max(T0, lo0), P.delta) : T0;
+            const uint32_t Ts1 = adv1 ? sat_add(max(T1, lo1), P.delta) : T1;
             unsigned int kmin0 = 0xFFFFFFFFu, kmin1 = 0xFFFFFFFFu;
+            int kp0 = 0, kp1 = 0, mv0 = 0, mv1 = 0;  // kept / moved per direction (this lane)
             int c_n = 0, c_f = 0;
             if (threadIdx.x == 0) ctl->far_scanned += (unsigned long long)nfar;
             for (int64_t base = (int64_t)warp * 32; base < nfar; base += (int64_t)(blockDim.x >> 5) * 32) {
@@ -375,10 +409,18 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 if (idx < nfar) {
                     en = __ldcg(fcur + idx);
                     if (en.z < mu) {
-                        if (en.z < Tsplit) to_near = true;
+                        const bool rev = (en.x >> 31) != 0;
+                        if (en.z < (rev ? Ts1 : Ts0)) to_near = true;
                         else keep = true;
-                        if (en.x >> 31) kmin1 = min(kmin1, en.z);
-                        else kmin0 = min(kmin0, en.z);
+                        if (rev) {
+                            kmin1 = min(kmin1, en.z);
+                            if (to_near) mv1++;
+                            else kp1++;
+                        } else {
+                            kmin0 = min(kmin0, en.z);
+                            if (to_near) mv0++;
+                            else kp0++;
+                        }
                     }
                 }
                 stage_push(to_near, make_uint2(en.x, en.y), wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
@@ -390,16 +432,28 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             for (int o = 16; o > 0; o >>= 1) {
                 kmin0 = min(kmin0, __shfl_xor_sync(FULL, kmin0, o));
                 kmin1 = min(kmin1, __shfl_xor_sync(FULL, kmin1, o));
+                kp0 += __shfl_xor_sync(FULL, kp0, o);
+                kp1 += __shfl_xor_sync(FULL, kp1, o);
+                mv0 += __shfl_xor_sync(FULL, mv0, o);
+                mv1 += __shfl_xor_sync(FULL, mv1, o);
             }
+            __syncthreads();  // every thread has read open_dir
+            if (threadIdx.x == 0) sq->open_dir[0] = sq->open_dir[1] = 0;
+            __syncthreads();
             if (lane == 0) {
                 if (kmin0 != 0xFFFFFFFFu) atomicMin(&sq->minkey[0], kmin0);
                 if (kmin1 != 0xFFFFFFFFu) atomicMin(&sq->minkey[1], kmin1);
+                if (kp0) atomicAdd(&sq->open_dir[0], kp0);
+                if (kp1) atomicAdd(&sq->open_dir[1], kp1);
+                if (mv0) atomicAdd(&sq->moved_dir[0], mv0);
+                if (mv1) atomicAdd(&sq->moved_dir[1], mv1);
             }
             __syncthreads();
             const int m = min(*(volatile int *)&sq->tail, cap);
             const int kept = *(volatile int *)&sq->alt_cnt;
             const unsigned int a = *(volatile unsigned int *)&sq->minkey[0];
             const unsigned int b = *(volatile unsigned int *)&sq->minkey[1];
+            const int moved0 = *(volatile int *)&sq->moved_dir[0], moved1 = *(volatile int *)&sq->moved_dir[1];
             const uint32_t mu2 = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
             const int st = *(volatile int *)&ctl->status;
             phases++;
@@ -407,6 +461,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             if (threadIdx.x == 0) {
                 sq->alt_cnt = 0;
                 sq->minkey[0] = sq->minkey[1] = 0xFFFFFFFFu;
+                sq->moved_dir[0] = sq->moved_dir[1] = 0;
                 sq->head = 0;
                 sq->pending = m;
             }
@@ -426,13 +481,13 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 for (int i = threadIdx.x; i < m; i += blockDim.x) ring[i].x = RING_EMPTY;
                 break;
             }
-            if (m > 0) {
-                T = Tsplit;
-                do_expand = true;
-            } else {
-                Tsplit = sat_add(min(a, b), P.delta);
-                do_expand = false;
-            }
+            // a direction that advanced without moving anything jumps to its
+            // smallest open key next time
+            lo0 = (adv0 && moved0 == 0) ? a : 0u;
+            lo1 = (adv1 && moved1 == 0) ? b : 0u;
+            T0 = Ts0;
+            T1 = Ts1;
+            do_expand = m > 0;
             __syncthreads();
         }
     }

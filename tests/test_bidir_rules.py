@@ -1,7 +1,8 @@
 """The bidirectional engine's rules, restated sequentially in Python and
-checked against Dijkstra (no GPU): buckets of width delta on g shared by
-both directions, entries popped in random order (standing in for the warps'
-interleaving), the meeting offer g(u) + w + g_other(v) kept with the arc's
+checked against Dijkstra (no GPU): buckets of width delta on g with one
+threshold per direction, advanced only while that direction's open set is
+not much larger than the other's, entries popped in random order (standing
+in for the warps' interleaving), the meeting offer g(u) + w + g_other(v) kept with the arc's
 forward-side tail, relaxations and far entries at or above mu dropped, the
 stop rule (smallest open forward key + smallest open reverse key >= mu, or
 an empty direction), and the path rebuilt from the meeting tail.  This is
@@ -53,9 +54,9 @@ def bidir(n, fw, rv, s, t, delta, rng):
     mu, mux = INF, -1
     near = [(s, 0, 0), (t, 1, 0)]
     far = []
-    T = delta
+    Td = [delta, delta]   # per-direction thresholds of the current bucket
+    lo = [0, 0]           # jump target of a direction whose advance moved nothing
     expand = True
-    Tsplit = T
     while True:
         if expand:
             while near:
@@ -73,28 +74,29 @@ def bidir(n, fw, rv, s, t, delta, rng):
                     if ng < lab[dr][v]:
                         lab[dr][v] = ng
                         par[dr][v] = u
-                        (near if ng < T else far).append((v, dr, ng))
-            Tsplit = T + delta
-        moved, kept, a, b = [], [], INF, INF
+                        (near if ng < Td[dr] else far).append((v, dr, ng))
+        # balance: advance a direction while its open set is not much larger
+        opn = [sum(1 for e in far if e[1] == d) for d in (0, 1)]
+        adv = [opn[0] <= 2 * opn[1] + 64, opn[1] <= 2 * opn[0] + 64]
+        Ts = [max(Td[d], lo[d]) + delta if adv[d] else Td[d] for d in (0, 1)]
+        moved, kept, mins, nmoved = [], [], [INF, INF], [0, 0]
         for (v, dr, g) in far:
             if g >= mu:
                 continue
-            (moved if g < Tsplit else kept).append((v, dr, g))
-            if dr == 0:
-                a = min(a, g)
+            if g < Ts[dr]:
+                moved.append((v, dr, g))
+                nmoved[dr] += 1
             else:
-                b = min(b, g)
+                kept.append((v, dr, g))
+            mins[dr] = min(mins[dr], g)
         far = kept
+        a, b = mins
         if a == INF or b == INF or a + b >= mu:
             break
-        if moved:
-            T = Tsplit
-            near = moved
-            expand = True
-        else:
-            Tsplit = min(a, b) + delta
-            far = kept
-            expand = False
+        lo = [mins[d] if adv[d] and nmoved[d] == 0 else 0 for d in (0, 1)]
+        Td = Ts
+        near = moved
+        expand = bool(moved)
     if mu >= INF:
         return INF, []
     x = mux

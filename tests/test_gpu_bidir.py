@@ -62,7 +62,7 @@ def test_bidir_zero_weights_and_unreachable(gpu, oracle):
     chain-free random graph leaves some pairs disconnected."""
     d = gpu
     rng = np.random.default_rng(5)
-    n, e = 4000, 7000
+    n, e = 4000, 10000
     u = rng.integers(0, n, e)
     v = rng.integers(0, n, e)
     keep = u != v
@@ -77,7 +77,7 @@ def test_bidir_zero_weights_and_unreachable(gpu, oracle):
     dg = d.DeviceGraph.from_csr(g)
     S, T = _pairs(n, 400, 6)
     want = _oracle_costs(oracle, g, S, T)
-    assert (want == INF).any() and (want == 0).sum() > 3
+    assert (want == INF).any() and ((want > 0) & (want < INF)).sum() > 50
     be = d.BatchEngine(dg, d.H_BIDIR, grid=32)
     cost, plen = be.solve(S, T)
     _check(oracle, be, g, S, T, cost, want, plen)
