@@ -86,6 +86,7 @@ def args_parse():
     p.add_argument("--block", type=int, default=0)
     p.add_argument("--delta", type=int, default=0)
     p.add_argument("--K", type=int, default=0)
+    p.add_argument("--queue-cap", type=int, default=0, help="entries per slot queue (0 = automatic)")
     p.add_argument("--group", type=int, default=19, help="CTAs per query slot (with --no-tune)")
     p.add_argument("--no-tune", action="store_true",
                    help="take group/block/delta/K from the flags instead of the autotuner")
@@ -698,7 +699,7 @@ def main():
         l0 = time.perf_counter()
         dg.build_landmarks(lm, seed=c["gseed"], bits=a.landmark_bits)
         lm_s = time.perf_counter() - l0
-    opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group)
+    opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group, queue_cap=a.queue_cap)
     tuned = None
     if not a.no_tune:
         # autotuner on random queries (not the measured pairs), outside the timed region

@@ -541,7 +541,8 @@ def tune_batch(graph: DeviceGraph, hkind: int, S, T, **base) -> tuple:
     n = C.c_int32()
     check(lib().ddp_batch_tune(graph.handle, int(hkind), len(S), ptr(S), ptr(T), C.byref(b), C.byref(o),
                                C.byref(q), C.byref(n)))
-    return dict(K=o.K, delta=o.delta, block=o.block, grid=o.grid, group=o.group), q.value, n.value
+    return (dict(K=o.K, delta=o.delta, block=o.block, grid=o.grid, group=o.group, queue_cap=o.queue_cap), q.value,
+            n.value)
 
 
 def k_paths(graph: DeviceGraph, s: int, t: int, k: int, hkind: int = H_BFS_HOPS, restore: bool = True):

@@ -9,8 +9,9 @@
 // (g << 32 | parent), state[2v + 1] reverse (g << 32 | successor)), so one
 // 16-byte load of v's pair gives the label being relaxed and the other
 // side's label for the meeting test.  Entries carry their direction in the
-// top bit of the node id: ring {v | dir << 31, g}, far {v | dir << 31, g,
-// g, 0}.  The touched log holds a node once per direction that reached it
+// top bit of the node id: ring and far entries are {v | dir << 31, g}
+// (the key is g).  The ring holds one bucket; when it is full, entries stay
+// in the far pile.  The touched log holds a node once per direction that reached it
 // (capacity 2n); a reset clears both words.
 //
 // Work distribution is the asynchronous engine's (engine_async.cuh): the
@@ -72,6 +73,36 @@ __device__ __forceinline__ int bi_ring_reserve(BiQ *sq, int k, int cap) {
         if (t + k > cap) return -1;
         if (atomicCAS(&sq->tail, t, t + k) == t) return t;
     }
+}
+
+// Flushes a warp's staged split entries to the ring; entries past the
+// ring's capacity go to the far pile `falt` instead, where they stay open
+// (the stop rule reads its keys) and move at the next split.
+__device__ __forceinline__ void flush_ring_or_far(uint2 *buf, int &cnt, BiQ *sq, uint2 *ring, int cap, uint2 *falt,
+                                                  int64_t cap_f, SearchCtl *ctl) {
+    if (cnt == 0) return;  // warp-uniform
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    int b = 0;
+    if (lane == 0) b = atomicAdd(&sq->tail, cnt);
+    b = __shfl_sync(FULL, b, 0);
+    const int over = min(cnt, max(0, b + cnt - cap));
+    int fb = 0;
+    if (over > 0 && lane == 0) fb = atomicAdd(&sq->alt_cnt, over);
+    fb = __shfl_sync(FULL, fb, 0);
+    const int first_over = max(b, cap);
+    for (int i = lane; i < cnt; i += 32) {
+        const int pos = b + i;
+        if (pos < cap) {
+            ring[pos] = buf[i];
+        } else {
+            const int64_t p2 = (int64_t)fb + (pos - first_over);
+            if (p2 < cap_f) falt[p2] = buf[i];
+            else raise_err(ctl, 0, ST_OVERFLOW);
+        }
+    }
+    __syncwarp();
+    cnt = 0;
 }
 
 __device__ __forceinline__ ulonglong2 ld_pair(const unsigned long long *st2, int v) {
@@ -170,7 +201,9 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
         return r0;
     }
 
-    uint4 *fcur = B.f0, *falt = B.f1;
+    // far piles hold {v | dir << 31, g}: the key is g
+    uint2 *fcur = reinterpret_cast<uint2 *>(B.f0), *falt = reinterpret_cast<uint2 *>(B.f1);
+    uint2 *sf2 = reinterpret_cast<uint2 *>(wr.sf);  // staged far pushes
     int64_t nfar = 0;
     // the current bucket holds keys < T0 (forward) and < T1 (reverse); lo_d
     // is a lower bound of direction d's open keys when its last advance
@@ -348,7 +381,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         if (dir) nf1++;
                         else nf0++;
                     }
-                    stage_push(to_far, make_uint4(vd, ng, ng, 0u), wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
+                    stage_push(to_far, make_uint2(vd, ng), sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
                                ctl, 0);
                     stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
                 }
@@ -357,7 +390,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 if (lane == 0 && n > 0) atomicSub(&sq->pending, n);
                 if (*(volatile int *)&sq->status & ST_TIMEOUT) break;
             }
-            stage_flush(wr.sf, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
+            stage_flush(sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
             stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -405,29 +438,34 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             for (int64_t base = (int64_t)warp * 32; base < nfar; base += (int64_t)(blockDim.x >> 5) * 32) {
                 const int64_t idx = base + lane;
                 bool to_near = false, keep = false;
-                uint4 en = make_uint4(0u, 0u, 0u, 0u);
+                uint2 en = make_uint2(0u, 0u);
                 if (idx < nfar) {
                     en = __ldcg(fcur + idx);
-                    if (en.z < mu) {
+                    if (en.y < mu) {
                         const bool rev = (en.x >> 31) != 0;
-                        if (en.z < (rev ? Ts1 : Ts0)) to_near = true;
+                        if (en.y < (rev ? Ts1 : Ts0)) to_near = true;
                         else keep = true;
                         if (rev) {
-                            kmin1 = min(kmin1, en.z);
+                            kmin1 = min(kmin1, en.y);
                             if (to_near) mv1++;
                             else kp1++;
                         } else {
-                            kmin0 = min(kmin0, en.z);
+                            kmin0 = min(kmin0, en.y);
                             if (to_near) mv0++;
                             else kp0++;
                         }
                     }
                 }
-                stage_push(to_near, make_uint2(en.x, en.y), wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
-                stage_push(keep, en, wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
+                {
+                    const unsigned m = __ballot_sync(FULL, to_near);
+                    if (to_near) wr.sn[c_n + __popc(m & ((1u << lane) - 1u))] = en;
+                    c_n += __popc(m);
+                    if (c_n >= 32) flush_ring_or_far(wr.sn, c_n, sq, ring, cap, falt, B.cap_f, ctl);
+                }
+                stage_push(keep, en, sf2, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
             }
-            stage_flush(wr.sn, c_n, &sq->tail, ring, 0, (int64_t)cap, ctl, 0);
-            stage_flush(wr.sf, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
+            flush_ring_or_far(wr.sn, c_n, sq, ring, cap, falt, B.cap_f, ctl);
+            stage_flush(sf2, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 kmin0 = min(kmin0, __shfl_xor_sync(FULL, kmin0, o));
@@ -463,9 +501,10 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 sq->minkey[0] = sq->minkey[1] = 0xFFFFFFFFu;
                 sq->moved_dir[0] = sq->moved_dir[1] = 0;
                 sq->head = 0;
+                sq->tail = m;  // entries past the ring's capacity stayed in far
                 sq->pending = m;
             }
-            uint4 *t2 = fcur;
+            uint2 *t2 = fcur;
             fcur = falt;
             falt = t2;
             nfar = kept;

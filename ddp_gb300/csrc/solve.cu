@@ -29,8 +29,9 @@ size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind) {
     b += sizeof(unsigned long long) * (size_t)n * words;  // state
     b += sizeof(int32_t) * (size_t)n * words;             // touched
     if (kind & SLOT_HOPS) b += sizeof(uint32_t) * (size_t)n;
-    b += 2 * sizeof(uint2) * (size_t)cap_q;
-    b += 2 * sizeof(uint4) * (size_t)cap_f;
+    // paired (bidirectional) slots: one ring, far entries of 8 bytes
+    b += (words == 2 ? 1 : 2) * sizeof(uint2) * (size_t)cap_q;
+    b += 2 * (words == 2 ? sizeof(uint2) : sizeof(uint4)) * (size_t)cap_f;
     b += sizeof(SearchCtl);
     return b;
 }
@@ -49,15 +50,17 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)n * words * S));
     DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * words * S));
     if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
-    DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * 2 * S));
-    DDP_CUDA(cudaMalloc(&sa.f, sizeof(uint4) * (size_t)cap_f * 2 * S));
+    const size_t qn = words == 2 ? 1 : 2;                                      // rings per slot
+    const size_t fb = words == 2 ? sizeof(uint2) : sizeof(uint4);              // bytes per far entry
+    DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * qn * S));
+    DDP_CUDA(cudaMalloc(&sa.f, fb * (size_t)cap_f * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
     DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
     DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * words * S, st));
     if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
     // queue slots start as "empty" (the asynchronous engine's ring marker)
-    DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * 2 * S, st));
+    DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * qn * S, st));
     DDP_CUDA(cudaMemsetAsync(sa.ctl, 0, sizeof(SearchCtl) * S, st));
     return DDP_OK;
 }
@@ -79,10 +82,20 @@ __device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
     b.state = sa.state + n * sa.words * i;
     b.touched = sa.touched + n * sa.words * i;
     b.hops = sa.hops ? sa.hops + n * i : nullptr;
-    b.q0 = sa.q + (size_t)sa.cap_q * 2 * i;
-    b.q1 = b.q0 + sa.cap_q;
-    b.f0 = sa.f + (size_t)sa.cap_f * 2 * i;
-    b.f1 = b.f0 + sa.cap_f;
+    if (sa.words == 2) {
+        // paired slots: one ring; far piles of 8-byte entries (the uint4
+        // pointers only carry the address)
+        b.q0 = sa.q + (size_t)sa.cap_q * i;
+        b.q1 = b.q0;
+        uint2 *fb = reinterpret_cast<uint2 *>(sa.f) + (size_t)sa.cap_f * 2 * i;
+        b.f0 = reinterpret_cast<uint4 *>(fb);
+        b.f1 = reinterpret_cast<uint4 *>(fb + sa.cap_f);
+    } else {
+        b.q0 = sa.q + (size_t)sa.cap_q * 2 * i;
+        b.q1 = b.q0 + sa.cap_q;
+        b.f0 = sa.f + (size_t)sa.cap_f * 2 * i;
+        b.f1 = b.f0 + sa.cap_f;
+    }
     b.ctl = sa.ctl + i;
     b.cap_q = sa.cap_q;
     b.cap_f = sa.cap_f;
@@ -520,8 +533,13 @@ __device__ void service_loop(const BatchArgs &A) {
     }
 }
 
+// CTAs per SM the bidirectional instance is compiled for (its per-warp
+// register budget: 2 -> 64, 3 -> 40)
+#ifndef DDP_BIDIR_MIN_BLOCKS
+#define DDP_BIDIR_MIN_BLOCKS 2
+#endif
 template <int HK>
-__global__ void __launch_bounds__(512, 2) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
+__global__ void __launch_bounds__(512, (HK == 5 ? DDP_BIDIR_MIN_BLOCKS : 2)) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
     __shared__ WarpRows wrows[MAX_WARPS];
     __shared__ CtaQ sq;
     __shared__ BiQ bq;
@@ -1293,7 +1311,11 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     if (b->group > coresident) b->group = coresident;
     int nslots = coresident / b->group;
     if (b->o.grid > 0) nslots = std::min(b->o.grid, b->group > 1 ? nslots : b->o.grid);
-    const int64_t cap = b->o.queue_cap > 0 ? b->o.queue_cap : (int64_t)g->n + 4096;
+    // the bidirectional ring holds one bucket and spills to the far pile
+    // when full, so it needs far less than a node count
+    const int64_t cap = b->o.queue_cap > 0      ? b->o.queue_cap
+                        : hkind == DDP_H_BIDIR ? std::min<int64_t>((int64_t)g->n + 4096, 1 << 18)
+                                                : (int64_t)g->n + 4096;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     // the far pile holds every open node beyond the current bucket: twice the

@@ -43,8 +43,9 @@ def _dijkstra(n, off, col, w, s, t):
     return INF
 
 
-def bidir(n, fw, rv, s, t, delta, rng):
-    """fw, rv = (off, col, w) of the graph and of its reverse."""
+def bidir(n, fw, rv, s, t, delta, rng, ring_cap=1 << 30):
+    """fw, rv = (off, col, w) of the graph and of its reverse.  A split
+    moves at most ring_cap entries to the bucket; the rest stay in far."""
     if s == t:
         return 0, [s]
     lab = [[INF] * n, [INF] * n]
@@ -83,7 +84,7 @@ def bidir(n, fw, rv, s, t, delta, rng):
         for (v, dr, g) in far:
             if g >= mu:
                 continue
-            if g < Ts[dr]:
+            if g < Ts[dr] and len(moved) < ring_cap:
                 moved.append((v, dr, g))
                 nmoved[dr] += 1
             else:
@@ -124,8 +125,8 @@ def _path_weight(fw, p):
 
 @pytest.mark.parametrize("seed,n,e,wmax,zero", [(1, 300, 1200, 100, False), (2, 500, 900, 5, True),
                                                 (3, 2000, 16000, 100, False), (4, 800, 900, 3, True)])
-@pytest.mark.parametrize("delta", [1, 7, 60])
-def test_bidir_rules_match_dijkstra(seed, n, e, wmax, zero, delta):
+@pytest.mark.parametrize("delta,ring_cap", [(1, 1 << 30), (7, 1 << 30), (60, 1 << 30), (60, 5)])
+def test_bidir_rules_match_dijkstra(seed, n, e, wmax, zero, delta, ring_cap):
     r = np.random.default_rng(seed)
     u = r.integers(0, n, e)
     v = r.integers(0, n, e)
@@ -138,7 +139,7 @@ def test_bidir_rules_match_dijkstra(seed, n, e, wmax, zero, delta):
     for q in range(40):
         s, t = int(r.integers(0, n)), int(r.integers(0, n))
         want = _dijkstra(n, *fw, s, t)
-        got, path = bidir(n, fw, rv, s, t, delta, rng)
+        got, path = bidir(n, fw, rv, s, t, delta, rng, ring_cap)
         assert got == want, (s, t)
         if want < INF:
             assert path[0] == s and path[-1] == t
