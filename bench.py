@@ -3,10 +3,12 @@
 
 Workload (default, `--config c4`): 4,096 seeded source/target pairs on a
 4M-node random digraph (Hamiltonian chain + uniform arcs, average out-degree
-8, int32 weights uniform in [1,100]); heuristic h = the ALT landmark bound
-from 64 landmarks stored as 8-bit entries (128-B rows; the table is built
-once per graph, outside the timed region; `--heuristic capped` restores the per-query reverse BFS built
-inside the batch kernel); slot shape, bucket width and K from the
+8, int32 weights uniform in [1,100]), solved by the bidirectional engine
+(a forward search from s and a reverse search from t meet in the middle; no
+heuristic table).  `--heuristic landmark` runs A* with the ALT bound from 64
+landmarks of 8 bits instead (table built once per graph, outside the timed
+region), `--heuristic capped` the per-query reverse BFS built inside the
+batch kernel.  Slot shape, bucket width and queue capacity come from the
 autotuner, run on random queries before timing.  One step = one batch of
 all pairs through the persistent batch kernel.
 
@@ -71,7 +73,7 @@ def workload_name(c):
     return (f"batched multi-query GA*: {c['pairs']} seeded (s,t) pairs, target BFS hops log-uniform in "
             f"[{c['hop_lo']},{c['hop_hi']}] (clipped to what the graph realises), on a {c['n']:,}-node "
             f"random digraph (Hamiltonian chain + uniform arcs), avg out-degree {c['deg']}, int32 w U[{c['wmin']},"
-            f"{c['wmax']}]; heuristic in config.heuristic")
+            f"{c['wmax']}]; search method in engine.heuristic")
 
 
 def args_parse():
@@ -95,7 +97,7 @@ def args_parse():
     p.add_argument("--landmarks", type=int, default=64, help="landmark count for --heuristic landmark")
     p.add_argument("--landmark-bits", type=int, default=8, choices=[16, 8],
                    help="landmark table entry width (rows of 2 x landmarks entries)")
-    p.add_argument("--heuristic", default="landmark", choices=["capped", "bfs", "zero", "landmark", "bidir"],
+    p.add_argument("--heuristic", default="bidir", choices=["capped", "bfs", "zero", "landmark", "bidir"],
                    help="landmark: ALT bound from --landmarks landmarks (table built once per graph); "
                         "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
                         "get last level + 1); bfs: full reverse BFS; zero: h = 0; bidir: no heuristic, "

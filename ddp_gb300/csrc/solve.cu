@@ -533,10 +533,11 @@ __device__ void service_loop(const BatchArgs &A) {
     }
 }
 
-// CTAs per SM the bidirectional instance is compiled for (its per-warp
-// register budget: 2 -> 64, 3 -> 40)
+// CTAs per SM the bidirectional instance is compiled for (its register
+// budget per thread: 2 -> 64, 3 -> 40).  Measured on the 4M-node batch of
+// 4,096 pairs: 2 -> 243k queries/s, 3 -> 255k (456 slots), 4 -> 236k.
 #ifndef DDP_BIDIR_MIN_BLOCKS
-#define DDP_BIDIR_MIN_BLOCKS 2
+#define DDP_BIDIR_MIN_BLOCKS 3
 #endif
 template <int HK>
 __global__ void __launch_bounds__(512, (HK == 5 ? DDP_BIDIR_MIN_BLOCKS : 2)) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
