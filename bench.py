@@ -107,6 +107,7 @@ def args_parse():
     p.add_argument("--serve-rates", default="5000,10000,20000",
                    help="offered Poisson rates (requests/s) of the serving leg ('' = skip)")
     p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per serving rate")
+    p.add_argument("--rates", default="", help="serving configs: offered rates to run (default: the config's)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -171,23 +172,23 @@ def peak_hbm():
         return 6800.0, "fallback"
 
 
-# DRAM bytes per query of k_batch (dram__bytes_read.sum + dram__bytes_write.sum
-# of one ncu capture, divided by the launch's query count), keyed by
-# (workload, heuristic, table).  Each figure comes from the capture named
-# beside it (profiles/ holds its summary and command); None where no capture
-# covers the kernel as built.
-TRAFFIC_PER_QUERY = {
-    # profiles/k_batch_c4_landmark.md: full-size one-pass capture, 4,096 pairs
-    ("c4", "landmark", 64, 8): 143.77e6,
+# Measured DRAM traffic of k_batch per algorithmic byte
+# ((dram__bytes_read.sum + dram__bytes_write.sum) / algorithmic bytes of the
+# same launch), keyed by (workload family, method).  The capture runs a
+# smaller case of the same kernel (the 400k-node graph of the family, 1,024
+# pairs, one slot per SM), whose state still exceeds L2; a full launch's
+# traffic is this ratio times its own algorithmic bytes.  The summary and
+# the command are in profiles/k_batch5_c4_bidir.md.
+TRAFFIC_PER_ALG_BYTE = {
+    ("c4", "bidir"): 2761910528 / 372935900,
 }
 
 
-def traffic_per_launch(config_name, pairs, heuristic, landmarks, bits):
-    """Measured DRAM bytes of one k_batch launch: the per-query figure of
-    TRAFFIC_PER_QUERY scaled to this launch's query count, or None."""
-    per_query = TRAFFIC_PER_QUERY.get((config_name.replace("-small", ""), heuristic, landmarks or 0,
-                                       bits if landmarks else 0))
-    return None if per_query is None else per_query * pairs
+def traffic_per_launch(config_name, heuristic, alg_bytes):
+    """Measured DRAM bytes of one k_batch launch, scaled from the small-case
+    capture by algorithmic bytes, or None without a capture."""
+    r = TRAFFIC_PER_ALG_BYTE.get((config_name.replace("-small", ""), heuristic))
+    return None if r is None else r * alg_bytes
 
 
 FIXTURES = os.path.join(ROOT, "tests", "golden")
@@ -572,16 +573,19 @@ def bench_serving(a, c):
     import ddp_gb300 as d
     from oracle import oracle as O
     fixed = "deg" in c
+    bid = a.heuristic == "bidir"  # else A* with the graph's bound (landmarks / Euclidean)
     if fixed:
         g = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
         dg = d.DeviceGraph.from_csr(g)
-        dg.build_landmarks(a.landmarks, seed=c["gseed"], bits=a.landmark_bits)
-        srv = d.Server(dg, d.H_LANDMARK, max_requests=1 << 22, grid=a.slots, block=a.block)
+        if not bid:
+            dg.build_landmarks(a.landmarks, seed=c["gseed"], bits=a.landmark_bits)
+        hk = d.H_BIDIR if bid else d.H_LANDMARK
     else:
         g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
         dg = d.DeviceGraph.from_csr(g)
         dg.set_euclid(d.euclid_rho_fp(g))
-        srv = d.Server(dg, d.H_EUCLID, max_requests=1 << 22, grid=a.slots, block=a.block)
+        hk = d.H_BIDIR if bid else d.H_EUCLID
+    srv = d.Server(dg, hk, max_requests=1 << 22, grid=a.slots, block=a.block, delta=a.delta)
     rng = np.random.default_rng(c["gseed"] + 1)
     src = np.repeat(np.arange(g.n, dtype=np.int32), np.diff(g.off))
     deleted = []
@@ -614,8 +618,9 @@ def bench_serving(a, c):
     def endpoints(k):
         return rng.integers(0, g.n, k).astype(np.int32), rng.integers(0, g.n, k).astype(np.int32)
 
+    rates = [float(x) for x in a.rates.split(",") if x.strip()] or c["rates"]
     rows = [poisson_run(srv, rate, c["seconds"], rng, endpoints, None if fixed else update_batch,
-                        c.get("update_ms", 0))[0] for rate in c["rates"]]
+                        c.get("update_ms", 0))[0] for rate in rates]
     # exactness on a sample (against the current graph version: no updates now)
     Sx = rng.integers(0, g.n, 8).astype(np.int32)
     Tx = rng.integers(0, g.n, 8).astype(np.int32)
@@ -638,12 +643,13 @@ def bench_serving(a, c):
     out = {"metric": "A* serving queries/sec + p50/p99 latency (exact)", "value": best["served_qps"],
            "unit": "queries/s", "higher_is_better": True, "n_gpus": 1, "dtype": "int32",
            "data": "synthetic (seeded generators)",
+           "engine": {"method": "bidirectional" if bid else ("landmark A*" if fixed else "Euclidean A*")},
            "config": {"workload": (f"serving: {c['n']:,}-node random digraph (chain + uniform arcs), avg out-degree "
-                                   f"{c['deg']}, w U[{c['wmin']},{c['wmax']}], landmark heuristic ({a.landmarks}), "
+                                   f"{c['deg']}, w U[{c['wmin']},{c['wmax']}], "
                                    f"uniform random endpoints, Poisson arrivals, no updates") if fixed else
                                   (f"serving: {c['n']:,} points uniform on a {c['side']}^2 grid, symmetric "
                                    f"{c['k']}-NN arcs, w = max(1, round({c['wscale']} x length / mean spacing)), "
-                                   f"h = floor(rho x floor(distance)), Poisson arrivals, every {c['update_ms']} ms "
+                                   f"Poisson arrivals, every {c['update_ms']} ms "
                                    f"{c['wchanges']} weight changes x U[0.5,2] + {c['deletes']} deletes + up to "
                                    f"{c['inserts']} re-inserts"), "n": g.n, "e": g.e, "slots": st["slots"]},
            "rates": rows, "exact_on_sample": bool(exact), "server": st,
@@ -754,7 +760,7 @@ def main():
     alg = float(algorithmic_bytes(st, lm, a.landmark_bits).sum())
     peak, peak_kind = peak_hbm()
     achieved = alg / kernel_s / 1e9
-    traffic = traffic_per_launch(a.config, pairs, a.heuristic, lm, a.landmark_bits)
+    traffic = traffic_per_launch(a.config, a.heuristic, alg)
     lat_service = (t1 - t0) / 1e6
     lat_complete = (t1 - t0.min()) / 1e6
     # every answer against the oracle's costs for the same inputs (committed

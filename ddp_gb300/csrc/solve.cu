@@ -25,8 +25,9 @@ constexpr int MAX_WARPS = 16;  // blocks of at most 512 threads
 // ---- slot arrays -------------------------------------------------------------
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind) {
     const size_t words = (kind & SLOT_PAIR) ? 2 : 1;
+    const size_t nn = words == 2 ? (size_t)((n + 1) & ~1) : (size_t)n;
     size_t b = 0;
-    b += sizeof(unsigned long long) * (size_t)n * words;  // state
+    b += sizeof(unsigned long long) * nn * words;  // state
     b += sizeof(int32_t) * (size_t)n * words;             // touched
     if (kind & SLOT_HOPS) b += sizeof(uint32_t) * (size_t)n;
     // paired (bidirectional) slots: one ring, far entries of 8 bytes
@@ -43,11 +44,12 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     const size_t words = (kind & SLOT_PAIR) ? 2 : 1;
     sa.n = n;
     sa.words = (int)words;
+    sa.sstride = words == 2 ? 2 * (int64_t)((n + 1) & ~1) : (int64_t)n;
     sa.nslots = nslots;
     sa.cap_q = cap_q;
     sa.cap_f = cap_f;
     const size_t S = (size_t)nslots;
-    DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)n * words * S));
+    DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)sa.sstride * S));
     DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * words * S));
     if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
     const size_t qn = words == 2 ? 1 : 2;                                      // rings per slot
@@ -57,7 +59,7 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
     DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
-    DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)n * words * S, st));
+    DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)sa.sstride * S, st));
     if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
     // queue slots start as "empty" (the asynchronous engine's ring marker)
     DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * qn * S, st));
@@ -79,7 +81,7 @@ void slots_free(SlotArrays &sa) {
 __device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
     SlotBufs b;
     const size_t n = (size_t)sa.n;
-    b.state = sa.state + n * sa.words * i;
+    b.state = sa.state + (size_t)sa.sstride * i;
     b.touched = sa.touched + n * sa.words * i;
     b.hops = sa.hops ? sa.hops + n * i : nullptr;
     if (sa.words == 2) {
@@ -395,9 +397,14 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         grp.sync();
         const int cnt = *(volatile int *)&ctl->touched;
         if (HK == 5) {
-            // both words of each logged node (one 16-byte store)
+            // every word of a finished slot returns to all-ones, so the whole
+            // 32-byte sector holding a logged node (it and its neighbour
+            // node) is written: a full-sector store needs no read of the
+            // old sector
+            ulonglong4_32a ones;
+            ones.x = ones.y = ones.z = ones.w = ~0ull;
             for (int i = grp.rank(); i < cnt; i += grp.size())
-                reinterpret_cast<ulonglong2 *>(B.state)[B.touched[i]] = make_ulonglong2(~0ull, ~0ull);
+                reinterpret_cast<ulonglong4_32a *>(B.state)[B.touched[i] >> 1] = ones;
         } else {
             for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
         }

@@ -12,6 +12,8 @@ struct SlotArrays {
     int32_t n = 0;
     int nslots = 0;
     int words = 1;  // state words per node: 1, or 2 (forward and reverse, side by side)
+    int64_t sstride = 0;  // state words per slot (paired slots: an even node count, so that
+                          // every slot starts on a 32-byte boundary)
     int64_t cap_q = 0, cap_f = 0;
     unsigned long long *state = nullptr;  // nslots x n x words
     int32_t *touched = nullptr;           // nslots x n x words

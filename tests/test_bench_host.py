@@ -18,13 +18,13 @@ def test_algorithmic_bytes_accounting():
     assert bench.algorithmic_bytes(hops)[0] == 12 * 10 + 16 * 80 + 16 * 60 + 12 * 500 + 8 * 4000
 
 
-def test_traffic_figure_covers_its_table_only():
+def test_traffic_scales_with_algorithmic_bytes():
     import bench
-    per_query = bench.TRAFFIC_PER_QUERY[("c4", "landmark", 64, 8)]
-    assert bench.traffic_per_launch("c4", 4096, "landmark", 64, 8) == per_query * 4096
-    assert bench.traffic_per_launch("c4-small", 10, "landmark", 64, 8) == per_query * 10
-    assert bench.traffic_per_launch("c4", 4096, "landmark", 16, 16) is None
-    assert bench.traffic_per_launch("nonexistent", 100, "landmark", 64, 8) is None
+    r = bench.TRAFFIC_PER_ALG_BYTE[("c4", "bidir")]
+    assert 1.0 < r < 20.0
+    assert bench.traffic_per_launch("c4", "bidir", 1e9) == r * 1e9
+    assert bench.traffic_per_launch("c4-small", "bidir", 10.0) == r * 10.0
+    assert bench.traffic_per_launch("c4", "landmark", 1e9) is None
 
 
 def test_fixture_check_needs_matching_inputs(tmp_path, monkeypatch):

@@ -42,7 +42,7 @@ def _pairs(n, k, seed):
     return S, T
 
 
-@pytest.mark.parametrize("n,deg,wmax,seed", [(30000, 8, 100, 11), (20000, 3, 1000, 12), (5000, 2, 5, 13)])
+@pytest.mark.parametrize("n,deg,wmax,seed", [(30000, 8, 100, 11), (20000, 3, 1000, 12), (5001, 2, 5, 13)])
 def test_bidir_random_graphs(gpu, oracle, n, deg, wmax, seed):
     d = gpu
     g = d.gen_random_chain(n, deg, 1, wmax, seed)
