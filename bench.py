@@ -180,7 +180,7 @@ def peak_hbm():
 # traffic is this ratio times its own algorithmic bytes.  The summary and
 # the command are in profiles/k_batch5_c4_bidir.md.
 TRAFFIC_PER_ALG_BYTE = {
-    ("c4", "bidir"): 2761910528 / 372935900,
+    ("c4", "bidir"): (1.715554e9 + 1.047687e9) / 372840316,
 }
 
 
@@ -459,7 +459,7 @@ def bench_dynamic(a, c):
     t0 = time.perf_counter()
     dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS, grid=a.slots)
     t_init = time.perf_counter() - t0
-    cost0 = dyn.cost()
+    cost0 = dyn.cost
     nb = c["batches"]
     sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}
     off, col, ww = g.off[:-1].copy(), g.col.copy(), g.w.copy()
