@@ -180,7 +180,7 @@ def peak_hbm():
 # traffic is this ratio times its own algorithmic bytes.  The summary and
 # the command are in profiles/k_batch5_c4_bidir.md.
 TRAFFIC_PER_ALG_BYTE = {
-    ("c4", "bidir"): (1.715554e9 + 1.047687e9) / 372840316,
+    ("c4", "bidir"): (1.604023e9 + 0.638226e9) / 372947624,
 }
 
 

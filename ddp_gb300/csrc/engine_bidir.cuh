@@ -5,14 +5,16 @@
 // replace one ball of the full radius (orders of magnitude fewer nodes on
 // random digraphs).
 //
-// Layout: two state words per node, side by side (state[2v] forward
-// (g << 32 | parent), state[2v + 1] reverse (g << 32 | successor)), so one
-// 16-byte load of v's pair gives the label being relaxed and the other
-// side's label for the meeting test.  Entries carry their direction in the
-// top bit of the node id: ring and far entries are {v | dir << 31, g}
-// (the key is g).  The ring holds one bucket; when it is full, entries stay
-// in the far pile.  The touched log holds a node once per direction that reached it
-// (capacity 2n); a reset clears both words.
+// Layout: one 32-byte record per node (one DRAM sector), two 16-byte units,
+// forward then reverse, each {epoch, g, parent (reverse: successor), 0}.
+// Loading v's record gives the label being relaxed and the other side's
+// label for the meeting test.  A unit whose epoch is not the current
+// query's reads as unreached, so a slot is never reset between queries:
+// each query only advances the slot's epoch.  A label changes by one
+// 128-bit compare-and-swap of its unit (epoch, g and parent together).
+// Entries carry their direction in the top bit of the node id: ring and far
+// entries are {v | dir << 31, g} (the key is g).  The ring holds one bucket;
+// when it is full, entries stay in the far pile.
 //
 // Work distribution is the asynchronous engine's (engine_async.cuh): the
 // current bucket (keys below the thresholds) is a pool that warps drain
@@ -49,6 +51,13 @@
 #include "engine_async.cuh"
 
 namespace ddp {
+
+// Longest sleep (ns) of an idle warp's poll for bucket work.  With 64 ns
+// polls, idle warps executed half of all instructions of a batch; backing
+// off to 1 us halves the instruction count and costs no time.
+#ifndef DDP_BIDIR_SPIN_CAP
+#define DDP_BIDIR_SPIN_CAP 1024
+#endif
 
 constexpr uint32_t DIR_BIT = 0x80000000u;
 constexpr uint32_t NODE_MASK = 0x7FFFFFFFu;
@@ -105,12 +114,41 @@ __device__ __forceinline__ void flush_ring_or_far(uint2 *buf, int &cnt, BiQ *sq,
     cnt = 0;
 }
 
-__device__ __forceinline__ ulonglong2 ld_pair(const unsigned long long *st2, int v) {
-    return __ldcg(reinterpret_cast<const ulonglong2 *>(st2) + v);
+// Unit of node v in direction dir of a paired slot's records.
+__device__ __forceinline__ uint4 *unit_ptr(unsigned long long *st, int v, uint32_t dir) {
+    return reinterpret_cast<uint4 *>(st) + 2 * (size_t)v + dir;
+}
+
+// g of a unit, or INF_G when it belongs to another query.
+__device__ __forceinline__ uint32_t unit_g(const uint4 &u, uint32_t ep) { return u.x == ep ? u.y : INF_G; }
+
+__device__ __forceinline__ bool unit_eq(const uint4 &a, const uint4 &b) {
+    return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w;
+}
+
+// 128-bit compare-and-swap (PTX atom.cas.b128, sm_90 and later) on a
+// 16-byte aligned unit; returns the unit's old value.  The first 64-bit
+// operand of each pair is the low half ({x, y}), the second the high half.
+__device__ __forceinline__ uint4 cas_unit(uint4 *addr, const uint4 &cmp, const uint4 &val) {
+    const unsigned long long c0 = ((unsigned long long)cmp.y << 32) | cmp.x;
+    const unsigned long long c1 = ((unsigned long long)cmp.w << 32) | cmp.z;
+    const unsigned long long v0 = ((unsigned long long)val.y << 32) | val.x;
+    const unsigned long long v1 = ((unsigned long long)val.w << 32) | val.z;
+    unsigned long long o0, o1;
+    asm volatile(
+        "{\n\t.reg .b128 cc, vv, oo;\n\t"
+        "mov.b128 cc, {%2, %3};\n\t"
+        "mov.b128 vv, {%4, %5};\n\t"
+        "atom.global.cas.b128 oo, [%6], cc, vv;\n\t"
+        "mov.b128 {%0, %1}, oo;\n\t}"
+        : "=l"(o0), "=l"(o1)
+        : "l"(c0), "l"(c1), "l"(v0), "l"(v1), "l"(addr)
+        : "memory");
+    return make_uint4((uint32_t)o0, (uint32_t)(o0 >> 32), (uint32_t)o1, (uint32_t)(o1 >> 32));
 }
 
 // Path s..t from the meeting word; returns its length (0 when no path).
-__device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B, int32_t s, int32_t t,
+__device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B, uint32_t ep, int32_t s, int32_t t,
                                            unsigned long long mu, int32_t *path, int32_t cap, int *status) {
     const uint32_t cost = uint32_t(mu >> 32);
     if (cost >= INF_G) return 0;
@@ -118,42 +156,45 @@ __device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B,
         if (cap > 0) path[0] = s;
         return 1;
     }
+    unsigned long long *st = B.state;
     const int32_t x = int32_t(uint32_t(mu));
-    const uint32_t gx = st_g(__ldcg(B.state + 2 * (size_t)x));
+    const uint32_t gx = unit_g(__ldcg(unit_ptr(st, x, 0)), ep);
     int32_t y = -1;
     const int r1 = row_end(G.off, G.oend, x);
     for (int k = row_begin(G.off, G.oend, x); k < r1 && y < 0; k++) {
         const uint2 a = G.oend ? __ldcg(G.arc + k) : __ldg(G.arc + k);
         if ((int)a.x < 0) continue;
-        const uint32_t gr = st_g(__ldcg(B.state + 2 * (size_t)a.x + 1));
+        const uint32_t gr = unit_g(__ldcg(unit_ptr(st, (int)a.x, 1)), ep);
         if (gr < INF_G && (uint64_t)gx + a.y + gr == cost) y = (int32_t)a.x;
     }
     if (y < 0) {
         atomicOr(status, ST_TIMEOUT);  // no meeting arc: report the query failed
         return 0;
     }
-    // lengths of s..x and y..t
+    // lengths of s..x (forward parents) and y..t (reverse successors)
     int32_t lf = 0, lr = 0;
-    for (int32_t c = x; c >= 0 && lf <= G.n; c = st_parent(__ldcg(B.state + 2 * (size_t)c))) {
+    for (int32_t c = x; c >= 0 && lf <= G.n; c = (int32_t)__ldcg(unit_ptr(st, c, 0)).z) {
         lf++;
         if (c == s) break;
     }
-    for (int32_t c = y; c >= 0 && lr <= G.n; c = st_parent(__ldcg(B.state + 2 * (size_t)c + 1))) {
+    for (int32_t c = y; c >= 0 && lr <= G.n; c = (int32_t)__ldcg(unit_ptr(st, c, 1)).z) {
         lr++;
         if (c == t) break;
     }
     const int32_t len = lf + lr;
     if (len > cap) atomicOr(status, ST_PATH_TRUNC);
     int32_t i = lf - 1;
-    for (int32_t c = x; c >= 0 && i >= 0; c = st_parent(__ldcg(B.state + 2 * (size_t)c)), i--)
+    for (int32_t c = x; c >= 0 && i >= 0; c = (int32_t)__ldcg(unit_ptr(st, c, 0)).z, i--)
         if (i < cap) path[i] = c;
     i = lf;
-    for (int32_t c = y; c >= 0 && i < len; c = st_parent(__ldcg(B.state + 2 * (size_t)c + 1)), i++)
+    for (int32_t c = y; c >= 0 && i < len; c = (int32_t)__ldcg(unit_ptr(st, c, 1)).z, i++)
         if (i < cap) path[i] = c;
     return len;
 }
 
-__device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, const SearchParams &P,
+// ep: the slot's epoch for this query (never 0; units of other epochs read
+// as unreached).
+__device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, const SearchParams &P, uint32_t ep,
                                       WarpRows *wrows, BiQ *sq) {
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
@@ -162,7 +203,6 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
     uint2 *ring = B.q0;
     unsigned long long *st2 = B.state;
     const int cap = (int)min(B.cap_q, (int64_t)0x3FFFFFFF);
-    const int64_t cap_t = 2 * (int64_t)G.n;
 
     if (threadIdx.x == 0) {
         ctl->iters = 0;
@@ -182,10 +222,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             ctl->touched = 0;
         } else {
             sq->mu = ~0ull;
-            st2[2 * (size_t)P.s] = st_make(0, -1);
-            st2[2 * (size_t)P.t + 1] = st_make(0, -1);
-            B.touched[0] = P.s;
-            B.touched[1] = P.t;
+            *unit_ptr(st2, P.s, 0) = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
+            *unit_ptr(st2, P.t, 1) = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
             ctl->touched = 2;
             ring[0] = make_uint2((uint32_t)P.s, 0u);
             ring[1] = make_uint2((uint32_t)P.t | DIR_BIT, 0u);
@@ -211,13 +249,13 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
     uint32_t T0 = P.delta, T1 = P.delta;
     uint32_t lo0 = 0, lo1 = 0;
     bool do_expand = true;
-    unsigned long long n_exp = 0, n_scan = 0, n_rel = 0;
+    unsigned long long n_exp = 0, n_scan = 0, n_rel = 0, n_first = 0;
     int phases = 0;
     const int64_t max_phases = 4 * (int64_t)G.n + (1 << 22);
 
     for (;;) {
         if (do_expand) {
-            int c_f = 0, c_t = 0, c_loc = 0;  // staged far pushes, touches, own children
+            int c_f = 0, c_loc = 0;  // staged far pushes, own children
             int nf0 = 0, nf1 = 0;             // far pushes per direction (this lane)
             for (;;) {
                 const uint32_t mu = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
@@ -233,6 +271,10 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     int h0 = 0;
                     if (lane == 0) {
                         n = -1;
+                        // an idle warp backs off exponentially (up to
+                        // DDP_BIDIR_SPIN_CAP ns): its polls would otherwise
+                        // take issue slots from the warps that have work
+                        unsigned int ns = 32;
                         for (uint32_t spins = 0;; spins++) {
                             const int h = *(volatile int *)&sq->head, t = *(volatile int *)&sq->tail;
                             if (h < t) {
@@ -249,7 +291,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                 atomicOr(&sq->status, ST_TIMEOUT);
                                 break;
                             }
-                            __nanosleep(64);
+                            __nanosleep(ns);
+                            if (ns < DDP_BIDIR_SPIN_CAP) ns <<= 1;
                         }
                     }
                     n = __shfl_sync(FULL, n, 0);
@@ -279,8 +322,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     gu = en.y;
                     const int u = (int)(ud & NODE_MASK);
                     const uint32_t dir = ud >> 31;
-                    const uint64_t su = __ldcg(st2 + 2 * (size_t)u + dir);
-                    if (st_g(su) == gu && gu < mu) {
+                    if (unit_g(__ldcg(unit_ptr(st2, u, dir)), ep) == gu && gu < mu) {
                         const int r0 = dir ? row_begin(G.roff, G.roend, u) : row_begin(G.off, G.oend, u);
                         const int r1 = dir ? row_end(G.roff, G.roend, u) : row_end(G.off, G.oend, u);
                         rb = r0;
@@ -304,7 +346,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     int v = 0;
                     uint32_t ng = 0, dir = 0;
                     uint32_t uo = 0;
-                    ulonglong2 pr = make_ulonglong2(0ull, 0ull);
+                    uint4 uf = make_uint4(0u, 0u, 0u, 0u), ur = uf;
                     if (k < total) {
                         const int o = row_owner(wr, k);
                         uo = (uint32_t)wr.u[o];
@@ -314,11 +356,15 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
                         live = v >= 0 && ng64 < (uint64_t)min(mu, INF_G);
                         ng = (uint32_t)ng64;
-                        if (live) pr = ld_pair(st2, v);
+                        if (live) {
+                            // the node's record: both units, one sector
+                            uf = __ldcg(unit_ptr(st2, v, 0));
+                            ur = __ldcg(unit_ptr(st2, v, 1));
+                        }
                     }
                     if (live) {
-                        const uint64_t mine = dir ? pr.y : pr.x;
-                        const uint32_t go = st_g(dir ? pr.x : pr.y);
+                        const uint4 mine = dir ? ur : uf;
+                        const uint32_t go = unit_g(dir ? uf : ur, ep);
                         if (go < INF_G) {
                             // the two searches meet over this arc
                             const uint64_t c = (uint64_t)ng + go;
@@ -327,21 +373,27 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                 atomicMin(&sq->mu, (c << 32) | x);
                             }
                         }
-                        live = ng < st_g(mine);
+                        live = ng < unit_g(mine, ep);
                         if (live) {
-                            const uint64_t nv = st_make(ng, (int32_t)(uo & NODE_MASK));
-                            unsigned long long *w = st2 + 2 * (size_t)v + dir;
-                            uint64_t c0 = mine;
+                            const uint4 nv = make_uint4(ep, ng, uo & NODE_MASK, 0u);
+                            uint4 *w = unit_ptr(st2, v, dir);
+                            uint4 c0 = mine;
                             live = false;
-                            for (;;) {
-                                const uint64_t got = atomicCAS(w, c0, nv);
-                                if (got == c0) {
+                            // bounded: contention on one unit comes from at
+                            // most the CTA's own threads
+                            for (int tries = 0;; tries++) {
+                                if (tries == 4096) {
+                                    atomicOr(&sq->status, ST_TIMEOUT);
+                                    break;
+                                }
+                                const uint4 got = cas_unit(w, c0, nv);
+                                if (unit_eq(got, c0)) {
                                     live = true;
-                                    first = st_g(c0) >= INF_G;
+                                    first = c0.x != ep;
                                     break;
                                 }
                                 c0 = got;
-                                if (ng >= st_g(c0)) break;
+                                if (ng >= unit_g(c0, ep)) break;
                             }
                         }
                     }
@@ -383,7 +435,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     }
                     stage_push(to_far, make_uint2(vd, ng), sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
                                ctl, 0);
-                    stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
+                    if (first) n_first++;
                 }
                 __syncwarp();
                 // 3. retire the chunk (its children are already counted)
@@ -391,7 +443,6 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 if (*(volatile int *)&sq->status & ST_TIMEOUT) break;
             }
             stage_flush(sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
-            stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, cap_t, ctl, 0);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 nf0 += __shfl_xor_sync(FULL, nf0, o);
@@ -536,10 +587,12 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
     for (int o = 16; o > 0; o >>= 1) {
         n_exp += __shfl_xor_sync(FULL, n_exp, o);
         n_rel += __shfl_xor_sync(FULL, n_rel, o);
+        n_first += __shfl_xor_sync(FULL, n_first, o);
     }
     if (lane == 0) {
         if (n_exp) atomicAdd(&ctl->expanded, n_exp);
         if (n_rel) atomicAdd(&ctl->relaxed, n_rel);
+        if (n_first) atomicAdd(&ctl->touched, (int)n_first);
     }
     if (threadIdx.x == 0) ctl->iters = phases;
     __syncthreads();

@@ -406,7 +406,9 @@ int launch(ddp_server *s) {
     A.path_cap = 0;
     A.work = s->d_work;
     A.status = s->d_work + 1;
-    A.delta = s->o.delta > 0 ? (uint32_t)s->o.delta : auto_delta(s->g);
+    A.delta = s->o.delta > 0                ? (uint32_t)s->o.delta
+              : s->hkind == DDP_H_BIDIR ? auto_delta_bidir(s->g)
+                                        : auto_delta(s->g);
     A.K = s->o.K;
     A.bfs_budget = s->hkind == DDP_H_BFS_CAPPED ? bfs_budget(s->g->n) : 0;
     A.group = 1;

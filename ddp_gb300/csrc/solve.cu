@@ -23,16 +23,18 @@ namespace ddp {
 constexpr int MAX_WARPS = 16;  // blocks of at most 512 threads
 
 // ---- slot arrays -------------------------------------------------------------
+// Paired (bidirectional) slots hold a 32-byte record per node (two
+// epoch-tagged units), no touched log, one ring and 8-byte far entries;
+// the others one 8-byte state word per node, a touched log, two queues and
+// 16-byte far entries.
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind) {
-    const size_t words = (kind & SLOT_PAIR) ? 2 : 1;
-    const size_t nn = words == 2 ? (size_t)((n + 1) & ~1) : (size_t)n;
+    const bool pair = (kind & SLOT_PAIR) != 0;
     size_t b = 0;
-    b += sizeof(unsigned long long) * nn * words;  // state
-    b += sizeof(int32_t) * (size_t)n * words;             // touched
+    b += sizeof(unsigned long long) * (size_t)n * (pair ? 4 : 1);  // state
+    if (!pair) b += sizeof(int32_t) * (size_t)n;                     // touched
     if (kind & SLOT_HOPS) b += sizeof(uint32_t) * (size_t)n;
-    // paired (bidirectional) slots: one ring, far entries of 8 bytes
-    b += (words == 2 ? 1 : 2) * sizeof(uint2) * (size_t)cap_q;
-    b += 2 * (words == 2 ? sizeof(uint2) : sizeof(uint4)) * (size_t)cap_f;
+    b += (pair ? 1 : 2) * sizeof(uint2) * (size_t)cap_q;
+    b += 2 * (pair ? sizeof(uint2) : sizeof(uint4)) * (size_t)cap_f;
     b += sizeof(SearchCtl);
     return b;
 }
@@ -41,25 +43,27 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
                 cudaStream_t st) {
     sa = SlotArrays();
     const bool hops = (kind & SLOT_HOPS) != 0;
-    const size_t words = (kind & SLOT_PAIR) ? 2 : 1;
+    const bool pair = (kind & SLOT_PAIR) != 0;
     sa.n = n;
-    sa.words = (int)words;
-    sa.sstride = words == 2 ? 2 * (int64_t)((n + 1) & ~1) : (int64_t)n;
+    sa.words = pair ? 4 : 1;
+    sa.sstride = (int64_t)n * sa.words;
     sa.nslots = nslots;
     sa.cap_q = cap_q;
     sa.cap_f = cap_f;
     const size_t S = (size_t)nslots;
     DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)sa.sstride * S));
-    DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * words * S));
+    if (!pair) DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * S));
     if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
-    const size_t qn = words == 2 ? 1 : 2;                                      // rings per slot
-    const size_t fb = words == 2 ? sizeof(uint2) : sizeof(uint4);              // bytes per far entry
+    const size_t qn = pair ? 1 : 2;                             // rings per slot
+    const size_t fb = pair ? sizeof(uint2) : sizeof(uint4);     // bytes per far entry
     DDP_CUDA(cudaMalloc(&sa.q, sizeof(uint2) * (size_t)cap_q * qn * S));
     DDP_CUDA(cudaMalloc(&sa.f, fb * (size_t)cap_f * 2 * S));
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
     DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
-    DDP_CUDA(cudaMemsetAsync(sa.state, 0xFF, sizeof(unsigned long long) * (size_t)sa.sstride * S, st));
+    // unreached: all-ones words, or (paired records) epoch 0, which no
+    // query uses
+    DDP_CUDA(cudaMemsetAsync(sa.state, pair ? 0 : 0xFF, sizeof(unsigned long long) * (size_t)sa.sstride * S, st));
     if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
     // queue slots start as "empty" (the asynchronous engine's ring marker)
     DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * qn * S, st));
@@ -82,9 +86,9 @@ __device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
     SlotBufs b;
     const size_t n = (size_t)sa.n;
     b.state = sa.state + (size_t)sa.sstride * i;
-    b.touched = sa.touched + n * sa.words * i;
+    b.touched = sa.touched ? sa.touched + n * i : nullptr;
     b.hops = sa.hops ? sa.hops + n * i : nullptr;
-    if (sa.words == 2) {
+    if (sa.words == 4) {
         // paired slots: one ring; far piles of 8-byte entries (the uint4
         // pointers only carry the address)
         b.q0 = sa.q + (size_t)sa.cap_q * i;
@@ -290,9 +294,23 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
                 *epoch = ep;
                 ctl->tag = ep << 8;
             }
+            if (HK == 5) {
+                // per-query epoch of the slot's records (0 = never used);
+                // tag 0 asks for the records to be cleared once the
+                // 32-bit epoch wraps
+                const uint32_t ep = *epoch + 1;
+                *epoch = ep == 0 ? 1u : ep;
+                ctl->tag = ep;
+            }
             t0 = global_ns();
         }
         grp.sync();
+        if (HK == 5 && *(volatile uint32_t *)&ctl->tag == 0) {
+            for (size_t i = grp.rank(); i < 4 * (size_t)G0.n; i += grp.size()) B.state[i] = 0ull;
+            grp.sync();
+            if (grp.rank() == 0) ctl->tag = 1;
+            grp.sync();
+        }
         const int q = *(volatile int *)&ctl->cur_q;
         if (q >= A.nq) break;
         const int qver = A.vtab ? *(volatile int *)&ctl->cur_ver : A.version;
@@ -344,7 +362,8 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         } else if (HK == 5) {
             // bidirectional: one-CTA slots only (the host never launches
             // this kind with wider slots)
-            if constexpr (std::is_same<Grp, CtaGroup>::value) r = run_bidir_cta(G, B, P, wrows, bq);
+            if constexpr (std::is_same<Grp, CtaGroup>::value)
+                r = run_bidir_cta(G, B, P, *(volatile uint32_t *)&ctl->tag, wrows, bq);
         } else {
             r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
         }
@@ -359,8 +378,8 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             int32_t len = 0;
             if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths) {
                 if (HK == 5)
-                    len = write_path_bidir(G, B, s, t, bq->mu, A.paths + (size_t)q * A.path_cap, A.path_cap,
-                                           &ctl->status);
+                    len = write_path_bidir(G, B, ctl->tag, s, t, bq->mu, A.paths + (size_t)q * A.path_cap,
+                                           A.path_cap, &ctl->status);
                 else
                     len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
                                      &ctl->status);
@@ -396,16 +415,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         }
         grp.sync();
         const int cnt = *(volatile int *)&ctl->touched;
-        if (HK == 5) {
-            // every word of a finished slot returns to all-ones, so the whole
-            // 32-byte sector holding a logged node (it and its neighbour
-            // node) is written: a full-sector store needs no read of the
-            // old sector
-            ulonglong4_32a ones;
-            ones.x = ones.y = ones.z = ones.w = ~0ull;
-            for (int i = grp.rank(); i < cnt; i += grp.size())
-                reinterpret_cast<ulonglong4_32a *>(B.state)[B.touched[i] >> 1] = ones;
-        } else {
+        if (HK != 5) {  // paired records need no reset: the next query has a new epoch
             for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
         }
         grp.sync();
@@ -664,6 +674,14 @@ int slots_per_sm(int hkind, int block) {
 }
 
 int device_sms() { return sm_count(); }
+
+// The bidirectional search keys its buckets by g and each side only runs
+// to about half the distance, so narrower buckets pay (C4 family, 4,096
+// pairs: width 5 -> 319k queries/s, 8 -> 338k, 12 -> 314k, 25 -> 199k).
+uint32_t auto_delta_bidir(const ddp_graph *g) {
+    const uint32_t d = (g->wmin + g->wmax) / 12;
+    return d < 1 ? 1 : d;
+}
 
 uint32_t auto_delta(const ddp_graph *g) {
     // bucket width ~ a typical arc weight: wide enough for parallel buckets,
@@ -1241,7 +1259,9 @@ static bool batch_args(ddp_batch *b, int32_t n, const int32_t *dS, const int32_t
     A.tend = b->d_t1;
     A.work = b->d_work;
     A.status = b->d_status;
-    A.delta = b->o.delta > 0 ? (uint32_t)b->o.delta : auto_delta(b->g);
+    A.delta = b->o.delta > 0                ? (uint32_t)b->o.delta
+              : b->hkind == DDP_H_BIDIR ? auto_delta_bidir(b->g)
+                                        : auto_delta(b->g);
     A.bfs_budget = b->hkind == DDP_H_BFS_CAPPED ? bfs_budget(b->g->n) : 0;
     A.K = b->o.K;
     A.group = b->group;

@@ -11,12 +11,11 @@ struct SearchCtl;
 struct SlotArrays {
     int32_t n = 0;
     int nslots = 0;
-    int words = 1;  // state words per node: 1, or 2 (forward and reverse, side by side)
-    int64_t sstride = 0;  // state words per slot (paired slots: an even node count, so that
-                          // every slot starts on a 32-byte boundary)
+    int words = 1;        // 64-bit state words per node: 1, or 4 (paired slots: a 32-byte record)
+    int64_t sstride = 0;  // state words per slot
     int64_t cap_q = 0, cap_f = 0;
     unsigned long long *state = nullptr;  // nslots x n x words
-    int32_t *touched = nullptr;           // nslots x n x words
+    int32_t *touched = nullptr;           // nslots x n (null for paired slots)
     uint32_t *hops = nullptr;             // nslots x n (per-target heuristic) or null
     uint2 *q = nullptr;                   // nslots x 2 x cap_q
     uint4 *f = nullptr;                   // nslots x 2 x cap_f {node, g, f, 0}
@@ -93,6 +92,7 @@ cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, 
 int slots_per_sm(int hkind, int block);
 int device_sms();
 uint32_t auto_delta(const ddp_graph *g);
+uint32_t auto_delta_bidir(const ddp_graph *g);
 int64_t bfs_budget(int32_t n);
 
 }  // namespace ddp

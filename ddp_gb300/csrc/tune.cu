@@ -24,8 +24,9 @@ double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Queries/s of one configuration on the sample (one warm-up pass on a
-// prefix, then one timed pass over the whole sample); costs into `cost`.
+// Queries/s of one configuration on the sample (one warm-up pass over the
+// whole sample, so that every slot has run before the timing, then one
+// timed pass); costs into `cost`.
 int trial(ddp_graph *g, int32_t hkind, const ddp_opts &o, int32_t n, const int32_t *S, const int32_t *T,
           std::vector<int32_t> &cost, double *qps) {
     ddp_batch *b = nullptr;
@@ -33,8 +34,7 @@ int trial(ddp_graph *g, int32_t hkind, const ddp_opts &o, int32_t n, const int32
     if (rc) return rc;
     std::vector<int32_t> plen((size_t)n);
     cost.assign((size_t)n, 0);
-    const int32_t warm = n < 64 ? n : 64;
-    rc = ddp_batch_solve(b, warm, S, T, cost.data(), plen.data());
+    rc = ddp_batch_solve(b, n, S, T, cost.data(), plen.data());
     if (!rc) {
         const double t0 = now_s();
         rc = ddp_batch_solve(b, n, S, T, cost.data(), plen.data());
@@ -85,7 +85,7 @@ int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *source
     }
     // 2. bucket width: half and twice the automatic one, then further steps
     //    of 2/3 (or 3/2) while the winning direction keeps winning
-    const uint32_t d0 = auto_delta(g);
+    const uint32_t d0 = hkind == DDP_H_BIDIR ? auto_delta_bidir(g) : auto_delta(g);
     const ddp_opts shape = top_o;
     uint32_t best_d = d0;
     for (uint32_t dv : {d0 / 2, d0 * 2}) {
