@@ -89,6 +89,8 @@ def args_parse():
     p.add_argument("--delta", type=int, default=0)
     p.add_argument("--K", type=int, default=0)
     p.add_argument("--queue-cap", type=int, default=0, help="entries per slot queue (0 = automatic)")
+    p.add_argument("--dyn-group", type=int, default=0,
+                   help="dynamic configs: CTAs of each update batch (0/1 = one CTA, more = cooperative grid)")
     p.add_argument("--group", type=int, default=19, help="CTAs per query slot (with --no-tune)")
     p.add_argument("--no-tune", action="store_true",
                    help="take group/block/delta/K from the flags instead of the autotuner")
@@ -457,7 +459,7 @@ def bench_dynamic(a, c):
     g = base.with_sentinel()
     dg = d.DeviceGraph.from_csr(g)
     t0 = time.perf_counter()
-    dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS, grid=a.slots)
+    dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS, grid=a.slots, group=a.dyn_group)
     t_init = time.perf_counter() - t0
     cost0 = dyn.cost
     nb = c["batches"]
@@ -503,7 +505,8 @@ def bench_dynamic(a, c):
            "unit": "ms/batch", "higher_is_better": False, "n_gpus": 1, "steps": nb, "warmup": 0,
            "dtype": "int32", "data": "synthetic (seeded generators)",
            "config": {"workload": workload, "n": g.n, "e": g.e,
-                      "updates_per_batch_mean": float(np.mean(np.diff(bounds)))},
+                      "updates_per_batch_mean": float(np.mean(np.diff(bounds))),
+                      "update_ctas": max(1, a.dyn_group)},
            "batch_ms": {"p50": 1000 * _pct(dyn_t, 50), "p99": 1000 * _pct(dyn_t, 99),
                         "initial_search_ms": 1000 * t_init},
            "gpu_from_scratch_ms_per_batch": 1000 * float(np.mean(scratch_t)),

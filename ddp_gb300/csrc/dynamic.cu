@@ -62,10 +62,22 @@ struct DynMirror {
     uint2 *d_val = nullptr;
     int4 *d_rows = nullptr;
     int64_t scat_cap = 0, rows_cap = 0;
+    // pinned staging of the scatter lists ([0] forward, [1] reverse), so
+    // that their copies are asynchronous; reused once the graph's stream
+    // has been synchronised (every update path ends with that)
+    long long *h_slot[2] = {nullptr, nullptr};
+    uint2 *h_val[2] = {nullptr, nullptr};
+    int4 *h_rows[2] = {nullptr, nullptr};
+    int64_t h_scap[2] = {0, 0}, h_rcap[2] = {0, 0};
     ~DynMirror() {
         cudaFree(d_slot);
         cudaFree(d_val);
         cudaFree(d_rows);
+        for (int i = 0; i < 2; i++) {
+            cudaFreeHost(h_slot[i]);
+            cudaFreeHost(h_val[i]);
+            cudaFreeHost(h_rows[i]);
+        }
     }
 };
 
@@ -200,11 +212,21 @@ __device__ void dyn_level_end(const Grp &grp, DynCtl *dc, int it, int &nf) {
     nf = *(volatile int *)&dc->cnt[PH];
 }
 
+__device__ __forceinline__ GridGroup dyn_group(GridGroup *, const SlotBufs &B) {
+    return GridGroup{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
+}
+__device__ __forceinline__ CtaGroup dyn_group(CtaGroup *, const SlotBufs &B) { return CtaGroup{&B.ctl->status}; }
+
+// Grp = GridGroup: every CTA of a cooperative launch (the initial search);
+// Grp = CtaGroup: one CTA (update batches: the repair and the resumed
+// search touch little of the graph, and block barriers are far cheaper than
+// grid barriers between the repair steps and the search phases).
+template <class Grp>
 __global__ void __launch_bounds__(512, 2)
     k_dyn(DevGraph G, SlotArrays sa, uint32_t *hops, SearchParams P, DynArgs A, DynCtl *dc) {
     __shared__ WarpRows wrows[16];
     SlotBufs B = slot_of_dyn(sa);
-    GridGroup grp{{&B.ctl->bar_count, &B.ctl->bar_gen}, &B.ctl->status};
+    const Grp grp = dyn_group(static_cast<Grp *>(nullptr), B);
     const int rank = grp.rank(), size = grp.size();
     const uint32_t scale = G.wmin;
     int32_t *fa = reinterpret_cast<int32_t *>(B.q0);
@@ -395,12 +417,13 @@ struct ddp_dyn {
     int32_t cost = DDP_INF;
     int32_t path_len = 0;
     int64_t stats[10] = {0};
-    int grid = 0;
+    int grid = 0;      // CTAs of the initial search
+    int upd_grid = 0;  // CTAs of an update batch (1: the one-CTA kernel)
 };
 
 namespace ddp {
 
-int dyn_upload(ddp_graph *g) {
+int dyn_upload(ddp_graph *g, bool sync) {
     DynMirror *m = g->dyn;
     DynMirror *d = m;  // device bookkeeping lives in the mirror
     const int32_t n = g->n;
@@ -432,7 +455,7 @@ int dyn_upload(ddp_graph *g) {
         return DDP_OK;
     }
     // scatter the touched slots and row bounds
-    auto scatter = [&](std::vector<int64_t> &dirty, std::vector<uint2> &src, uint2 *dst) -> int {
+    auto scatter = [&](std::vector<int64_t> &dirty, std::vector<uint2> &src, uint2 *dst, int side) -> int {
         if (dirty.empty()) return DDP_OK;
         std::sort(dirty.begin(), dirty.end());
         dirty.erase(std::unique(dirty.begin(), dirty.end()), dirty.end());
@@ -456,15 +479,30 @@ int dyn_upload(ddp_graph *g) {
             DDP_CUDA(cudaMalloc(&d->d_val, sizeof(uint2) * k));
             d->scat_cap = k;
         }
-        DDP_CUDA(cudaMemcpyAsync(d->d_slot, sl.data(), sizeof(long long) * k, cudaMemcpyHostToDevice, g->stream));
-        DDP_CUDA(cudaMemcpyAsync(d->d_val, val.data(), sizeof(uint2) * k, cudaMemcpyHostToDevice, g->stream));
+        if (k > d->h_scap[side]) {
+            cudaFreeHost(d->h_slot[side]);
+            cudaFreeHost(d->h_val[side]);
+            d->h_slot[side] = nullptr;
+            d->h_val[side] = nullptr;
+            d->h_scap[side] = 0;
+            DDP_CUDA(cudaHostAlloc(&d->h_slot[side], sizeof(long long) * k, cudaHostAllocDefault));
+            DDP_CUDA(cudaHostAlloc(&d->h_val[side], sizeof(uint2) * k, cudaHostAllocDefault));
+            d->h_scap[side] = k;
+        }
+        std::memcpy(d->h_slot[side], sl.data(), sizeof(long long) * k);
+        std::memcpy(d->h_val[side], val.data(), sizeof(uint2) * k);
+        // device staging is shared by both sides: stream order keeps the
+        // forward scatter's kernel ahead of the reverse side's copies
+        DDP_CUDA(cudaMemcpyAsync(d->d_slot, d->h_slot[side], sizeof(long long) * k, cudaMemcpyHostToDevice,
+                                 g->stream));
+        DDP_CUDA(cudaMemcpyAsync(d->d_val, d->h_val[side], sizeof(uint2) * k, cudaMemcpyHostToDevice, g->stream));
         k_scatter_arcs<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(dst, d->d_slot, d->d_val, (int)k);
         DDP_CUDA(cudaGetLastError());  // stream-ordered; one synchronisation at the end
         dirty.clear();
         return DDP_OK;
     };
     auto rows = [&](std::vector<int32_t> &drow, std::vector<int32_t> &b, std::vector<int32_t> &e, int32_t *db,
-                    int32_t *de) -> int {
+                    int32_t *de, int side) -> int {
         if (drow.empty()) return DDP_OK;
         std::sort(drow.begin(), drow.end());
         drow.erase(std::unique(drow.begin(), drow.end()), drow.end());
@@ -486,22 +524,32 @@ int dyn_upload(ddp_graph *g) {
             DDP_CUDA(cudaMalloc(&d->d_rows, sizeof(int4) * k));
             d->rows_cap = k;
         }
-        DDP_CUDA(cudaMemcpyAsync(d->d_rows, r.data(), sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
+        if (k > d->h_rcap[side]) {
+            cudaFreeHost(d->h_rows[side]);
+            d->h_rows[side] = nullptr;
+            d->h_rcap[side] = 0;
+            DDP_CUDA(cudaHostAlloc(&d->h_rows[side], sizeof(int4) * k, cudaHostAllocDefault));
+            d->h_rcap[side] = k;
+        }
+        std::memcpy(d->h_rows[side], r.data(), sizeof(int4) * k);
+        DDP_CUDA(cudaMemcpyAsync(d->d_rows, d->h_rows[side], sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
         k_scatter_rows<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(db, de, d->d_rows, (int)k);
         DDP_CUDA(cudaGetLastError());
         drow.clear();
         return DDP_OK;
     };
-    int rc = scatter(m->dirty_arc, m->arc, g->d_arc);
-    if (!rc) rc = scatter(m->dirty_rarc, m->rarc, g->d_rarc);
-    if (!rc) rc = rows(m->dirty_row, m->beg, m->end, g->d_off, g->d_oend);
-    if (!rc) rc = rows(m->dirty_rrow, m->rbeg, m->rend, g->d_roff, g->d_roend);
-    // the device graph is current when this returns (other streams read it)
-    if (!rc) DDP_CUDA(cudaStreamSynchronize(g->stream));
+    int rc = scatter(m->dirty_arc, m->arc, g->d_arc, 0);
+    if (!rc) rc = scatter(m->dirty_rarc, m->rarc, g->d_rarc, 1);
+    if (!rc) rc = rows(m->dirty_row, m->beg, m->end, g->d_off, g->d_oend, 0);
+    if (!rc) rc = rows(m->dirty_rrow, m->rbeg, m->rend, g->d_roff, g->d_roend, 1);
+    // the device graph is current when this returns (other streams read it),
+    // unless the caller synchronises the graph's stream itself
+    if (!rc && sync) DDP_CUDA(cudaStreamSynchronize(g->stream));
     return rc;
 }
 
 static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
+    const bool one_cta = !initial && d->upd_grid == 1;
     ddp_graph *g = d->g;
     DevGraph G = graph_view(g);
     SearchParams P{d->s, d->t, d->o.delta > 0 ? (uint32_t)d->o.delta : std::max(1u, (g->wmin + g->wmax) / 4),
@@ -520,7 +568,11 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
     DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->bar_count, 0, 2 * sizeof(unsigned int), g->stream));
     DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->status, 0, sizeof(int), g->stream));
     void *args[] = {&G, &d->sa, &d->d_hops, &P, &A, &d->d_dc};
-    DDP_CUDA(cudaLaunchCooperativeKernel((const void *)k_dyn, dim3(d->grid), dim3(512), args, 0, g->stream));
+    if (one_cta)
+        DDP_CUDA(cudaLaunchKernel((const void *)k_dyn<CtaGroup>, dim3(1), dim3(512), args, 0, g->stream));
+    else
+        DDP_CUDA(cudaLaunchCooperativeKernel((const void *)k_dyn<GridGroup>, dim3(initial ? d->grid : d->upd_grid),
+                                             dim3(512), args, 0, g->stream));
     int32_t out[10];
     DDP_CUDA(cudaMemcpyAsync(out, d->d_out, sizeof(out), cudaMemcpyDeviceToHost, g->stream));
     DDP_CUDA(cudaStreamSynchronize(g->stream));
@@ -566,7 +618,7 @@ int dyn_graph_prepare(ddp_graph *g) {
 // Applies one update batch to the mirror with the reference's semantics and
 // uploads the touched slots.  ups receives the search-relevant updates.
 int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
-                    const uint32_t *w, std::vector<int4> &ups) {
+                    const uint32_t *w, std::vector<int4> &ups, bool sync) {
     g->update_count++;  // landmark distances no longer hold
     int rcp = dyn_graph_prepare(g);
     if (rcp) return rcp;
@@ -642,7 +694,7 @@ int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32
         if (w[i] < g->wmin) g->wmin = w[i];
         if (w[i] > g->wmax) g->wmax = w[i];
     }
-    return dyn_upload(g);
+    return dyn_upload(g, sync);
 }
 
 }  // namespace ddp
@@ -689,7 +741,7 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     DDP_CUDA(cudaMemsetAsync(d->sa.ctl, 0, sizeof(SearchCtl), g->stream));
     int per_sm = 0, sms = 0, dev = 0;
     cudaGetDevice(&dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dyn, 512, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dyn<GridGroup>, 512, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     // half the SMs by default: a batch repairs little, and fewer CTAs make
     // the grid barriers between repair steps cheaper (measured best on 1M
@@ -697,6 +749,12 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     const int coresident = std::max(1, per_sm) * std::max(1, sms);
     d->grid = std::min(coresident, std::max(1, sms / 2));
     if (d->o.grid > 0) d->grid = std::min(coresident, d->o.grid);
+    // update batches: the same grid as the initial search unless opts.group
+    // asks otherwise (1 = the one-CTA kernel).  On 1M nodes with 1000-update
+    // batches one CTA took 7.1 ms per batch against 1.23 ms on 76 CTAs: the
+    // resumed search needs the grid's parallelism more than it pays for the
+    // grid barriers.
+    d->upd_grid = d->o.group > 0 ? std::min(coresident, d->o.group) : d->grid;
     if (hkind == DDP_H_BFS_HOPS) {
         // exact reverse BFS from the target into the dynamic hop array
         ddp_heuristic *h = nullptr;
@@ -721,7 +779,9 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
     ddp_graph *g = d->g;
     std::lock_guard<std::mutex> lk(g->mu);
     std::vector<int4> ups;
-    int rc = dyn_graph_apply(g, nupd, flag, u, v, w, ups);
+    // no synchronisation after the graph scatters: k_dyn runs on the same
+    // stream, and dyn_launch synchronises it before returning
+    int rc = dyn_graph_apply(g, nupd, flag, u, v, w, ups, false);
     if (rc) return rc;
     const int32_t k = (int32_t)ups.size();
     if (k > d->upd_cap) {

@@ -50,7 +50,7 @@
 
 namespace ddp {
 int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
-                    const uint32_t *w, std::vector<int4> &ups);
+                    const uint32_t *w, std::vector<int4> &ups, bool sync = true);
 }
 
 // One graph version on the device (dynamic layout: row begin/end arrays).

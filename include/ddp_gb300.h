@@ -225,7 +225,9 @@ typedef struct ddp_dyn ddp_dyn;
  * DDP_H_BFS_HOPS) and keeps the search resident.  The graph switches to a
  * layout with growable rows; it stays usable by every other call and
  * ddp_graph_read_csr returns its current arcs.  One dynamic search per graph
- * at a time. */
+ * at a time.  opts.grid = CTAs of the initial search (0 = half the SMs);
+ * opts.group = CTAs of each update batch's repair and resumed search
+ * (0 or 1 = one CTA, block barriers; more = a cooperative grid). */
 int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind,
                    const ddp_opts *opts, ddp_dyn **out);
 /* Applies one update batch (DA_dyn_cpu.cu:1295-1326 Updates.txt lines):

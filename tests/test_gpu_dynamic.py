@@ -16,11 +16,11 @@ def _scratch_cost(O, off_ref, col, w, s, t, heuristic=True):
     return cost if found else 2147483647
 
 
-def _run(d, O, g, batches, s, t, hkind=None, check_csr_every=1):
+def _run(d, O, g, batches, s, t, hkind=None, check_csr_every=1, **opts):
     """g: CSR with a sentinel last node; batches: list of (flag,u,v,w)."""
     hkind = d.H_BFS_HOPS if hkind is None else hkind
     dg = d.DeviceGraph.from_csr(g)
-    dyn = d.DynamicSearch(dg, s, t, hkind)
+    dyn = d.DynamicSearch(dg, s, t, hkind, **opts)
     off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
     assert dyn.cost == _scratch_cost(O, off, col, w, s, t)
     for bi, (fl, uu, vv, ww) in enumerate(batches):
@@ -43,16 +43,18 @@ def _split(fl, u, v, w, per):
     return [(fl[i:i + per], u[i:i + per], v[i:i + per], w[i:i + per]) for i in range(0, len(fl), per)]
 
 
-def test_dynamic_random_batches(gpu, oracle):
+@pytest.mark.parametrize("group", [1, 8])
+def test_dynamic_random_batches(gpu, oracle, group):
     """The 1M-node update workload's shape at 1/50 scale (20k nodes, avg
     out-degree 10): inserts of new arcs and deletes of existing non-chain
-    arcs, weights in [1,1000]."""
+    arcs, weights in [1,1000].  Update batches on one CTA (the default) and
+    on a cooperative grid of 8 CTAs."""
     d = gpu
     base = d.gen_random_chain(20000, 10, 1, 1000, 303)
     fl, u, v, w = d.gen_updates(base, 25, 200, 100, 1, 1000, 304)
     g = base.with_sentinel()
     s, t = int(base.perm[0]), int(base.perm[-1])
-    _run(d, oracle, g, _split(fl, u, v, w, 200), s, t)
+    _run(d, oracle, g, _split(fl, u, v, w, 200), s, t, group=group)
 
 
 def test_dynamic_deletes_on_the_path(gpu, oracle):
