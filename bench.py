@@ -79,7 +79,7 @@ def workload_name(c):
 def args_parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=80)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", default="c4", choices=sorted(CONFIGS))
@@ -110,6 +110,8 @@ def args_parse():
                    help="offered Poisson rates (requests/s) of the serving leg ('' = skip)")
     p.add_argument("--serve-seconds", type=float, default=1.0, help="seconds of arrivals per serving rate")
     p.add_argument("--rates", default="", help="serving configs: offered rates to run (default: the config's)")
+    p.add_argument("--other-configs", default="c1,c2,c3",
+                   help="the batch run also measures these configurations (c1, c2, c3, c2dyn; '' = none)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -136,7 +138,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -420,7 +422,8 @@ def bench_single(a, c):
            "work": {"expanded": int(r.stats[0]), "scanned": int(r.stats[1]), "phases": int(r.stats[3])},
            "cpu_baseline": {"value": 1000 * osec, "unit": "ms/query", "cores": 1, "kind": "port",
                             "sample": "the same query, search loop only, position-map heap"}}
-    print(json.dumps(out), flush=True)
+    dg.close()
+    return out
 
 
 def bench_dynamic(a, c):
@@ -515,8 +518,9 @@ def bench_dynamic(a, c):
            "exact_on_sampled_batches": exact, "sampled_batches": sorted(sample),
            "exact_vs_oracle_all": fx["exact"] if fx else None, "oracle_fixture": fx,
            "invalidated_nodes_mean": float(np.mean(inval)), "costs_first_last": [costs[0], costs[-1]]}
-    print(json.dumps(out), flush=True)
     dyn.close()
+    dg.close()
+    return out
 
 
 def poisson_run(srv, rate, seconds, rng, endpoints, update_fn=None, update_ms=0):
@@ -668,11 +672,11 @@ def main():
     c = dict(CONFIGS[a.config])
     if a.config in ("c1", "c2"):
         if rank == 0:
-            bench_single(a, c)
+            print(json.dumps(bench_single(a, c)), flush=True)
         return
     if a.config in ("c3", "c2dyn"):
         if rank == 0:
-            bench_dynamic(a, c)
+            print(json.dumps(bench_dynamic(a, c)), flush=True)
         return
     if a.config in ("c5", "c5-small", "c4serve"):
         if rank == 0:
@@ -880,9 +884,20 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    dg.close()
+    if rank == 0 and world == 1 and a.other_configs:
+        # the other configurations, measured after the headline one, each
+        # checked against the oracle (its fixture where one exists)
+        others = {}
+        sub = argparse.Namespace(**vars(a))
+        sub.steps, sub.warmup = 5, 3
+        for name in [x.strip() for x in a.other_configs.split(",") if x.strip()]:
+            cc = dict(CONFIGS[name])
+            sub.config = name
+            others[name] = bench_single(sub, cc) if name in ("c1", "c2") else bench_dynamic(sub, cc)
+        out["other_configs"] = others
     if rank == 0:
         print(json.dumps(out), flush=True)
-    dg.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
