@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import argparse
 import json
+from types import SimpleNamespace
 import os
 import statistics
 import subprocess
@@ -99,11 +100,12 @@ def args_parse():
     p.add_argument("--landmarks", type=int, default=64, help="landmark count for --heuristic landmark")
     p.add_argument("--landmark-bits", type=int, default=8, choices=[16, 8],
                    help="landmark table entry width (rows of 2 x landmarks entries)")
-    p.add_argument("--heuristic", default="bidir", choices=["capped", "bfs", "zero", "landmark", "bidir"],
+    p.add_argument("--heuristic", default="bidir", choices=["capped", "bfs", "zero", "landmark", "bidir", "bidir-pot"],
                    help="landmark: ALT bound from --landmarks landmarks (table built once per graph); "
                         "capped: reverse-BFS hops stopped at max(4096, n/32) reached nodes (unreached nodes "
                         "get last level + 1); bfs: full reverse BFS; zero: h = 0; bidir: no heuristic, "
-                        "forward and reverse searches meet in the middle")
+                        "forward and reverse searches meet in the middle; bidir-pot: the same steered by "
+                        "average coordinate potentials (serving on the geometric graph)")
     p.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
     p.add_argument("--plain-sample", type=int, default=256, help="queries timed on plain single-query GA*")
     p.add_argument("--serve-rates", default="5000,10000,20000",
@@ -388,6 +390,9 @@ def bench_single(a, c):
     # the autotuner's space here: K for the whole-GPU phase-synchronous engine,
     # and the one-CTA asynchronous engine
     variants = [(f"grid K={K}", dict(K=K)) for K in Ks] + [("one-CTA async", dict(flags=d.OPT_ONE_CTA))]
+    # the maze also runs the one-CTA bidirectional A* (average Manhattan
+    # potentials) as a batch of one query
+    be_bi = d.BatchEngine(dg, d.H_BIDIR_MANHATTAN, grid=1) if a.config == "c2" else None
     for name, kw in variants:
         for _ in range(max(3, a.warmup)):
             r = dg.solve(s, t, h, **kw)
@@ -399,6 +404,20 @@ def bench_single(a, c):
         res[name] = (float(np.median(times)), r)
         assert cost is None or r.cost == cost, (name, r.cost, cost)
         cost = r.cost
+    if be_bi is not None:
+        S1, T1 = np.array([s], np.int32), np.array([t], np.int32)
+        for _ in range(max(3, a.warmup)):
+            be_bi.solve(S1, T1)
+        times = []
+        for _ in range(a.steps):
+            t0 = time.perf_counter()
+            cb, _ = be_bi.solve(S1, T1)
+            times.append(time.perf_counter() - t0)
+        assert int(cb[0]) == cost, ("bidirectional", int(cb[0]), cost)
+        res["one-CTA bidirectional A*"] = (float(np.median(times)),
+                                          SimpleNamespace(cost=int(cb[0]), path=be_bi.path(0),
+                                                          stats=be_bi.stats()[0][0]))
+        be_bi.close()
     bestK = min(res, key=lambda k: res[k][0])
     best_t, r = res[bestK]
     gs = g.with_sentinel()
@@ -580,7 +599,7 @@ def bench_serving(a, c):
     import ddp_gb300 as d
     from oracle import oracle as O
     fixed = "deg" in c
-    bid = a.heuristic == "bidir"  # else A* with the graph's bound (landmarks / Euclidean)
+    bid = a.heuristic in ("bidir", "bidir-pot")  # else A* with the graph's bound (landmarks / Euclidean)
     if fixed:
         g = d.gen_random_chain(c["n"], c["deg"], c["wmin"], c["wmax"], c["gseed"])
         dg = d.DeviceGraph.from_csr(g)
@@ -591,7 +610,7 @@ def bench_serving(a, c):
         g = d.gen_geometric(c["n"], c["k"], c["side"], c["wscale"], c["gseed"])
         dg = d.DeviceGraph.from_csr(g)
         dg.set_euclid(d.euclid_rho_fp(g))
-        hk = d.H_BIDIR if bid else d.H_EUCLID
+        hk = (d.H_BIDIR_EUCLID if a.heuristic == "bidir-pot" else d.H_BIDIR) if bid else d.H_EUCLID
     srv = d.Server(dg, hk, max_requests=1 << 22, grid=a.slots, block=a.block, delta=a.delta)
     rng = np.random.default_rng(c["gseed"] + 1)
     src = np.repeat(np.arange(g.n, dtype=np.int32), np.diff(g.off))
@@ -650,7 +669,8 @@ def bench_serving(a, c):
     out = {"metric": "A* serving queries/sec + p50/p99 latency (exact)", "value": best["served_qps"],
            "unit": "queries/s", "higher_is_better": True, "n_gpus": 1, "dtype": "int32",
            "data": "synthetic (seeded generators)",
-           "engine": {"method": "bidirectional" if bid else ("landmark A*" if fixed else "Euclidean A*")},
+           "engine": {"method": ("bidirectional A* (average Euclidean potentials)" if a.heuristic == "bidir-pot"
+                                 else "bidirectional") if bid else ("landmark A*" if fixed else "Euclidean A*")},
            "config": {"workload": (f"serving: {c['n']:,}-node random digraph (chain + uniform arcs), avg out-degree "
                                    f"{c['deg']}, w U[{c['wmin']},{c['wmax']}], "
                                    f"uniform random endpoints, Poisson arrivals, no updates") if fixed else

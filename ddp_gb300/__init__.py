@@ -25,6 +25,7 @@ import numpy as np
 from ._lib import DdpError, Opts, check, lib, ptr  # noqa: F401
 
 H_ZERO, H_BFS_HOPS, H_MANHATTAN, H_USER, H_BFS_CAPPED, H_EUCLID, H_LANDMARK, H_BIDIR = 0, 1, 2, 3, 4, 5, 6, 7
+H_BIDIR_EUCLID, H_BIDIR_MANHATTAN = 8, 9
 INF = 2147483647
 # per-query counters: expanded, scanned, relaxed, phases, bfs_reached,
 # bfs_scanned, far_scanned, touched

@@ -192,10 +192,80 @@ __device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B,
     return len;
 }
 
+// ---- potentials (bidirectional A*) ------------------------------------------
+// A potential pair gives, for node v, lower bounds pt(v) <= d(v, t) and
+// ps(v) <= d(s, v), each consistent (|p(u) - p(v)| <= w(u, v) on every arc).
+// The searches key their buckets by K_f(v) = 2 g_f(v) + pt(v) - ps(v) and
+// K_r(v) = 2 g_r(v) + ps(v) - pt(v) (the average potentials, doubled to stay
+// integral): both are non-negative and grow along arcs, so every proof of
+// the plain engine holds on the keys, with the stop rule a + b >= 2 mu and
+// pruning of a label g at v when g + pt(v) >= mu (forward) or
+// g + ps(v) >= mu (reverse).  PotNone keeps the keys equal to g.
+struct PotNone {
+    static constexpr bool on = false;
+    __device__ uint2 at(int) const { return make_uint2(0u, 0u); }
+};
+
+// floor(rho * |v - p|) in double precision: rho (16.16 fixed point, below
+// min w / length over live arcs) makes the exact real potential consistent,
+// and the rounding error (far below 1) cannot push a floor difference past
+// an integer weight.
+struct PotEuclid {
+    static constexpr bool on = true;
+    const int32_t *xy;
+    int2 s, t;
+    double rho;  // rho_fp / 65536
+    __device__ uint32_t d1(const int2 &q, const int2 &p) const {
+        const double dx = (double)q.x - p.x, dy = (double)q.y - p.y;
+        const double h = floor(rho * sqrt(dx * dx + dy * dy));
+        return h >= (double)(INF_G - 1) ? INF_G - 1 : (uint32_t)h;
+    }
+    __device__ uint2 at(int v) const {  // {pt(v), ps(v)}
+        const int2 q = __ldg(reinterpret_cast<const int2 *>(xy) + v);
+        return make_uint2(d1(q, t), d1(q, s));
+    }
+};
+
+// wmin x Manhattan distance: consistent on grids whose arcs join
+// 4-neighbours (length 1) with weights >= wmin.
+struct PotManhattan {
+    static constexpr bool on = true;
+    const int32_t *xy;
+    int2 s, t;
+    uint32_t wmin;
+    __device__ uint32_t d1(const int2 &q, const int2 &p) const {
+        const uint64_t h = (uint64_t)wmin * (uint64_t)(abs(q.x - p.x) + abs(q.y - p.y));
+        return h >= INF_G - 1 ? INF_G - 1 : (uint32_t)h;
+    }
+    __device__ uint2 at(int v) const {
+        const int2 q = __ldg(reinterpret_cast<const int2 *>(xy) + v);
+        return make_uint2(d1(q, t), d1(q, s));
+    }
+};
+
+// Bucket key of label g in direction dir, with pot = {pt(v), ps(v)}.
+template <class Pot>
+__device__ __forceinline__ uint32_t bi_key(uint32_t g, uint32_t dir, uint2 pot) {
+    if constexpr (!Pot::on) {
+        return g;
+    } else {
+        const int64_t k = 2 * (int64_t)g + (dir ? (int64_t)pot.y - (int64_t)pot.x : (int64_t)pot.x - (int64_t)pot.y);
+        return k <= 0 ? 0u : k >= 0xFFFFFFFFll ? 0xFFFFFFFFu : (uint32_t)k;
+    }
+}
+
+// The key every open key must stay below to matter (keys of labels at or
+// above mu's bound cannot lead to a shorter path).
+template <class Pot>
+__device__ __forceinline__ uint64_t bi_key_bound(uint32_t mu) {
+    return Pot::on ? 2 * (uint64_t)mu : (uint64_t)mu;
+}
+
 // ep: the slot's epoch for this query (never 0; units of other epochs read
 // as unreached).
+template <class Pot>
 __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, const SearchParams &P, uint32_t ep,
-                                      WarpRows *wrows, BiQ *sq) {
+                                      WarpRows *wrows, BiQ *sq, const Pot &pot) {
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
@@ -225,8 +295,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             *unit_ptr(st2, P.s, 0) = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
             *unit_ptr(st2, P.t, 1) = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
             ctl->touched = 2;
-            ring[0] = make_uint2((uint32_t)P.s, 0u);
-            ring[1] = make_uint2((uint32_t)P.t | DIR_BIT, 0u);
+            ring[0] = make_uint2((uint32_t)P.s, bi_key<Pot>(0u, 0u, pot.at(P.s)));
+            ring[1] = make_uint2((uint32_t)P.t | DIR_BIT, bi_key<Pot>(0u, 1u, pot.at(P.t)));
             sq->tail = 2;
             sq->pending = 2;
         }
@@ -239,14 +309,16 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
         return r0;
     }
 
-    // far piles hold {v | dir << 31, g}: the key is g
+    // ring and far entries hold {v | dir << 31, key}
     uint2 *fcur = reinterpret_cast<uint2 *>(B.f0), *falt = reinterpret_cast<uint2 *>(B.f1);
     uint2 *sf2 = reinterpret_cast<uint2 *>(wr.sf);  // staged far pushes
     int64_t nfar = 0;
     // the current bucket holds keys < T0 (forward) and < T1 (reverse); lo_d
     // is a lower bound of direction d's open keys when its last advance
     // moved nothing (the next advance jumps there)
-    uint32_t T0 = P.delta, T1 = P.delta;
+    // keys are doubled with potentials: so is the bucket width
+    const uint32_t dk = Pot::on ? 2 * P.delta : P.delta;
+    uint32_t T0 = sat_add(bi_key<Pot>(0u, 0u, pot.at(P.s)), dk), T1 = sat_add(bi_key<Pot>(0u, 1u, pot.at(P.t)), dk);
     uint32_t lo0 = 0, lo1 = 0;
     bool do_expand = true;
     unsigned long long n_exp = 0, n_scan = 0, n_rel = 0, n_first = 0;
@@ -319,10 +391,20 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 uint32_t gu = 0, ud = 0;
                 if (lane < n && en.x != RING_EMPTY) {
                     ud = en.x;
-                    gu = en.y;
+                    gu = en.y;  // the entry's key
                     const int u = (int)(ud & NODE_MASK);
                     const uint32_t dir = ud >> 31;
-                    if (unit_g(__ldcg(unit_ptr(st2, u, dir)), ep) == gu && gu < mu) {
+                    const uint32_t gl = unit_g(__ldcg(unit_ptr(st2, u, dir)), ep);
+                    bool cur = false;
+                    if constexpr (Pot::on) {
+                        // the entry is current when its key is the label's key
+                        cur = gl < INF_G && bi_key<Pot>(gl, dir, pot.at(u)) == gu &&
+                              (uint64_t)gu < bi_key_bound<Pot>(mu);
+                        gu = gl;
+                    } else {
+                        cur = gl == gu && gu < mu;
+                    }
+                    if (cur) {
                         const int r0 = dir ? row_begin(G.roff, G.roend, u) : row_begin(G.off, G.oend, u);
                         const int r1 = dir ? row_end(G.roff, G.roend, u) : row_end(G.off, G.oend, u);
                         rb = r0;
@@ -343,6 +425,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 for (int kb = 0; kb < total; kb += 32) {
                     const int k = kb + lane;
                     bool live = false, first = false;
+                    uint2 pv = make_uint2(0u, 0u);  // {pt(v), ps(v)}
                     int v = 0;
                     uint32_t ng = 0, dir = 0;
                     uint32_t uo = 0;
@@ -356,6 +439,14 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
                         live = v >= 0 && ng64 < (uint64_t)min(mu, INF_G);
                         ng = (uint32_t)ng64;
+                        if constexpr (Pot::on) {
+                            if (live) {
+                                // a path through v is at least g + the
+                                // bound of the other side
+                                pv = pot.at(v);
+                                live = ng64 + (dir ? pv.y : pv.x) < (uint64_t)mu;
+                            }
+                        }
                         if (live) {
                             // the node's record: both units, one sector
                             uf = __ldcg(unit_ptr(st2, v, 0));
@@ -397,7 +488,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                             }
                         }
                     }
-                    bool to_near = live && ng < (dir ? T1 : T0);
+                    const uint32_t nk = bi_key<Pot>(ng, dir, pv);
+                    bool to_near = live && nk < (dir ? T1 : T0);
                     bool to_far = live && !to_near;
                     if (live) n_rel++;
                     const uint32_t vd = (uint32_t)v | (dir << 31);
@@ -410,7 +502,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         if (lane == 0) atomicAdd(&sq->pending, kn);
                         __syncwarp();
                         if (c_loc + kn <= 64) {
-                            if (to_near) wr.sn[c_loc + rank_in] = make_uint2(vd, ng);
+                            if (to_near) wr.sn[c_loc + rank_in] = make_uint2(vd, nk);
                             c_loc += kn;
                         } else {
                             int p0 = 0;
@@ -420,7 +512,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                 if (to_near) {
                                     volatile unsigned long long *slot =
                                         reinterpret_cast<volatile unsigned long long *>(ring + p0 + rank_in);
-                                    *slot = ((unsigned long long)ng << 32) | vd;
+                                    *slot = ((unsigned long long)nk << 32) | vd;
                                 }
                             } else {
                                 if (lane == 0) atomicSub(&sq->pending, kn);
@@ -433,7 +525,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         if (dir) nf1++;
                         else nf0++;
                     }
-                    stage_push(to_far, make_uint2(vd, ng), sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
+                    stage_push(to_far, make_uint2(vd, nk), sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
                                ctl, 0);
                     if (first) n_first++;
                 }
@@ -480,8 +572,9 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             const int o0 = *(volatile int *)&sq->open_dir[0], o1 = *(volatile int *)&sq->open_dir[1];
             const bool adv0 = (int64_t)o0 <= 2 * (int64_t)o1 + 64;
             const bool adv1 = (int64_t)o1 <= 2 * (int64_t)o0 + 64;
-            const uint32_t Ts0 = adv0 ? sat_add(max(T0, lo0), P.delta) : T0;
-            const uint32_t Ts1 = adv1 ? sat_add(max(T1, lo1), P.delta) : T1;
+            const uint32_t Ts0 = adv0 ? sat_add(max(T0, lo0), dk) : T0;
+            const uint32_t Ts1 = adv1 ? sat_add(max(T1, lo1), dk) : T1;
+            const uint64_t kb = bi_key_bound<Pot>(mu);
             unsigned int kmin0 = 0xFFFFFFFFu, kmin1 = 0xFFFFFFFFu;
             int kp0 = 0, kp1 = 0, mv0 = 0, mv1 = 0;  // kept / moved per direction (this lane)
             int c_n = 0, c_f = 0;
@@ -492,7 +585,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 uint2 en = make_uint2(0u, 0u);
                 if (idx < nfar) {
                     en = __ldcg(fcur + idx);
-                    if (en.y < mu) {
+                    if ((uint64_t)en.y < kb) {
                         const bool rev = (en.x >> 31) != 0;
                         if (en.y < (rev ? Ts1 : Ts0)) to_near = true;
                         else keep = true;
@@ -566,7 +659,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             }
             // an empty direction, or a + b >= mu: mu is the distance.  The
             // ring entries just moved hold the direction minima too.
-            if (a == 0xFFFFFFFFu || b == 0xFFFFFFFFu || (uint64_t)a + b >= (uint64_t)mu2) {
+            if (a == 0xFFFFFFFFu || b == 0xFFFFFFFFu || (uint64_t)a + b >= bi_key_bound<Pot>(mu2)) {
                 // the ring may hold moved entries nobody will pop: clear it
                 for (int i = threadIdx.x; i < m; i += blockDim.x) ring[i].x = RING_EMPTY;
                 break;

@@ -407,7 +407,7 @@ int launch(ddp_server *s) {
     A.work = s->d_work;
     A.status = s->d_work + 1;
     A.delta = s->o.delta > 0                ? (uint32_t)s->o.delta
-              : s->hkind == DDP_H_BIDIR ? auto_delta_bidir(s->g)
+              : is_bidir_kind(s->hkind) ? auto_delta_bidir(s->g)
                                         : auto_delta(s->g);
     A.K = s->o.K;
     A.bfs_budget = s->hkind == DDP_H_BFS_CAPPED ? bfs_budget(s->g->n) : 0;
@@ -466,11 +466,12 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
         return fail(DDP_ERR_INVALID, "bad serving arguments");
     *out = nullptr;
     if (hkind != DDP_H_ZERO && hkind != DDP_H_BFS_HOPS && hkind != DDP_H_BFS_CAPPED && hkind != DDP_H_MANHATTAN &&
-        hkind != DDP_H_EUCLID && hkind != DDP_H_LANDMARK && hkind != DDP_H_BIDIR)
+        hkind != DDP_H_EUCLID && hkind != DDP_H_LANDMARK && !is_bidir_kind(hkind))
         return fail(DDP_ERR_INVALID, "unsupported heuristic kind for serving");
     if (hkind == DDP_H_LANDMARK && !graph_view(g).lm)
         return fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)");
-    if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID) && !g->d_xy)
+    if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID || hkind == DDP_H_BIDIR_EUCLID ||
+         hkind == DDP_H_BIDIR_MANHATTAN) && !g->d_xy)
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_server *s = new ddp_server();
     s->g = g;
@@ -492,7 +493,7 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
     const int hops = (hkind == DDP_H_BFS_HOPS || hkind == DDP_H_BFS_CAPPED ? SLOT_HOPS : 0) |
-                     (hkind == DDP_H_BIDIR ? SLOT_PAIR : 0);  // slot layout
+                     (is_bidir_kind(hkind) ? SLOT_PAIR : 0);  // slot layout
     // queue capacities: what each slot's share of half the free memory
     // holds after its state, up to the batch engine's sizes (n + 4096 near,
     // 2n + 4096 far); at least 64k.  A request that still outgrows its slot
@@ -606,7 +607,7 @@ int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int
             ddp_heuristic *h = nullptr;
             // (the bidirectional kind has no single-query form: Dijkstra
             // order gives the same cost)
-            const int hk = s->hkind == DDP_H_BIDIR ? DDP_H_ZERO : s->hkind;
+            const int hk = is_bidir_kind(s->hkind) ? DDP_H_ZERO : s->hkind;
             int rc = ddp_heuristic_build(s->g, s->h_T[i], hk, nullptr, nullptr, &h);
             if (rc) return rc;
             ddp_query *q = nullptr;

@@ -294,7 +294,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
                 *epoch = ep;
                 ctl->tag = ep << 8;
             }
-            if (HK == 5) {
+            if (bidir_hk(HK)) {
                 // per-query epoch of the slot's records (0 = never used);
                 // tag 0 asks for the records to be cleared once the
                 // 32-bit epoch wraps
@@ -305,7 +305,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             t0 = global_ns();
         }
         grp.sync();
-        if (HK == 5 && *(volatile uint32_t *)&ctl->tag == 0) {
+        if (bidir_hk(HK) && *(volatile uint32_t *)&ctl->tag == 0) {
             for (size_t i = grp.rank(); i < 4 * (size_t)G0.n; i += grp.size()) B.state[i] = 0ull;
             grp.sync();
             if (grp.rank() == 0) ctl->tag = 1;
@@ -359,15 +359,26 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             r = slot_search(grp, G, B, HeurEuclid{G.xy, tp.x, tp.y, G.rho_fp}, P, wrows, sq, async);
         } else if (HK == 4) {
             r = slot_search(grp, G, B, HeurALT{G.lm, G.lm_L, G.lm_scale, t, G.lm_bits}, P, wrows, sq, async);
-        } else if (HK == 5) {
+        } else if (bidir_hk(HK)) {
             // bidirectional: one-CTA slots only (the host never launches
-            // this kind with wider slots)
-            if constexpr (std::is_same<Grp, CtaGroup>::value)
-                r = run_bidir_cta(G, B, P, *(volatile uint32_t *)&ctl->tag, wrows, bq);
+            // these kinds with wider slots)
+            if constexpr (std::is_same<Grp, CtaGroup>::value) {
+                const uint32_t ep = *(volatile uint32_t *)&ctl->tag;
+                if constexpr (HK == 5) {
+                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{});
+                } else {
+                    const int2 sp = reinterpret_cast<const int2 *>(G.xy)[s];
+                    const int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
+                    if constexpr (HK == 6)
+                        r = run_bidir_cta(G, B, P, ep, wrows, bq, PotEuclid{G.xy, sp, tp, G.rho_fp / 65536.0});
+                    else
+                        r = run_bidir_cta(G, B, P, ep, wrows, bq, PotManhattan{G.xy, sp, tp, G.wmin});
+                }
+            }
         } else {
             r = slot_search(grp, G, B, HeurZero{}, P, wrows, sq, async);
         }
-        if ((async || HK == 5) && (*(volatile int *)&ctl->status & (ST_OVERFLOW | ST_TIMEOUT))) {
+        if ((async || bidir_hk(HK)) && (*(volatile int *)&ctl->status & (ST_OVERFLOW | ST_TIMEOUT))) {
             // an aborted asynchronous search may leave ring slots written:
             // clear the ring so the slot's next search starts clean
             for (int64_t i = grp.rank(); i < B.cap_q; i += grp.size()) B.q0[i].x = RING_EMPTY;
@@ -377,7 +388,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             const int st = ctl->status;
             int32_t len = 0;
             if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths) {
-                if (HK == 5)
+                if (bidir_hk(HK))
                     len = write_path_bidir(G, B, ctl->tag, s, t, bq->mu, A.paths + (size_t)q * A.path_cap,
                                            A.path_cap, &ctl->status);
                 else
@@ -415,7 +426,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         }
         grp.sync();
         const int cnt = *(volatile int *)&ctl->touched;
-        if (HK != 5) {  // paired records need no reset: the next query has a new epoch
+        if (!bidir_hk(HK)) {  // paired records need no reset: the next query has a new epoch
             for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
         }
         grp.sync();
@@ -557,7 +568,7 @@ __device__ void service_loop(const BatchArgs &A) {
 #define DDP_BIDIR_MIN_BLOCKS 3
 #endif
 template <int HK>
-__global__ void __launch_bounds__(512, (HK == 5 ? DDP_BIDIR_MIN_BLOCKS : 2)) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
+__global__ void __launch_bounds__(512, (bidir_hk(HK) ? DDP_BIDIR_MIN_BLOCKS : 2)) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
     __shared__ WarpRows wrows[MAX_WARPS];
     __shared__ CtaQ sq;
     __shared__ BiQ bq;
@@ -624,13 +635,13 @@ static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CA
 
 // Slot layout a batch heuristic kind needs.
 static int slot_kind(int hkind) {
-    return (is_bfs_kind(hkind) ? SLOT_HOPS : 0) | (hkind == DDP_H_BIDIR ? SLOT_PAIR : 0);
+    return (is_bfs_kind(hkind) ? SLOT_HOPS : 0) | (is_bidir_kind(hkind) ? SLOT_PAIR : 0);
 }
 
 // Heuristic kind of the single-query engine that re-runs a batch query
 // (the bidirectional form has no single-query counterpart: plain Dijkstra
 // order gives the same cost).
-static int rerun_kind(int hkind) { return hkind == DDP_H_BIDIR ? DDP_H_ZERO : hkind; }
+static int rerun_kind(int hkind) { return is_bidir_kind(hkind) ? DDP_H_ZERO : hkind; }
 
 // The batch kernel instance for a heuristic kind.
 static const void *batch_kernel(int hkind) {
@@ -639,6 +650,8 @@ static const void *batch_kernel(int hkind) {
     if (hkind == DDP_H_EUCLID) return (const void *)k_batch<3>;
     if (hkind == DDP_H_LANDMARK) return (const void *)k_batch<4>;
     if (hkind == DDP_H_BIDIR) return (const void *)k_batch<5>;
+    if (hkind == DDP_H_BIDIR_EUCLID) return (const void *)k_batch<6>;
+    if (hkind == DDP_H_BIDIR_MANHATTAN) return (const void *)k_batch<7>;
     return (const void *)k_batch<0>;
 }
 
@@ -1260,7 +1273,7 @@ static bool batch_args(ddp_batch *b, int32_t n, const int32_t *dS, const int32_t
     A.work = b->d_work;
     A.status = b->d_status;
     A.delta = b->o.delta > 0                ? (uint32_t)b->o.delta
-              : b->hkind == DDP_H_BIDIR ? auto_delta_bidir(b->g)
+              : is_bidir_kind(b->hkind) ? auto_delta_bidir(b->g)
                                         : auto_delta(b->g);
     A.bfs_budget = b->hkind == DDP_H_BFS_CAPPED ? bfs_budget(b->g->n) : 0;
     A.K = b->o.K;
@@ -1311,12 +1324,13 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     if (!g || !out) return fail(DDP_ERR_INVALID, "null argument");
     *out = nullptr;
     if (hkind != DDP_H_ZERO && !is_bfs_kind(hkind) && hkind != DDP_H_MANHATTAN && hkind != DDP_H_EUCLID &&
-        hkind != DDP_H_LANDMARK && hkind != DDP_H_BIDIR)
+        hkind != DDP_H_LANDMARK && !is_bidir_kind(hkind))
         return fail(DDP_ERR_INVALID,
                     "batch heuristic must be ZERO, BFS_HOPS, BFS_CAPPED, MANHATTAN, EUCLID, LANDMARK or BIDIR");
     if (hkind == DDP_H_LANDMARK && !graph_view(g).lm)
         return fail(DDP_ERR_INVALID, "no current landmark table (ddp_landmarks_build)");
-    if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID) && !g->d_xy)
+    if ((hkind == DDP_H_MANHATTAN || hkind == DDP_H_EUCLID || hkind == DDP_H_BIDIR_EUCLID ||
+         hkind == DDP_H_BIDIR_MANHATTAN) && !g->d_xy)
         return fail(DDP_ERR_INVALID, "graph has no coordinates (ddp_graph_set_coords)");
     ddp_batch *b = new ddp_batch();
     b->g = g;
@@ -1334,7 +1348,7 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     // slots: occupancy-limited, then memory-limited (half of free memory)
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(hkind), b->block, 0);
-    b->group = hkind == DDP_H_BIDIR ? 1 : std::max(1, b->o.group);  // bidirectional slots are one CTA
+    b->group = is_bidir_kind(hkind) ? 1 : std::max(1, b->o.group);  // bidirectional slots are one CTA
     const int coresident = std::max(1, per_sm) * sm_count();
     if (b->group > coresident) b->group = coresident;
     int nslots = coresident / b->group;
@@ -1342,7 +1356,7 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     // the bidirectional ring holds one bucket and spills to the far pile
     // when full, so it needs far less than a node count
     const int64_t cap = b->o.queue_cap > 0      ? b->o.queue_cap
-                        : hkind == DDP_H_BIDIR ? std::min<int64_t>((int64_t)g->n + 4096, 1 << 18)
+                        : is_bidir_kind(hkind) ? std::min<int64_t>((int64_t)g->n + 4096, 1 << 18)
                                                 : (int64_t)g->n + 4096;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);

@@ -78,6 +78,13 @@ struct BatchArgs {
     int *inflight;                // per buffer: searches running on it (host memory)
 };
 
+// The bidirectional batch kinds, and their k_batch instances (5: no
+// potential, 6: Euclidean, 7: Manhattan potentials).
+inline bool is_bidir_kind(int k) {
+    return k == DDP_H_BIDIR || k == DDP_H_BIDIR_EUCLID || k == DDP_H_BIDIR_MANHATTAN;
+}
+constexpr bool bidir_hk(int hk) { return hk >= 5 && hk <= 7; }
+
 // Slot kinds (bits): a per-target hop array; paired forward/reverse state.
 enum { SLOT_HOPS = 1, SLOT_PAIR = 2 };
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind);

@@ -72,7 +72,7 @@ int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *source
     };
     // 1. slot shape (bidirectional slots are one CTA)
     const int shapes[][2] = {{1, 512}, {1, 256}, {2, 512}, {4, 512}, {8, 512}, {19, 512}};
-    const int nshapes = hkind == DDP_H_BIDIR ? 2 : 6;
+    const int nshapes = is_bidir_kind(hkind) ? 2 : 6;
     for (int si = 0; si < nshapes; si++) {
         const auto &sh = shapes[si];
         ddp_opts o = b0;
@@ -85,7 +85,7 @@ int ddp_batch_tune(ddp_graph *g, int32_t hkind, int32_t n, const int32_t *source
     }
     // 2. bucket width: half and twice the automatic one, then further steps
     //    of 2/3 (or 3/2) while the winning direction keeps winning
-    const uint32_t d0 = hkind == DDP_H_BIDIR ? auto_delta_bidir(g) : auto_delta(g);
+    const uint32_t d0 = is_bidir_kind(hkind) ? auto_delta_bidir(g) : auto_delta(g);
     const ddp_opts shape = top_o;
     uint32_t best_d = d0;
     for (uint32_t dv : {d0 / 2, d0 * 2}) {

@@ -68,11 +68,17 @@ enum ddp_heuristic_kind {
                             reference counterpart (the reference only has
                             bfs_hx.cu hop counts, which carry little on random
                             graphs)                                           */
-    DDP_H_BIDIR = 7      /* batch and serving only: no heuristic; a forward
+    DDP_H_BIDIR = 7,     /* batch and serving only: no heuristic; a forward
                             search from s and a reverse search from t meet
                             in the middle (bidirectional Dijkstra).  No
                             table, so it stays valid under updates.  No
                             reference counterpart                             */
+    DDP_H_BIDIR_EUCLID = 8,    /* DDP_H_BIDIR steered by average Euclidean
+                                  potentials (bidirectional A*): coordinates
+                                  and ddp_graph_set_euclid's scale          */
+    DDP_H_BIDIR_MANHATTAN = 9  /* DDP_H_BIDIR steered by average Manhattan
+                                  potentials (x min weight): grids whose arcs
+                                  join 4-neighbours                          */
 };
 
 typedef struct ddp_graph ddp_graph;         /* device-resident CSR + reverse CSR */
@@ -172,8 +178,9 @@ int ddp_query_free(ddp_query *q);
  *      reference solves one (s,t) per process, GA_v2.cu:301-305) --------- */
 /* hkind: DDP_H_ZERO, DDP_H_BFS_HOPS / DDP_H_BFS_CAPPED (per target, built
  * inside the batch kernel), DDP_H_MANHATTAN, DDP_H_EUCLID (coordinates),
- * DDP_H_LANDMARK (ddp_landmarks_build first) or DDP_H_BIDIR (one-CTA
- * slots, twice the per-slot state).  opts: group = CTAs per slot
+ * DDP_H_LANDMARK (ddp_landmarks_build first) or DDP_H_BIDIR,
+ * DDP_H_BIDIR_EUCLID, DDP_H_BIDIR_MANHATTAN (one-CTA slots, 32 bytes per
+ * node of slot state).  opts: group = CTAs per slot
  * (1 = the asynchronous one-CTA engine), block, K, delta, grid = slot cap;
  * ddp_batch_tune picks them.  A query whose search outgrew
  * its slot's queues reports cost -1 from ddp_batch_solve_device;

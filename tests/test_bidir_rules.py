@@ -43,31 +43,50 @@ def _dijkstra(n, off, col, w, s, t):
     return INF
 
 
-def bidir(n, fw, rv, s, t, delta, rng, ring_cap=1 << 30):
+def bidir(n, fw, rv, s, t, delta, rng, ring_cap=1 << 30, pot=None):
     """fw, rv = (off, col, w) of the graph and of its reverse.  A split
-    moves at most ring_cap entries to the bucket; the rest stay in far."""
+    moves at most ring_cap entries to the bucket; the rest stay in far.
+    pot = (pt, ps): consistent lower bounds of d(v, t) and d(s, v); keys are
+    then 2g + pt - ps (forward) and 2g + ps - pt (reverse), the stop rule
+    a + b >= 2 mu, and a label g is pruned when g + the other side's bound
+    reaches mu.  Without pot, keys are g."""
     if s == t:
         return 0, [s]
+    if pot is None:
+        def key(g, v, dr):
+            return g
+        bound = lambda m: m
+        other = lambda v, dr: 0
+        dk = delta
+    else:
+        pt, ps = pot
+
+        def key(g, v, dr):
+            return 2 * g + (int(ps[v]) - int(pt[v]) if dr else int(pt[v]) - int(ps[v]))
+        bound = lambda m: 2 * m
+        other = lambda v, dr: int(ps[v]) if dr else int(pt[v])
+        dk = 2 * delta
     lab = [[INF] * n, [INF] * n]
     par = [[-1] * n, [-1] * n]
     lab[0][s] = 0
     lab[1][t] = 0
     mu, mux = INF, -1
-    near = [(s, 0, 0), (t, 1, 0)]
+    near = [(s, 0, key(0, s, 0)), (t, 1, key(0, t, 1))]
     far = []
-    Td = [delta, delta]   # per-direction thresholds of the current bucket
+    Td = [key(0, s, 0) + dk, key(0, t, 1) + dk]   # per-direction thresholds of the current bucket
     lo = [0, 0]           # jump target of a direction whose advance moved nothing
     expand = True
     while True:
         if expand:
             while near:
-                u, dr, g = near.pop(rng.randrange(len(near)))
-                if lab[dr][u] != g or g >= mu:
+                u, dr, kk = near.pop(rng.randrange(len(near)))
+                g = lab[dr][u]
+                if g >= INF or key(g, u, dr) != kk or kk >= bound(mu):
                     continue
                 off, col, w = fw if dr == 0 else rv
                 for k in range(off[u], off[u + 1]):
                     v, ng = int(col[k]), g + int(w[k])
-                    if ng >= min(mu, INF):
+                    if ng >= min(mu, INF) or ng + other(v, dr) >= mu:
                         continue
                     go = lab[1 - dr][v]
                     if go < INF and ng + go < mu:
@@ -75,14 +94,15 @@ def bidir(n, fw, rv, s, t, delta, rng, ring_cap=1 << 30):
                     if ng < lab[dr][v]:
                         lab[dr][v] = ng
                         par[dr][v] = u
-                        (near if ng < Td[dr] else far).append((v, dr, ng))
+                        nk = key(ng, v, dr)
+                        (near if nk < Td[dr] else far).append((v, dr, nk))
         # balance: advance a direction while its open set is not much larger
         opn = [sum(1 for e in far if e[1] == d) for d in (0, 1)]
         adv = [opn[0] <= 2 * opn[1] + 64, opn[1] <= 2 * opn[0] + 64]
-        Ts = [max(Td[d], lo[d]) + delta if adv[d] else Td[d] for d in (0, 1)]
+        Ts = [max(Td[d], lo[d]) + dk if adv[d] else Td[d] for d in (0, 1)]
         moved, kept, mins, nmoved = [], [], [INF, INF], [0, 0]
-        for (v, dr, g) in far:
-            if g >= mu:
+        for (v, dr, g) in far:   # g: the entry's key
+            if g >= bound(mu):
                 continue
             if g < Ts[dr] and len(moved) < ring_cap:
                 moved.append((v, dr, g))
@@ -92,7 +112,7 @@ def bidir(n, fw, rv, s, t, delta, rng, ring_cap=1 << 30):
             mins[dr] = min(mins[dr], g)
         far = kept
         a, b = mins
-        if a == INF or b == INF or a + b >= mu:
+        if a == INF or b == INF or a + b >= bound(mu):
             break
         lo = [mins[d] if adv[d] and nmoved[d] == 0 else 0 for d in (0, 1)]
         Td = Ts
@@ -175,3 +195,36 @@ def test_bidir_rules_grid():
         assert got == want
         if want < INF:
             assert _path_weight(fw, path) == want
+
+
+@pytest.mark.parametrize("seed,delta", [(11, 3), (12, 40), (13, 400)])
+def test_bidir_rules_euclidean_potentials(seed, delta):
+    """Points in a square joined to near neighbours, w = ceil(length); the
+    potentials floor(rho |v - t|) and floor(rho |s - v|) with rho <= w /
+    length on every arc are consistent, so the keyed rules stay exact."""
+    r = np.random.default_rng(seed)
+    n = 700
+    xy = r.integers(0, 10000, (n, 2))
+    us, vs, ws = [], [], []
+    for a in range(n):
+        d2 = ((xy - xy[a]) ** 2).sum(1)
+        for b in np.argsort(d2)[1:6]:
+            ln = float(np.sqrt(d2[b]))
+            us += [a, b]
+            vs += [b, a]
+            ws += [int(np.ceil(ln)) + int(r.integers(0, 50))] * 2
+    u, v, w = np.array(us), np.array(vs), np.array(ws, np.int64)
+    fw = _csr(n, u, v, w)
+    rv = _csr(n, v, u, w)
+    ln = np.sqrt(((xy[u] - xy[v]) ** 2).sum(1))
+    rho = float((w / np.maximum(ln, 1e-9)).min()) * (1 - 1e-9)
+    rng = random.Random(seed)
+    for q in range(40):
+        s, t = (int(x) for x in r.integers(0, n, 2))
+        pt = np.floor(rho * np.sqrt(((xy - xy[t]) ** 2).sum(1))).astype(np.int64)
+        ps = np.floor(rho * np.sqrt(((xy - xy[s]) ** 2).sum(1))).astype(np.int64)
+        want = _dijkstra(n, *fw, s, t)
+        got, path = bidir(n, fw, rv, s, t, delta, rng, pot=(pt, ps))
+        assert got == want, (s, t)
+        if want < INF:
+            assert path[0] == s and path[-1] == t and _path_weight(fw, path) == want

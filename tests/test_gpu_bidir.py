@@ -201,3 +201,93 @@ def test_bidir_serving_with_updates(gpu, oracle):
         assert costs[k] == want, (int(ids[k]), int(ver[k]))
     srv.close()
     dg.close()
+
+
+@pytest.mark.parametrize("rows,cols,wall,seed", [(200, 300, 0.25, 51), (120, 120, 0.35, 52)])
+def test_bidir_manhattan_potentials_maze(gpu, oracle, rows, cols, wall, seed):
+    """Bidirectional A* with average Manhattan potentials on mazes: costs
+    against the oracle, every path valid; the corner-to-corner query too."""
+    d = gpu
+    m = d.gen_maze(rows, cols, wall, seed)
+    dg = d.DeviceGraph.from_csr(m)
+    S, T = _pairs(m.n, 96, seed + 1)
+    S[10], T[10] = 0, m.n - 1
+    want = _oracle_costs(oracle, m, S, T)
+    be = d.BatchEngine(dg, d.H_BIDIR_MANHATTAN)
+    for _ in range(2):
+        cost, plen = be.solve(S, T)
+        _check(oracle, be, m, S, T, cost, want, plen)
+    # the potentials only steer the search: it expands fewer nodes than the
+    # plain bidirectional search on the long query
+    st_pot = be.stats()[0][10, 0]
+    bz = d.BatchEngine(dg, d.H_BIDIR)
+    bz.solve(S, T)
+    assert st_pot < bz.stats()[0][10, 0]
+    bz.close()
+    be.close()
+    dg.close()
+
+
+def _geo(d, n, seed):
+    g = d.gen_geometric(n, 6, 1 << 20, 100000, seed)
+    dg = d.DeviceGraph.from_csr(g)
+    dg.set_euclid(d.euclid_rho_fp(g))
+    return g, dg
+
+
+def test_bidir_euclid_potentials_geometric(gpu, oracle):
+    d = gpu
+    g, dg = _geo(d, 30000, 61)
+    S, T = _pairs(g.n, 200, 62)
+    want = _oracle_costs(oracle, g, S, T)
+    be = d.BatchEngine(dg, d.H_BIDIR_EUCLID)
+    cost, plen = be.solve(S, T)
+    _check(oracle, be, g, S, T, cost, want, plen)
+    expanded_pot = be.stats()[0][:, 0].sum()
+    bz = d.BatchEngine(dg, d.H_BIDIR)
+    bz.solve(S, T)
+    assert expanded_pot < bz.stats()[0][:, 0].sum()
+    bz.close()
+    be.close()
+    dg.close()
+
+
+def test_bidir_euclid_serving_with_updates(gpu, oracle):
+    """Weight changes x[0.5, 2] (the Euclidean scale drops), deletes and
+    inserts while searches run: each answer equals the oracle on the graph
+    version it reports."""
+    d = gpu
+    g, dg = _geo(d, 20000, 71)
+    srv = d.Server(dg, d.H_BIDIR_EUCLID, max_requests=4096, versions=3, grid=32)
+    rng = np.random.default_rng(72)
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    versions = [g]
+    submitted = []
+    for rnd in range(4):
+        S = rng.integers(0, g.n, 40).astype(np.int32)
+        T = rng.integers(0, g.n, 40).astype(np.int32)
+        srv.submit(S, T)
+        submitted += list(zip(S.tolist(), T.tolist()))
+        src = np.repeat(np.arange(len(off)), np.diff(np.append(off, len(col))))
+        live = np.flatnonzero(col >= 0)
+        pick = rng.choice(live, 60, replace=False)
+        fl, uu, vv, ww = [], [], [], []
+        for j in pick[:40]:
+            fl.append(2); uu.append(int(src[j])); vv.append(int(col[j]))
+            ww.append(max(1, int(round(w[j] * rng.uniform(0.5, 2.0)))))
+        for j in pick[40:50]:
+            fl.append(0); uu.append(int(src[j])); vv.append(int(col[j])); ww.append(0)
+        for j in pick[50:60]:
+            fl.append(1); uu.append(int(col[j])); vv.append(int(src[j])); ww.append(int(w[j]))
+        srv.update(fl, uu, vv, ww)
+        off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, uu, vv, ww)
+        versions.append(d.CSR(g.n, np.append(off, len(col)).astype(np.int32), col, w, xy=g.xy))
+    ids, costs, lat, ver = srv.drain()
+    assert len(ids) == len(submitted)
+    for k in range(len(ids)):
+        s_, t_ = submitted[int(ids[k])]
+        gv = versions[int(ver[k])]
+        want = _oracle_costs(oracle, gv, np.array([s_], np.int32), np.array([t_], np.int32))[0]
+        assert costs[k] == want, (int(ids[k]), int(ver[k]))
+    srv.close()
+    dg.close()
