@@ -90,6 +90,8 @@ def args_parse():
     p.add_argument("--delta", type=int, default=0)
     p.add_argument("--K", type=int, default=0)
     p.add_argument("--queue-cap", type=int, default=0, help="entries per slot queue (0 = automatic)")
+    p.add_argument("--hash", action="store_true",
+                   help="bidirectional slots keep their closed set in a hash table (DDP_OPT_HASH)")
     p.add_argument("--dyn-group", type=int, default=0,
                    help="dynamic configs: CTAs of each update batch (0/1 = one CTA, more = cooperative grid)")
     p.add_argument("--group", type=int, default=19, help="CTAs per query slot (with --no-tune)")
@@ -734,7 +736,8 @@ def main():
         l0 = time.perf_counter()
         dg.build_landmarks(lm, seed=c["gseed"], bits=a.landmark_bits)
         lm_s = time.perf_counter() - l0
-    opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group, queue_cap=a.queue_cap)
+    opts = dict(grid=a.slots, block=a.block, delta=a.delta, K=a.K, group=a.group, queue_cap=a.queue_cap,
+                flags=d.OPT_HASH if a.hash else 0)
     tuned = None
     if not a.no_tune:
         # autotuner on random queries (not the measured pairs), outside the timed region
@@ -743,10 +746,13 @@ def main():
         tS = trng.integers(0, g.n, ns).astype(np.int32)
         tT = trng.integers(0, g.n, ns).astype(np.int32)
         u0 = time.perf_counter()
-        best, tq, ntr = d.tune_batch(dg, hkind, tS, tT, grid=a.slots, stream=stream.cuda_stream)
+        best, tq, ntr = d.tune_batch(dg, hkind, tS, tT, grid=a.slots, stream=stream.cuda_stream,
+                                     flags=d.OPT_HASH if a.hash else 0)
         tuned = {"options": best, "sample_qps": tq, "trials": ntr, "sample": int(ns),
                  "seconds": time.perf_counter() - u0}
         opts = dict(best)
+        if a.hash:
+            opts["flags"] = d.OPT_HASH
     be = d.BatchEngine(dg, hkind, stream=stream.cuda_stream, **opts)
     dS = torch.from_numpy(S).to(dev)
     dT = torch.from_numpy(T).to(dev)
@@ -875,7 +881,8 @@ def main():
                    "landmark_bits": a.landmark_bits if lm else None,
                    "landmark_build_s": lm_s, "autotuner": tuned,
                    "slots": info["slots"], "block": info["block"], "K": opts["K"], "group": info["group"],
-                   "queue_cap": info["queue_cap"], "delta": opts["delta"] or "auto"},
+                   "queue_cap": info["queue_cap"], "delta": opts["delta"] or "auto",
+                   "closed_set": "hash table per slot" if a.hash else "one record per node per slot"},
         "exact_vs_oracle_all": fixture["exact"] if fixture else None,
         "oracle_fixture": fixture,
         "latency_ms": {"p50": float(np.percentile(lat_complete, 50)), "p99": float(np.percentile(lat_complete, 99)),

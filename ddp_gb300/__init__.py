@@ -333,7 +333,7 @@ def write_updates_text(path: str, batches) -> None:
 
 # ---------------------------------------------------------------------------
 # device objects
-OPT_SYNC, OPT_ONE_CTA = 1, 2
+OPT_SYNC, OPT_ONE_CTA, OPT_HASH = 1, 2, 4
 
 
 def _opts(K=0, delta=0, block=0, grid=0, queue_cap=0, stream=None, group=0, flags=0) -> Opts:

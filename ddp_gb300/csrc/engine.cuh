@@ -71,6 +71,8 @@ struct SlotBufs {
     uint32_t *hops;             // n: per-target hop heuristic (may be null)
     SearchCtl *ctl;
     int64_t cap_q, cap_f;
+    int64_t swords;  // 64-bit words of the state array
+    int hbits;       // hashed records: log2 of the table size (0: one record per node)
 };
 
 // ---- groups ------------------------------------------------------------------

@@ -147,8 +147,66 @@ __device__ __forceinline__ uint4 cas_unit(uint4 *addr, const uint4 &cmp, const u
     return make_uint4((uint32_t)o0, (uint32_t)(o0 >> 32), (uint32_t)o1, (uint32_t)(o1 >> 32));
 }
 
+// ---- record layouts ----------------------------------------------------------
+// A layout maps node v to its record (two units, forward then reverse).
+// find(v) returns the record or null when v has none this query; claim(v)
+// returns it, creating it if needed (null when the table is full).
+// keyw(v) is the forward unit's w field: 0 for dense records, the node id
+// for hashed ones.
+
+// One record per node, at index v (the slot's state array holds n).
+struct RecDense {
+    static constexpr bool hashed = false;
+    unsigned long long *st;
+    __device__ uint4 *find(int v, uint32_t) const { return unit_ptr(st, v, 0); }
+    __device__ uint4 *claim(int v, uint32_t) const { return unit_ptr(st, v, 0); }
+    __device__ uint32_t keyw(int) const { return 0u; }
+};
+
+// Open addressing: 2^bits records, multiplicative hashing, linear probing.
+// A record belongs to this query when its forward unit carries the epoch,
+// and to node v when that unit's w field is v; records of other epochs are
+// free.  A record is claimed by one 128-bit CAS of its forward unit to
+// {epoch, unreached, no parent, v}; within a query records are never freed,
+// so a probe for v ends at v's record or at the first free one.  This is the
+// closed set of a search that touches far fewer nodes than the graph holds:
+// the table is sized to the touched set, not to n.
+constexpr int HASH_PROBES = 256;  // probe limit before the table counts as full
+struct RecHash {
+    static constexpr bool hashed = true;
+    unsigned long long *st;
+    uint32_t mask;
+    int shift;  // 32 - bits
+    __device__ uint32_t home(int v) const { return ((uint32_t)v * 0x9E3779B1u) >> shift; }
+    __device__ uint4 *rec(uint32_t i) const { return unit_ptr(st, (int)i, 0); }
+    __device__ uint4 *find(int v, uint32_t ep) const {
+        uint32_t i = home(v);
+        for (int k = 0; k < HASH_PROBES; k++, i = (i + 1) & mask) {
+            const uint4 f = __ldcg(rec(i));
+            if (f.x != ep) return nullptr;
+            if (f.w == (uint32_t)v) return rec(i);
+        }
+        return nullptr;
+    }
+    __device__ uint4 *claim(int v, uint32_t ep) const {
+        uint32_t i = home(v);
+        for (int k = 0; k < HASH_PROBES; k++, i = (i + 1) & mask) {
+            uint4 f = __ldcg(rec(i));
+            if (f.x != ep) {
+                const uint4 got = cas_unit(rec(i), f, make_uint4(ep, INF_G, 0xFFFFFFFFu, (uint32_t)v));
+                if (unit_eq(got, f)) return rec(i);
+                f = got;  // another thread claimed it meanwhile
+            }
+            if (f.x == ep && f.w == (uint32_t)v) return rec(i);
+        }
+        return nullptr;
+    }
+    __device__ uint32_t keyw(int v) const { return (uint32_t)v; }
+};
+
 // Path s..t from the meeting word; returns its length (0 when no path).
-__device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B, uint32_t ep, int32_t s, int32_t t,
+template <class Rec>
+__device__ inline int32_t write_path_bidir(const DevGraph &G, const Rec &R, uint32_t ep, int32_t s, int32_t t,
                                            unsigned long long mu, int32_t *path, int32_t cap, int *status) {
     const uint32_t cost = uint32_t(mu >> 32);
     if (cost >= INF_G) return 0;
@@ -156,15 +214,27 @@ __device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B,
         if (cap > 0) path[0] = s;
         return 1;
     }
-    unsigned long long *st = B.state;
+    // label of node v in direction dir (unit absent: unreached) and its
+    // parent / successor
+    auto lab = [&](int v, uint32_t dir, int32_t *link) -> uint32_t {
+        const uint4 *r = R.find(v, ep);
+        if (!r) {
+            *link = -1;
+            return INF_G;
+        }
+        const uint4 u = __ldcg(r + dir);
+        *link = (int32_t)u.z;
+        return unit_g(u, ep);
+    };
     const int32_t x = int32_t(uint32_t(mu));
-    const uint32_t gx = unit_g(__ldcg(unit_ptr(st, x, 0)), ep);
+    int32_t lk;
+    const uint32_t gx = lab(x, 0, &lk);
     int32_t y = -1;
     const int r1 = row_end(G.off, G.oend, x);
     for (int k = row_begin(G.off, G.oend, x); k < r1 && y < 0; k++) {
         const uint2 a = G.oend ? __ldcg(G.arc + k) : __ldg(G.arc + k);
         if ((int)a.x < 0) continue;
-        const uint32_t gr = unit_g(__ldcg(unit_ptr(st, (int)a.x, 1)), ep);
+        const uint32_t gr = lab((int)a.x, 1, &lk);
         if (gr < INF_G && (uint64_t)gx + a.y + gr == cost) y = (int32_t)a.x;
     }
     if (y < 0) {
@@ -173,22 +243,32 @@ __device__ inline int32_t write_path_bidir(const DevGraph &G, const SlotBufs &B,
     }
     // lengths of s..x (forward parents) and y..t (reverse successors)
     int32_t lf = 0, lr = 0;
-    for (int32_t c = x; c >= 0 && lf <= G.n; c = (int32_t)__ldcg(unit_ptr(st, c, 0)).z) {
+    for (int32_t c = x; c >= 0 && lf <= G.n;) {
         lf++;
         if (c == s) break;
+        lab(c, 0, &lk);
+        c = lk;
     }
-    for (int32_t c = y; c >= 0 && lr <= G.n; c = (int32_t)__ldcg(unit_ptr(st, c, 1)).z) {
+    for (int32_t c = y; c >= 0 && lr <= G.n;) {
         lr++;
         if (c == t) break;
+        lab(c, 1, &lk);
+        c = lk;
     }
     const int32_t len = lf + lr;
     if (len > cap) atomicOr(status, ST_PATH_TRUNC);
     int32_t i = lf - 1;
-    for (int32_t c = x; c >= 0 && i >= 0; c = (int32_t)__ldcg(unit_ptr(st, c, 0)).z, i--)
+    for (int32_t c = x; c >= 0 && i >= 0; i--) {
         if (i < cap) path[i] = c;
+        lab(c, 0, &lk);
+        c = lk;
+    }
     i = lf;
-    for (int32_t c = y; c >= 0 && i < len; c = (int32_t)__ldcg(unit_ptr(st, c, 1)).z, i++)
+    for (int32_t c = y; c >= 0 && i < len; i++) {
         if (i < cap) path[i] = c;
+        lab(c, 1, &lk);
+        c = lk;
+    }
     return len;
 }
 
@@ -263,15 +343,14 @@ __device__ __forceinline__ uint64_t bi_key_bound(uint32_t mu) {
 
 // ep: the slot's epoch for this query (never 0; units of other epochs read
 // as unreached).
-template <class Pot>
+template <class Pot, class Rec>
 __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, const SearchParams &P, uint32_t ep,
-                                      WarpRows *wrows, BiQ *sq, const Pot &pot) {
+                                      WarpRows *wrows, BiQ *sq, const Pot &pot, const Rec &R) {
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
     WarpRows &wr = wrows[warp];
     uint2 *ring = B.q0;
-    unsigned long long *st2 = B.state;
     const int cap = (int)min(B.cap_q, (int64_t)0x3FFFFFFF);
 
     if (threadIdx.x == 0) {
@@ -292,8 +371,11 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             ctl->touched = 0;
         } else {
             sq->mu = ~0ull;
-            *unit_ptr(st2, P.s, 0) = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
-            *unit_ptr(st2, P.t, 1) = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
+            // the endpoints' records (a fresh slot's table has room for two)
+            uint4 *rs = R.claim(P.s, ep);
+            uint4 *rt = R.claim(P.t, ep);
+            rs[0] = make_uint4(ep, 0u, 0xFFFFFFFFu, R.keyw(P.s));
+            rt[1] = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
             ctl->touched = 2;
             ring[0] = make_uint2((uint32_t)P.s, bi_key<Pot>(0u, 0u, pot.at(P.s)));
             ring[1] = make_uint2((uint32_t)P.t | DIR_BIT, bi_key<Pot>(0u, 1u, pot.at(P.t)));
@@ -394,7 +476,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     gu = en.y;  // the entry's key
                     const int u = (int)(ud & NODE_MASK);
                     const uint32_t dir = ud >> 31;
-                    const uint32_t gl = unit_g(__ldcg(unit_ptr(st2, u, dir)), ep);
+                    const uint4 *ru = R.find(u, ep);
+                    const uint32_t gl = ru ? unit_g(__ldcg(ru + dir), ep) : INF_G;
                     bool cur = false;
                     if constexpr (Pot::on) {
                         // the entry is current when its key is the label's key
@@ -426,6 +509,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     const int k = kb + lane;
                     bool live = false, first = false;
                     uint2 pv = make_uint2(0u, 0u);  // {pt(v), ps(v)}
+                    uint4 *rv = nullptr;           // v's record
                     int v = 0;
                     uint32_t ng = 0, dir = 0;
                     uint32_t uo = 0;
@@ -449,8 +533,14 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         }
                         if (live) {
                             // the node's record: both units, one sector
-                            uf = __ldcg(unit_ptr(st2, v, 0));
-                            ur = __ldcg(unit_ptr(st2, v, 1));
+                            rv = R.claim(v, ep);
+                            if (rv) {
+                                uf = __ldcg(rv);
+                                ur = __ldcg(rv + 1);
+                            } else {
+                                atomicOr(&sq->status, ST_OVERFLOW);  // the slot's table is full
+                                live = false;
+                            }
                         }
                     }
                     if (live) {
@@ -466,8 +556,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         }
                         live = ng < unit_g(mine, ep);
                         if (live) {
-                            const uint4 nv = make_uint4(ep, ng, uo & NODE_MASK, 0u);
-                            uint4 *w = unit_ptr(st2, v, dir);
+                            const uint4 nv = make_uint4(ep, ng, uo & NODE_MASK, dir ? 0u : R.keyw(v));
+                            uint4 *w = rv + dir;
                             uint4 c0 = mine;
                             live = false;
                             // bounded: contention on one unit comes from at
@@ -480,7 +570,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                 const uint4 got = cas_unit(w, c0, nv);
                                 if (unit_eq(got, c0)) {
                                     live = true;
-                                    first = c0.x != ep;
+                                    first = unit_g(c0, ep) >= INF_G;
                                     break;
                                 }
                                 c0 = got;

@@ -27,10 +27,19 @@ constexpr int MAX_WARPS = 16;  // blocks of at most 512 threads
 // epoch-tagged units), no touched log, one ring and 8-byte far entries;
 // the others one 8-byte state word per node, a touched log, two queues and
 // 16-byte far entries.
-size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind) {
+// Hashed records per slot: a quarter of the nodes, between 2^16 and 2^20
+// (a C4 query touches about 35k nodes; the table stays under 15 % full).
+int hash_bits(int32_t n) {
+    int b = 16;
+    while (b < 20 && ((int64_t)1 << b) < (int64_t)n / 4) b++;
+    return b;
+}
+
+size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind, int hbits) {
     const bool pair = (kind & SLOT_PAIR) != 0;
+    const size_t recs = (kind & SLOT_HASH) ? ((size_t)1 << hbits) : (size_t)n;
     size_t b = 0;
-    b += sizeof(unsigned long long) * (size_t)n * (pair ? 4 : 1);  // state
+    b += sizeof(unsigned long long) * recs * (pair ? 4 : 1);  // state
     if (!pair) b += sizeof(int32_t) * (size_t)n;                     // touched
     if (kind & SLOT_HOPS) b += sizeof(uint32_t) * (size_t)n;
     b += (pair ? 1 : 2) * sizeof(uint2) * (size_t)cap_q;
@@ -40,13 +49,14 @@ size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind) {
 }
 
 int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, int kind,
-                cudaStream_t st) {
+                cudaStream_t st, int hbits) {
     sa = SlotArrays();
     const bool hops = (kind & SLOT_HOPS) != 0;
     const bool pair = (kind & SLOT_PAIR) != 0;
     sa.n = n;
     sa.words = pair ? 4 : 1;
-    sa.sstride = (int64_t)n * sa.words;
+    sa.hbits = (kind & SLOT_HASH) ? hbits : 0;
+    sa.sstride = (sa.hbits ? ((int64_t)1 << sa.hbits) : (int64_t)n) * sa.words;
     sa.nslots = nslots;
     sa.cap_q = cap_q;
     sa.cap_f = cap_f;
@@ -105,6 +115,8 @@ __device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
     b.ctl = sa.ctl + i;
     b.cap_q = sa.cap_q;
     b.cap_f = sa.cap_f;
+    b.swords = sa.sstride;
+    b.hbits = sa.hbits;
     return b;
 }
 
@@ -306,7 +318,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         }
         grp.sync();
         if (bidir_hk(HK) && *(volatile uint32_t *)&ctl->tag == 0) {
-            for (size_t i = grp.rank(); i < 4 * (size_t)G0.n; i += grp.size()) B.state[i] = 0ull;
+            for (size_t i = grp.rank(); i < (size_t)B.swords; i += grp.size()) B.state[i] = 0ull;
             grp.sync();
             if (grp.rank() == 0) ctl->tag = 1;
             grp.sync();
@@ -365,14 +377,19 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             if constexpr (std::is_same<Grp, CtaGroup>::value) {
                 const uint32_t ep = *(volatile uint32_t *)&ctl->tag;
                 if constexpr (HK == 5) {
-                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{});
+                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{}, RecDense{B.state});
+                } else if constexpr (HK == 8) {
+                    const RecHash R{B.state, (1u << B.hbits) - 1u, 32 - B.hbits};
+                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{}, R);
                 } else {
                     const int2 sp = reinterpret_cast<const int2 *>(G.xy)[s];
                     const int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
                     if constexpr (HK == 6)
-                        r = run_bidir_cta(G, B, P, ep, wrows, bq, PotEuclid{G.xy, sp, tp, G.rho_fp / 65536.0});
+                        r = run_bidir_cta(G, B, P, ep, wrows, bq, PotEuclid{G.xy, sp, tp, G.rho_fp / 65536.0},
+                                          RecDense{B.state});
                     else
-                        r = run_bidir_cta(G, B, P, ep, wrows, bq, PotManhattan{G.xy, sp, tp, G.wmin});
+                        r = run_bidir_cta(G, B, P, ep, wrows, bq, PotManhattan{G.xy, sp, tp, G.wmin},
+                                          RecDense{B.state});
                 }
             }
         } else {
@@ -388,9 +405,12 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             const int st = ctl->status;
             int32_t len = 0;
             if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths) {
-                if (bidir_hk(HK))
-                    len = write_path_bidir(G, B, ctl->tag, s, t, bq->mu, A.paths + (size_t)q * A.path_cap,
-                                           A.path_cap, &ctl->status);
+                if (HK == 8)
+                    len = write_path_bidir(G, RecHash{B.state, (1u << B.hbits) - 1u, 32 - B.hbits}, ctl->tag, s,
+                                           t, bq->mu, A.paths + (size_t)q * A.path_cap, A.path_cap, &ctl->status);
+                else if (bidir_hk(HK))
+                    len = write_path_bidir(G, RecDense{B.state}, ctl->tag, s, t, bq->mu,
+                                           A.paths + (size_t)q * A.path_cap, A.path_cap, &ctl->status);
                 else
                     len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
                                      &ctl->status);
@@ -644,7 +664,8 @@ static int slot_kind(int hkind) {
 static int rerun_kind(int hkind) { return is_bidir_kind(hkind) ? DDP_H_ZERO : hkind; }
 
 // The batch kernel instance for a heuristic kind.
-static const void *batch_kernel(int hkind) {
+static const void *batch_kernel(int hkind, bool hashed = false) {
+    if (hashed && hkind == DDP_H_BIDIR) return (const void *)k_batch<8>;
     if (is_bfs_kind(hkind)) return (const void *)k_batch<1>;
     if (hkind == DDP_H_MANHATTAN) return (const void *)k_batch<2>;
     if (hkind == DDP_H_EUCLID) return (const void *)k_batch<3>;
@@ -1210,6 +1231,7 @@ struct ddp_batch {
     int32_t launches = 0;
     int group = 1;  // CTAs per query slot
     bool no_graph = false;
+    bool hashed = false;  // DDP_OPT_HASH: hashed records in bidirectional slots
     // CUDA graph of the last device-pointer solve and the kernel arguments
     // it was captured with: a replay is valid only while a fresh launch
     // would pass exactly the same arguments (graph arrays, landmark table,
@@ -1292,7 +1314,7 @@ static cudaError_t batch_launch_args(ddp_batch *b, DevGraph G, BatchArgs A) {
     const int grid = b->sa.nslots * b->group;
     SlotArrays sa = b->sa;
     void *args[] = {&G, &sa, &A};
-    const void *fn = batch_kernel(b->hkind);
+    const void *fn = batch_kernel(b->hkind, b->hashed);
     if (b->group > 1)
         return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
     return cudaLaunchKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
@@ -1347,7 +1369,8 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     }
     // slots: occupancy-limited, then memory-limited (half of free memory)
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(hkind), b->block, 0);
+    b->hashed = hkind == DDP_H_BIDIR && (b->o.flags & DDP_OPT_HASH) != 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(hkind, b->hashed), b->block, 0);
     b->group = is_bidir_kind(hkind) ? 1 : std::max(1, b->o.group);  // bidirectional slots are one CTA
     const int coresident = std::max(1, per_sm) * sm_count();
     if (b->group > coresident) b->group = coresident;
@@ -1363,10 +1386,12 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     // the far pile holds every open node beyond the current bucket: twice the
     // node count leaves room for stale copies between compactions
     const int64_t cap_f = b->o.queue_cap > 0 ? b->o.queue_cap : 2 * (int64_t)g->n + 4096;
-    const size_t per = slot_bytes(g->n, cap, cap_f, slot_kind(hkind));
+    const int skind = slot_kind(hkind) | (b->hashed ? SLOT_HASH : 0);
+    const int hb = b->hashed ? hash_bits(g->n) : 0;
+    const size_t per = slot_bytes(g->n, cap, cap_f, skind, hb);
     const size_t budget = freeb / 2;
     if ((size_t)nslots * per > budget) nslots = (int)std::max<size_t>(1, budget / per);
-    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap_f, slot_kind(hkind), b->stream);
+    int rc = slots_alloc(b->sa, g->n, nslots, cap, cap_f, skind, b->stream, hb);
     if (rc == DDP_OK) {
         cudaError_t e1 = cudaMalloc(&b->d_work, sizeof(int) * 2);
         if (e1 != cudaSuccess) rc = cuda_fail(e1, "cudaMalloc(work)");

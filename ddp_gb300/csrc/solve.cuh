@@ -13,6 +13,7 @@ struct SlotArrays {
     int nslots = 0;
     int words = 1;        // 64-bit state words per node: 1, or 4 (paired slots: a 32-byte record)
     int64_t sstride = 0;  // state words per slot
+    int hbits = 0;        // hashed paired slots: log2 of the records per slot
     int64_t cap_q = 0, cap_f = 0;
     unsigned long long *state = nullptr;  // nslots x n x words
     int32_t *touched = nullptr;           // nslots x n (null for paired slots)
@@ -83,15 +84,19 @@ struct BatchArgs {
 inline bool is_bidir_kind(int k) {
     return k == DDP_H_BIDIR || k == DDP_H_BIDIR_EUCLID || k == DDP_H_BIDIR_MANHATTAN;
 }
-constexpr bool bidir_hk(int hk) { return hk >= 5 && hk <= 7; }
+// 8: DDP_H_BIDIR with hashed records (DDP_OPT_HASH)
+constexpr bool bidir_hk(int hk) { return hk >= 5 && hk <= 8; }
 
-// Slot kinds (bits): a per-target hop array; paired forward/reverse state.
-enum { SLOT_HOPS = 1, SLOT_PAIR = 2 };
-size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind);
+// Slot kinds (bits): a per-target hop array; paired forward/reverse state;
+// paired records in a hash table of 2^hbits records instead of one per node.
+enum { SLOT_HOPS = 1, SLOT_PAIR = 2, SLOT_HASH = 4 };
+size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind, int hbits = 0);
+// log2 of the hashed records per slot for an n-node graph
+int hash_bits(int32_t n);
 // Runs maintenance subs with ordinary launches on st (no serving kernel runs).
 cudaError_t svc_run_direct(const SvcSub *subs, int nsub, cudaStream_t st);
 int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t cap_f, int kind,
-                cudaStream_t st);
+                cudaStream_t st, int hbits = 0);
 void slots_free(SlotArrays &sa);
 uint32_t *heuristic_hops_ptr(const ddp_heuristic *h);
 cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,

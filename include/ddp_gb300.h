@@ -102,6 +102,8 @@ typedef struct ddp_opts {
 /* ddp_opts.flags */
 #define DDP_OPT_SYNC 1    /* one-CTA slots use the phase-synchronous engine      */
 #define DDP_OPT_ONE_CTA 2 /* ddp_solve: one CTA with the asynchronous engine      */
+#define DDP_OPT_HASH 4    /* DDP_H_BIDIR batches: each slot keeps its closed set in
+                             a hash table sized to the touched nodes, not n     */
 
 /* ---- library ----------------------------------------------------------- */
 const char *ddp_last_error(void);

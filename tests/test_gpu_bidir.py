@@ -291,3 +291,62 @@ def test_bidir_euclid_serving_with_updates(gpu, oracle):
         assert costs[k] == want, (int(ids[k]), int(ver[k]))
     srv.close()
     dg.close()
+
+
+@pytest.mark.parametrize("n,deg,wmax,seed", [(30000, 8, 100, 81), (6001, 2, 3, 82)])
+def test_bidir_hashed_records(gpu, oracle, n, deg, wmax, seed):
+    """DDP_OPT_HASH: each slot keeps its closed set in a hash table sized to
+    the touched nodes; costs and paths as with one record per node, on the
+    host path and the device path (two replays)."""
+    torch = pytest.importorskip("torch")
+    d = gpu
+    g = d.gen_random_chain(n, deg, 1, wmax, seed)
+    dg = d.DeviceGraph.from_csr(g)
+    S, T = _pairs(g.n, 300, seed)
+    want = _oracle_costs(oracle, g, S, T)
+    be = d.BatchEngine(dg, d.H_BIDIR, flags=d.OPT_HASH)
+    cost, plen = be.solve(S, T)
+    _check(oracle, be, g, S, T, cost, want, plen)
+    dev = torch.device("cuda", 0)
+    dS, dT = torch.from_numpy(S).to(dev), torch.from_numpy(T).to(dev)
+    dc = torch.empty(len(S), dtype=torch.int32, device=dev)
+    for _ in range(2):
+        dc.fill_(-7)
+        be.solve_device(len(S), dS.data_ptr(), dT.data_ptr(), dc.data_ptr(), 0)
+        be.sync()
+        _check(oracle, be, g, S, T, dc.cpu().numpy(), want)
+    be.close()
+    dg.close()
+
+
+def test_bidir_hashed_table_full(gpu, oracle):
+    """Two disconnected 100k-node components: a query across them explores
+    both (about 200k records, more than the 2^16-record table of a graph
+    this size holds).  The device path reports -1 for it; the host path
+    re-runs it and returns the oracle's answer; queries inside a component
+    stay exact."""
+    torch = pytest.importorskip("torch")
+    d = gpu
+    a = d.gen_random_chain(100000, 3, 1, 50, 91)
+    b = d.gen_random_chain(100000, 3, 1, 50, 92)
+    off = np.concatenate([a.off[:-1], b.off + a.e]).astype(np.int32)
+    col = np.concatenate([a.col, b.col + a.n]).astype(np.int32)
+    w = np.concatenate([a.w, b.w]).astype(np.uint32)
+    g = d.CSR(a.n + b.n, off, col, w)
+    dg = d.DeviceGraph.from_csr(g)
+    S = np.array([5, 7, 100005, 11], np.int32)
+    T = np.array([150000, 99999, 100100, 12], np.int32)  # query 0 crosses components
+    want = _oracle_costs(oracle, g, S, T)
+    assert want[0] == INF
+    be = d.BatchEngine(dg, d.H_BIDIR, flags=d.OPT_HASH, grid=4)
+    dev = torch.device("cuda", 0)
+    dS, dT = torch.from_numpy(S).to(dev), torch.from_numpy(T).to(dev)
+    dc = torch.empty(len(S), dtype=torch.int32, device=dev)
+    be.solve_device(len(S), dS.data_ptr(), dT.data_ptr(), dc.data_ptr(), 0)
+    be.sync()
+    got = dc.cpu().numpy()
+    assert got[0] == -1 and np.array_equal(got[1:], want[1:])
+    cost, _ = be.solve(S, T)
+    assert np.array_equal(cost, want)
+    be.close()
+    dg.close()
