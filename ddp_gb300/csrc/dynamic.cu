@@ -35,6 +35,7 @@
 // No parent cycles can arise: parents always point to strictly earlier
 // relaxations, and invalidated subtrees are rebuilt from valid nodes only.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <vector>
 
@@ -58,26 +59,15 @@ struct DynMirror {
     bool full = true;  // next upload sends everything
     // device side: capacities of the arc arrays and scatter staging buffers
     int64_t arc_cap = 0, rarc_cap = 0;
-    long long *d_slot = nullptr;
-    uint2 *d_val = nullptr;
-    int4 *d_rows = nullptr;
-    int64_t scat_cap = 0, rows_cap = 0;
-    // pinned staging of the scatter lists ([0] forward, [1] reverse), so
-    // that their copies are asynchronous; reused once the graph's stream
-    // has been synchronised (every update path ends with that)
-    long long *h_slot[2] = {nullptr, nullptr};
-    uint2 *h_val[2] = {nullptr, nullptr};
-    int4 *h_rows[2] = {nullptr, nullptr};
-    int64_t h_scap[2] = {0, 0}, h_rcap[2] = {0, 0};
+    // staging of a batch's scatter lists: pinned host memory (the copy is
+    // asynchronous; the buffer is reused once the graph's stream has been
+    // synchronised, which every update path does) and its device twin
+    char *h_stage = nullptr;
+    char *d_stage = nullptr;
+    int64_t stage_cap = 0;
     ~DynMirror() {
-        cudaFree(d_slot);
-        cudaFree(d_val);
-        cudaFree(d_rows);
-        for (int i = 0; i < 2; i++) {
-            cudaFreeHost(h_slot[i]);
-            cudaFreeHost(h_val[i]);
-            cudaFreeHost(h_rows[i]);
-        }
+        cudaFree(d_stage);
+        cudaFreeHost(h_stage);
     }
 };
 
@@ -152,18 +142,34 @@ bool mirror_append(std::vector<int32_t> &beg, std::vector<int32_t> &end, std::ve
     return true;
 }
 
-__global__ void k_scatter_arcs(uint2 *arc, const long long *slot, const uint2 *val, int m) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m) arc[slot[i]] = val[i];
-}
+// All of a batch's graph changes in one launch: thread i writes row bound
+// i of the forward rows, then of the reverse rows, then arc slot i of the
+// forward arcs, then of the reverse arcs.
+struct ScatterAll {
+    uint2 *arc, *rarc;
+    int32_t *off, *oend, *roff, *roend;
+    const int4 *rows;         // kr forward then krr reverse {row, begin, end}
+    const long long *slots;   // ka forward then kra reverse arc slots
+    const uint2 *vals;        // their values
+    int64_t ka, kra, kr, krr;
+};
 
-__global__ void k_scatter_rows(int32_t *beg, int32_t *end, const int4 *rows, int m) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m) {
-        int4 r = rows[i];
-        beg[r.x] = r.y;
-        end[r.x] = r.z;
+__global__ void k_scatter_all(ScatterAll j) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < j.kr + j.krr) {
+        const int4 r = j.rows[i];
+        if (i < j.kr) {
+            j.off[r.x] = r.y;
+            j.oend[r.x] = r.z;
+        } else {
+            j.roff[r.x] = r.y;
+            j.roend[r.x] = r.z;
+        }
+        return;
     }
+    i -= j.kr + j.krr;
+    if (i < j.ka) j.arc[j.slots[i]] = j.vals[i];
+    else if (i < j.ka + j.kra) j.rarc[j.slots[i]] = j.vals[i];
 }
 
 struct DynArgs {
@@ -425,7 +431,6 @@ namespace ddp {
 
 int dyn_upload(ddp_graph *g, bool sync) {
     DynMirror *m = g->dyn;
-    DynMirror *d = m;  // device bookkeeping lives in the mirror
     const int32_t n = g->n;
     if (m->full) {
         if ((int64_t)m->arc.size() > m->arc_cap) {
@@ -454,94 +459,106 @@ int dyn_upload(ddp_graph *g, bool sync) {
         m->dirty_rrow.clear();
         return DDP_OK;
     }
-    // scatter the touched slots and row bounds
-    auto scatter = [&](std::vector<int64_t> &dirty, std::vector<uint2> &src, uint2 *dst, int side) -> int {
-        if (dirty.empty()) return DDP_OK;
-        std::sort(dirty.begin(), dirty.end());
-        dirty.erase(std::unique(dirty.begin(), dirty.end()), dirty.end());
-        const int64_t k = (int64_t)dirty.size();
-        std::vector<long long> sl(dirty.begin(), dirty.end());
-        std::vector<uint2> val((size_t)k);
-        for (int64_t i = 0; i < k; i++) val[(size_t)i] = src[(size_t)dirty[(size_t)i]];
-        const int h = g->hook.fn ? g->hook.fn(g->hook.ctx, 0, dst, nullptr, sl.data(), val.data(), k)
-                                 : SCATTER_LAUNCH;
-        if (h != SCATTER_LAUNCH) {
-            if (h) return h;
-            dirty.clear();
-            return DDP_OK;
-        }
-        if (k > d->scat_cap) {
-            graph_free_dev(g, d->d_slot);
-            graph_free_dev(g, d->d_val);
-            d->d_slot = nullptr;
-            d->d_val = nullptr;
-            DDP_CUDA(cudaMalloc(&d->d_slot, sizeof(long long) * k));
-            DDP_CUDA(cudaMalloc(&d->d_val, sizeof(uint2) * k));
-            d->scat_cap = k;
-        }
-        if (k > d->h_scap[side]) {
-            cudaFreeHost(d->h_slot[side]);
-            cudaFreeHost(d->h_val[side]);
-            d->h_slot[side] = nullptr;
-            d->h_val[side] = nullptr;
-            d->h_scap[side] = 0;
-            DDP_CUDA(cudaHostAlloc(&d->h_slot[side], sizeof(long long) * k, cudaHostAllocDefault));
-            DDP_CUDA(cudaHostAlloc(&d->h_val[side], sizeof(uint2) * k, cudaHostAllocDefault));
-            d->h_scap[side] = k;
-        }
-        std::memcpy(d->h_slot[side], sl.data(), sizeof(long long) * k);
-        std::memcpy(d->h_val[side], val.data(), sizeof(uint2) * k);
-        // device staging is shared by both sides: stream order keeps the
-        // forward scatter's kernel ahead of the reverse side's copies
-        DDP_CUDA(cudaMemcpyAsync(d->d_slot, d->h_slot[side], sizeof(long long) * k, cudaMemcpyHostToDevice,
-                                 g->stream));
-        DDP_CUDA(cudaMemcpyAsync(d->d_val, d->h_val[side], sizeof(uint2) * k, cudaMemcpyHostToDevice, g->stream));
-        k_scatter_arcs<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(dst, d->d_slot, d->d_val, (int)k);
-        DDP_CUDA(cudaGetLastError());  // stream-ordered; one synchronisation at the end
-        dirty.clear();
-        return DDP_OK;
+    // the touched arc slots and row bounds, sorted and without repeats
+    auto uniq = [](auto &x) {
+        std::sort(x.begin(), x.end());
+        x.erase(std::unique(x.begin(), x.end()), x.end());
     };
-    auto rows = [&](std::vector<int32_t> &drow, std::vector<int32_t> &b, std::vector<int32_t> &e, int32_t *db,
-                    int32_t *de, int side) -> int {
-        if (drow.empty()) return DDP_OK;
-        std::sort(drow.begin(), drow.end());
-        drow.erase(std::unique(drow.begin(), drow.end()), drow.end());
-        const int64_t k = (int64_t)drow.size();
-        std::vector<int4> r((size_t)k);
-        for (int64_t i = 0; i < k; i++) {
-            const int32_t u = drow[(size_t)i];
-            r[(size_t)i] = make_int4(u, b[(size_t)u], e[(size_t)u], 0);
+    uniq(m->dirty_arc);
+    uniq(m->dirty_rarc);
+    uniq(m->dirty_row);
+    uniq(m->dirty_rrow);
+    int64_t ka = (int64_t)m->dirty_arc.size(), kra = (int64_t)m->dirty_rarc.size();
+    int64_t kr = (int64_t)m->dirty_row.size(), krr = (int64_t)m->dirty_rrow.size();
+    int rc = DDP_OK;
+    if (g->hook.fn) {
+        // a serving kernel holds the GPU: each list goes to its service CTA
+        // (lists it cannot take stay for the launch below)
+        auto hook_arcs = [&](std::vector<int64_t> &dirty, std::vector<uint2> &src, uint2 *dst, int64_t &k) {
+            if (!k || rc) return;
+            std::vector<long long> sl(dirty.begin(), dirty.end());
+            std::vector<uint2> val((size_t)k);
+            for (int64_t i = 0; i < k; i++) val[(size_t)i] = src[(size_t)dirty[(size_t)i]];
+            const int h = g->hook.fn(g->hook.ctx, 0, dst, nullptr, sl.data(), val.data(), k);
+            if (h == SCATTER_LAUNCH) return;
+            rc = h;
+            k = 0;
+        };
+        auto hook_rows = [&](std::vector<int32_t> &drow, std::vector<int32_t> &bb, std::vector<int32_t> &ee,
+                             int32_t *db, int32_t *de, int64_t &k) {
+            if (!k || rc) return;
+            std::vector<int4> r((size_t)k);
+            for (int64_t i = 0; i < k; i++) {
+                const int32_t x = drow[(size_t)i];
+                r[(size_t)i] = make_int4(x, bb[(size_t)x], ee[(size_t)x], 0);
+            }
+            const int h = g->hook.fn(g->hook.ctx, 1, db, de, r.data(), nullptr, k);
+            if (h == SCATTER_LAUNCH) return;
+            rc = h;
+            k = 0;
+        };
+        hook_arcs(m->dirty_arc, m->arc, g->d_arc, ka);
+        hook_arcs(m->dirty_rarc, m->rarc, g->d_rarc, kra);
+        hook_rows(m->dirty_row, m->beg, m->end, g->d_off, g->d_oend, kr);
+        hook_rows(m->dirty_rrow, m->rbeg, m->rend, g->d_roff, g->d_roend, krr);
+    }
+    const int64_t total = ka + kra + kr + krr;
+    if (!rc && total) {
+        // one staging buffer, one copy, one kernel: rows (int4) first, then
+        // arc slots (int64), then arc values (uint2)
+        const size_t bytes = sizeof(int4) * (size_t)(kr + krr) + (sizeof(long long) + sizeof(uint2)) * (size_t)(ka + kra);
+        if ((int64_t)bytes > m->stage_cap) {
+            graph_free_dev(g, m->d_stage);
+            m->d_stage = nullptr;
+            cudaFreeHost(m->h_stage);
+            m->h_stage = nullptr;
+            m->stage_cap = 0;
+            const size_t cap = std::max<size_t>(bytes * 2, 1 << 16);
+            DDP_CUDA(cudaMalloc(&m->d_stage, cap));
+            DDP_CUDA(cudaHostAlloc(&m->h_stage, cap, cudaHostAllocDefault));
+            m->stage_cap = (int64_t)cap;
         }
-        const int h = g->hook.fn ? g->hook.fn(g->hook.ctx, 1, db, de, r.data(), nullptr, k) : SCATTER_LAUNCH;
-        if (h != SCATTER_LAUNCH) {
-            if (h) return h;
-            drow.clear();
-            return DDP_OK;
+        int4 *hr = reinterpret_cast<int4 *>(m->h_stage);
+        for (int64_t i = 0; i < kr; i++) {
+            const int32_t x = m->dirty_row[(size_t)i];
+            hr[i] = make_int4(x, m->beg[(size_t)x], m->end[(size_t)x], 0);
         }
-        if (k > d->rows_cap) {
-            graph_free_dev(g, d->d_rows);
-            d->d_rows = nullptr;
-            DDP_CUDA(cudaMalloc(&d->d_rows, sizeof(int4) * k));
-            d->rows_cap = k;
+        for (int64_t i = 0; i < krr; i++) {
+            const int32_t x = m->dirty_rrow[(size_t)i];
+            hr[kr + i] = make_int4(x, m->rbeg[(size_t)x], m->rend[(size_t)x], 0);
         }
-        if (k > d->h_rcap[side]) {
-            cudaFreeHost(d->h_rows[side]);
-            d->h_rows[side] = nullptr;
-            d->h_rcap[side] = 0;
-            DDP_CUDA(cudaHostAlloc(&d->h_rows[side], sizeof(int4) * k, cudaHostAllocDefault));
-            d->h_rcap[side] = k;
+        long long *hs = reinterpret_cast<long long *>(hr + kr + krr);
+        uint2 *hv = reinterpret_cast<uint2 *>(hs + ka + kra);
+        for (int64_t i = 0; i < ka; i++) {
+            hs[i] = m->dirty_arc[(size_t)i];
+            hv[i] = m->arc[(size_t)m->dirty_arc[(size_t)i]];
         }
-        std::memcpy(d->h_rows[side], r.data(), sizeof(int4) * k);
-        DDP_CUDA(cudaMemcpyAsync(d->d_rows, d->h_rows[side], sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
-        k_scatter_rows<<<(int)((k + 255) / 256), 256, 0, g->stream>>>(db, de, d->d_rows, (int)k);
-        DDP_CUDA(cudaGetLastError());
-        drow.clear();
-        return DDP_OK;
-    };
-    int rc = scatter(m->dirty_arc, m->arc, g->d_arc, 0);
-    if (!rc) rc = scatter(m->dirty_rarc, m->rarc, g->d_rarc, 1);
-    if (!rc) rc = rows(m->dirty_row, m->beg, m->end, g->d_off, g->d_oend, 0);
-    if (!rc) rc = rows(m->dirty_rrow, m->rbeg, m->rend, g->d_roff, g->d_roend, 1);
+        for (int64_t i = 0; i < kra; i++) {
+            hs[ka + i] = m->dirty_rarc[(size_t)i];
+            hv[ka + i] = m->rarc[(size_t)m->dirty_rarc[(size_t)i]];
+        }
+        DDP_CUDA(cudaMemcpyAsync(m->d_stage, m->h_stage, bytes, cudaMemcpyHostToDevice, g->stream));
+        ScatterAll j;
+        j.arc = g->d_arc;
+        j.rarc = g->d_rarc;
+        j.off = g->d_off;
+        j.oend = g->d_oend;
+        j.roff = g->d_roff;
+        j.roend = g->d_roend;
+        j.rows = reinterpret_cast<const int4 *>(m->d_stage);
+        j.slots = reinterpret_cast<const long long *>(j.rows + kr + krr);
+        j.vals = reinterpret_cast<const uint2 *>(j.slots + ka + kra);
+        j.ka = ka;
+        j.kra = kra;
+        j.kr = kr;
+        j.krr = krr;
+        k_scatter_all<<<(int)((total + 255) / 256), 256, 0, g->stream>>>(j);
+        DDP_CUDA(cudaGetLastError());  // stream-ordered; synchronised below or by the caller
+    }
+    m->dirty_arc.clear();
+    m->dirty_rarc.clear();
+    m->dirty_row.clear();
+    m->dirty_rrow.clear();
     // the device graph is current when this returns (other streams read it),
     // unless the caller synchronises the graph's stream itself
     if (!rc && sync) DDP_CUDA(cudaStreamSynchronize(g->stream));
@@ -619,6 +636,7 @@ int dyn_graph_prepare(ddp_graph *g) {
 // uploads the touched slots.  ups receives the search-relevant updates.
 int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
                     const uint32_t *w, std::vector<int4> &ups, bool sync) {
+    const auto t0 = std::chrono::steady_clock::now();
     g->update_count++;  // landmark distances no longer hold
     int rcp = dyn_graph_prepare(g);
     if (rcp) return rcp;
@@ -664,6 +682,7 @@ int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32
     // inserts, appended to their rows in batch order (createDiffGraph).  When
     // a row cannot grow, everything is laid out again with fresh slack and a
     // reserve sized for the inserts still to come (larger on each retry).
+    const auto t_del = std::chrono::steady_clock::now();
     int relayouts = 0;
     for (int32_t i = 0; i < nupd; i++) {
         if (flag[i] != 1) continue;
@@ -694,7 +713,17 @@ int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32
         if (w[i] < g->wmin) g->wmin = w[i];
         if (w[i] > g->wmax) g->wmax = w[i];
     }
-    return dyn_upload(g, sync);
+    if (!trace_on()) return dyn_upload(g, sync);
+    const auto t1 = std::chrono::steady_clock::now();
+    const int rc = dyn_upload(g, sync);
+    const auto t2 = std::chrono::steady_clock::now();
+    trace("dyn_apply: mirror %.1f us (deletes and weight changes %.1f us, inserts %.1f us, %d re-layouts), "
+          "upload %.1f us",
+          std::chrono::duration<double, std::micro>(t1 - t0).count(),
+          std::chrono::duration<double, std::micro>(t_del - t0).count(),
+          std::chrono::duration<double, std::micro>(t1 - t_del).count(), relayouts,
+          std::chrono::duration<double, std::micro>(t2 - t1).count());
+    return rc;
 }
 
 }  // namespace ddp
@@ -781,8 +810,10 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
     std::vector<int4> ups;
     // no synchronisation after the graph scatters: k_dyn runs on the same
     // stream, and dyn_launch synchronises it before returning
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = dyn_graph_apply(g, nupd, flag, u, v, w, ups, false);
     if (rc) return rc;
+    const auto t1 = std::chrono::steady_clock::now();
     const int32_t k = (int32_t)ups.size();
     if (k > d->upd_cap) {
         cudaFree(d->d_upd);
@@ -793,6 +824,12 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
     if (k) DDP_CUDA(cudaMemcpyAsync(d->d_upd, ups.data(), sizeof(int4) * k, cudaMemcpyHostToDevice, g->stream));
     rc = dyn_launch(d, 0, k);
     if (rc) return rc;
+    if (trace_on()) {
+        const auto t2 = std::chrono::steady_clock::now();
+        trace("dyn_update: %d updates, host apply + scatters %.1f us, repair + search (synchronised) %.1f us",
+              nupd, std::chrono::duration<double, std::micro>(t1 - t0).count(),
+              std::chrono::duration<double, std::micro>(t2 - t1).count());
+    }
     if (out_cost) *out_cost = d->cost;
     return DDP_OK;
 }
