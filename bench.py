@@ -391,10 +391,11 @@ def bench_single(a, c):
     cost = None
     # the autotuner's space here: K for the whole-GPU phase-synchronous engine,
     # and the one-CTA asynchronous engine
-    variants = [(f"grid K={K}", dict(K=K)) for K in Ks] + [("one-CTA async", dict(flags=d.OPT_ONE_CTA))]
+    variants = [(f"grid K={K}", dict(K=K, delta=a.delta)) for K in Ks] + \
+               [("one-CTA async", dict(flags=d.OPT_ONE_CTA, delta=a.delta))]
     # the maze also runs the one-CTA bidirectional A* (average Manhattan
     # potentials) as a batch of one query
-    be_bi = d.BatchEngine(dg, d.H_BIDIR_MANHATTAN, grid=1) if a.config == "c2" else None
+    be_bi = d.BatchEngine(dg, d.H_BIDIR_MANHATTAN, grid=1, delta=a.delta) if a.config == "c2" else None
     for name, kw in variants:
         for _ in range(max(3, a.warmup)):
             r = dg.solve(s, t, h, **kw)
