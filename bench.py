@@ -801,12 +801,17 @@ def main():
     # fixture, checked by input digest)
     fixture = check_fixture(c, pairs, rank, g, S, T, costs)
 
-    # end to end through the C-ABI with host buffers (H2D + D2H inside)
+    # end to end through the C-ABI with pinned host buffers (H2D of the
+    # pairs, D2H of costs and path lengths inside the timed region)
+    pin = lambda x: torch.from_numpy(x).pin_memory().numpy()
+    hS, hT = pin(S), pin(T)
+    hc = torch.empty(pairs, dtype=torch.int32).pin_memory().numpy()
+    hp = torch.empty(pairs, dtype=torch.int32).pin_memory().numpy()
     e2e_times = []
     for i in range(a.steps + 1):
         torch.cuda.synchronize(dev)
         s0 = time.perf_counter()
-        hc, hp = be.solve(S, T)
+        be.solve(hS, hT, hc, hp)
         s1 = time.perf_counter()
         if i > 0:
             e2e_times.append(s1 - s0)
@@ -907,7 +912,8 @@ def main():
                            "far_scanned_mean": float(st[:, 6].mean()), "touched_mean": float(st[:, 7].mean())},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": int(S.nbytes + T.nbytes),
-                "d2h_bytes_per_step": int(2 * 4 * pairs), "exact_vs_device_run": exact_vs_batch},
+                "d2h_bytes_per_step": int(2 * 4 * pairs), "exact_vs_device_run": exact_vs_batch,
+                "host_buffers": "pinned", "call": "ddp_batch_solve (C ABI), one per step, synchronous"},
         "overflowed_queries": int((costs == -1).sum()),
         "gpu_launches": launches,
         "clocks": clocks,

@@ -473,11 +473,14 @@ class BatchEngine:
         self.handle = b
         self.n_last = 0
 
-    def solve(self, S, T):
+    def solve(self, S, T, cost=None, plen=None):
+        """Host arrays in and out; cost / plen may be caller-owned int32
+        arrays of len(S) (for example views of pinned host memory)."""
         S, T = _i32(S), _i32(T)
         n = len(S)
-        cost = np.empty(n, np.int32)
-        plen = np.empty(n, np.int32)
+        cost = np.empty(n, np.int32) if cost is None else cost
+        plen = np.empty(n, np.int32) if plen is None else plen
+        assert cost.dtype == np.int32 and plen.dtype == np.int32 and len(cost) == n and len(plen) == n
         check(lib().ddp_batch_solve(self.handle, n, ptr(S), ptr(T), ptr(cost), ptr(plen)))
         self.n_last = n
         return cost, plen
