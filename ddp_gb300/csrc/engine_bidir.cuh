@@ -154,13 +154,51 @@ __device__ __forceinline__ uint4 cas_unit(uint4 *addr, const uint4 &cmp, const u
 // keyw(v) is the forward unit's w field: 0 for dense records, the node id
 // for hashed ones.
 
+// Unit operations shared by the epoch-tagged layouts (16-byte units).
+struct UnitOps16 {
+    using U = uint4;
+    static constexpr bool logs = false;  // no touched log: epochs retire the records
+    __device__ static U ld(const U *p) { return __ldcg(p); }
+    __device__ static uint32_t g(const U &u, uint32_t ep) { return unit_g(u, ep); }
+    __device__ static int32_t link(const U &u) { return (int32_t)u.z; }
+    __device__ static U make(uint32_t ep, uint32_t g, uint32_t parent, uint32_t keyw) {
+        return make_uint4(ep, g, parent, keyw);
+    }
+    __device__ static U cas(U *p, const U &cmp, const U &val) { return cas_unit(p, cmp, val); }
+    __device__ static bool eq(const U &a, const U &b) { return unit_eq(a, b); }
+};
+
 // One record per node, at index v (the slot's state array holds n).
-struct RecDense {
+struct RecDense : UnitOps16 {
     static constexpr bool hashed = false;
     unsigned long long *st;
     __device__ uint4 *find(int v, uint32_t) const { return unit_ptr(st, v, 0); }
     __device__ uint4 *claim(int v, uint32_t) const { return unit_ptr(st, v, 0); }
     __device__ uint32_t keyw(int) const { return 0u; }
+};
+
+// One 16-byte pair per node: a 64-bit (g << 32 | parent) word per direction,
+// all-ones = unreached.  Two nodes share a 32-byte sector, which pays where
+// node ids have spatial locality (grids in row order, points in Morton
+// order): a search's neighbours are then often in the same sector.  The
+// price is a touched log and a reset pass after each query (full-sector
+// stores of the logged nodes' sectors).
+struct RecPair16 {
+    using U = unsigned long long;
+    static constexpr bool hashed = false;
+    static constexpr bool logs = true;
+    unsigned long long *st;
+    __device__ U *find(int v, uint32_t) const { return st + 2 * (size_t)v; }
+    __device__ U *claim(int v, uint32_t) const { return st + 2 * (size_t)v; }
+    __device__ uint32_t keyw(int) const { return 0u; }
+    __device__ static U ld(const U *p) { return __ldcg(p); }
+    __device__ static uint32_t g(const U &u, uint32_t) { return min(st_g(u), INF_G); }
+    __device__ static int32_t link(const U &u) { return st_parent(u); }
+    __device__ static U make(uint32_t, uint32_t g, uint32_t parent, uint32_t) {
+        return st_make(g, (int32_t)parent);
+    }
+    __device__ static U cas(U *p, const U &cmp, const U &val) { return atomicCAS(p, cmp, val); }
+    __device__ static bool eq(const U &a, const U &b) { return a == b; }
 };
 
 // Open addressing: 2^bits records, multiplicative hashing, linear probing.
@@ -172,7 +210,7 @@ struct RecDense {
 // closed set of a search that touches far fewer nodes than the graph holds:
 // the table is sized to the touched set, not to n.
 constexpr int HASH_PROBES = 256;  // probe limit before the table counts as full
-struct RecHash {
+struct RecHash : UnitOps16 {
     static constexpr bool hashed = true;
     unsigned long long *st;
     uint32_t mask;
@@ -217,14 +255,14 @@ __device__ inline int32_t write_path_bidir(const DevGraph &G, const Rec &R, uint
     // label of node v in direction dir (unit absent: unreached) and its
     // parent / successor
     auto lab = [&](int v, uint32_t dir, int32_t *link) -> uint32_t {
-        const uint4 *r = R.find(v, ep);
+        const typename Rec::U *r = R.find(v, ep);
         if (!r) {
             *link = -1;
             return INF_G;
         }
-        const uint4 u = __ldcg(r + dir);
-        *link = (int32_t)u.z;
-        return unit_g(u, ep);
+        const typename Rec::U u = Rec::ld(r + dir);
+        *link = Rec::link(u);
+        return Rec::g(u, ep);
     };
     const int32_t x = int32_t(uint32_t(mu));
     int32_t lk;
@@ -372,10 +410,14 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
         } else {
             sq->mu = ~0ull;
             // the endpoints' records (a fresh slot's table has room for two)
-            uint4 *rs = R.claim(P.s, ep);
-            uint4 *rt = R.claim(P.t, ep);
-            rs[0] = make_uint4(ep, 0u, 0xFFFFFFFFu, R.keyw(P.s));
-            rt[1] = make_uint4(ep, 0u, 0xFFFFFFFFu, 0u);
+            typename Rec::U *rs = R.claim(P.s, ep);
+            typename Rec::U *rt = R.claim(P.t, ep);
+            rs[0] = Rec::make(ep, 0u, 0xFFFFFFFFu, R.keyw(P.s));
+            rt[1] = Rec::make(ep, 0u, 0xFFFFFFFFu, 0u);
+            if constexpr (Rec::logs) {
+                B.touched[0] = P.s;
+                B.touched[1] = P.t;
+            }
             ctl->touched = 2;
             ring[0] = make_uint2((uint32_t)P.s, bi_key<Pot>(0u, 0u, pot.at(P.s)));
             ring[1] = make_uint2((uint32_t)P.t | DIR_BIT, bi_key<Pot>(0u, 1u, pot.at(P.t)));
@@ -409,7 +451,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
 
     for (;;) {
         if (do_expand) {
-            int c_f = 0, c_loc = 0;  // staged far pushes, own children
+            int c_f = 0, c_loc = 0, c_t = 0;  // staged far pushes, own children, touches
             int nf0 = 0, nf1 = 0;             // far pushes per direction (this lane)
             for (;;) {
                 const uint32_t mu = uint32_t(*(volatile unsigned long long *)&sq->mu >> 32);
@@ -476,8 +518,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     gu = en.y;  // the entry's key
                     const int u = (int)(ud & NODE_MASK);
                     const uint32_t dir = ud >> 31;
-                    const uint4 *ru = R.find(u, ep);
-                    const uint32_t gl = ru ? unit_g(__ldcg(ru + dir), ep) : INF_G;
+                    const typename Rec::U *ru = R.find(u, ep);
+                    const uint32_t gl = ru ? Rec::g(Rec::ld(ru + dir), ep) : INF_G;
                     bool cur = false;
                     if constexpr (Pot::on) {
                         // the entry is current when its key is the label's key
@@ -509,11 +551,11 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     const int k = kb + lane;
                     bool live = false, first = false;
                     uint2 pv = make_uint2(0u, 0u);  // {pt(v), ps(v)}
-                    uint4 *rv = nullptr;           // v's record
+                    typename Rec::U *rv = nullptr;  // v's record
                     int v = 0;
                     uint32_t ng = 0, dir = 0;
                     uint32_t uo = 0;
-                    uint4 uf = make_uint4(0u, 0u, 0u, 0u), ur = uf;
+                    typename Rec::U uf{}, ur{};
                     if (k < total) {
                         const int o = row_owner(wr, k);
                         uo = (uint32_t)wr.u[o];
@@ -535,8 +577,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                             // the node's record: both units, one sector
                             rv = R.claim(v, ep);
                             if (rv) {
-                                uf = __ldcg(rv);
-                                ur = __ldcg(rv + 1);
+                                uf = Rec::ld(rv);
+                                ur = Rec::ld(rv + 1);
                             } else {
                                 atomicOr(&sq->status, ST_OVERFLOW);  // the slot's table is full
                                 live = false;
@@ -544,8 +586,8 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         }
                     }
                     if (live) {
-                        const uint4 mine = dir ? ur : uf;
-                        const uint32_t go = unit_g(dir ? uf : ur, ep);
+                        const typename Rec::U mine = dir ? ur : uf;
+                        const uint32_t go = Rec::g(dir ? uf : ur, ep);
                         if (go < INF_G) {
                             // the two searches meet over this arc
                             const uint64_t c = (uint64_t)ng + go;
@@ -554,11 +596,11 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                 atomicMin(&sq->mu, (c << 32) | x);
                             }
                         }
-                        live = ng < unit_g(mine, ep);
+                        live = ng < Rec::g(mine, ep);
                         if (live) {
-                            const uint4 nv = make_uint4(ep, ng, uo & NODE_MASK, dir ? 0u : R.keyw(v));
-                            uint4 *w = rv + dir;
-                            uint4 c0 = mine;
+                            const typename Rec::U nv = Rec::make(ep, ng, uo & NODE_MASK, dir ? 0u : R.keyw(v));
+                            typename Rec::U *w = rv + dir;
+                            typename Rec::U c0 = mine;
                             live = false;
                             // bounded: contention on one unit comes from at
                             // most the CTA's own threads
@@ -567,14 +609,14 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                     atomicOr(&sq->status, ST_TIMEOUT);
                                     break;
                                 }
-                                const uint4 got = cas_unit(w, c0, nv);
-                                if (unit_eq(got, c0)) {
+                                const typename Rec::U got = Rec::cas(w, c0, nv);
+                                if (Rec::eq(got, c0)) {
                                     live = true;
-                                    first = unit_g(c0, ep) >= INF_G;
+                                    first = Rec::g(c0, ep) >= INF_G;
                                     break;
                                 }
                                 c0 = got;
-                                if (ng >= unit_g(c0, ep)) break;
+                                if (ng >= Rec::g(c0, ep)) break;
                             }
                         }
                     }
@@ -617,7 +659,13 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     }
                     stage_push(to_far, make_uint2(vd, nk), sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f,
                                ctl, 0);
-                    if (first) n_first++;
+                    if constexpr (Rec::logs) {
+                        // first touches of either direction (a node may be
+                        // logged twice; the reset takes it twice)
+                        stage_push(first, v, wr.st, c_t, &ctl->touched, B.touched, 0, 2 * (int64_t)G.n, ctl, 0);
+                    } else if (first) {
+                        n_first++;
+                    }
                 }
                 __syncwarp();
                 // 3. retire the chunk (its children are already counted)
@@ -625,6 +673,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                 if (*(volatile int *)&sq->status & ST_TIMEOUT) break;
             }
             stage_flush(sf2, c_f, &sq->far_cnt, fcur, nfar, B.cap_f, ctl, 0);
+            if constexpr (Rec::logs) stage_flush(wr.st, c_t, &ctl->touched, B.touched, 0, 2 * (int64_t)G.n, ctl, 0);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 nf0 += __shfl_xor_sync(FULL, nf0, o);

@@ -81,6 +81,7 @@ struct ddp_server {
     std::mutex mu;
     ddp_graph *g = nullptr;
     int hkind = DDP_H_ZERO;
+    int hk = 0;  // k_batch instance (heuristic kind and record layout)
     ddp_opts o{};
     cudaStream_t stream = nullptr;
     int block = 512;
@@ -441,7 +442,7 @@ int launch(ddp_server *s) {
     A.inflight = s->d_inflight;
     DDP_CUDA(cudaMemsetAsync(s->sa.ctl, 0, sizeof(SearchCtl) * (size_t)s->sa.nslots, s->stream));
     DDP_CUDA(cudaMemsetAsync(s->d_work + 2, 0, sizeof(int) * 2, s->stream));
-    cudaError_t e = launch_slots(s->hkind, s->sa.nslots, s->block, false, graph_view(s->g), s->sa, A, s->stream);
+    cudaError_t e = launch_slots(s->hk, s->sa.nslots, s->block, false, graph_view(s->g), s->sa, A, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "serving kernel launch");
     s->running = true;
     s->launches++;
@@ -487,13 +488,13 @@ int ddp_serve_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, int64_t 
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
     // slots: occupancy, then the memory budget (half of free memory)
-    const int per_sm = std::max(1, slots_per_sm(hkind, s->block));
+    s->hk = kernel_hk(hkind, g->d_xy != nullptr, false);
+    const int per_sm = std::max(1, slots_per_sm(s->hk, s->block));
     int nslots = per_sm * device_sms();
     if (s->o.grid > 0) nslots = std::min(nslots, s->o.grid);
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    const int hops = (hkind == DDP_H_BFS_HOPS || hkind == DDP_H_BFS_CAPPED ? SLOT_HOPS : 0) |
-                     (is_bidir_kind(hkind) ? SLOT_PAIR : 0);  // slot layout
+    const int hops = hk_slot_kind(s->hk);  // slot layout
     // queue capacities: what each slot's share of half the free memory
     // holds after its state, up to the batch engine's sizes (n + 4096 near,
     // 2n + 4096 far); at least 64k.  A request that still outgrows its slot

@@ -36,11 +36,17 @@ int hash_bits(int32_t n) {
 }
 
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind, int hbits) {
-    const bool pair = (kind & SLOT_PAIR) != 0;
+    const bool p16 = (kind & SLOT_PAIR16) != 0;
+    const bool pair = (kind & SLOT_PAIR) != 0 || p16;
     const size_t recs = (kind & SLOT_HASH) ? ((size_t)1 << hbits) : (size_t)n;
     size_t b = 0;
-    b += sizeof(unsigned long long) * recs * (pair ? 4 : 1);  // state
-    if (!pair) b += sizeof(int32_t) * (size_t)n;                     // touched
+    if (p16) {
+        b += sizeof(unsigned long long) * 2 * (size_t)((n + 1) & ~1);  // state (an even node count)
+        b += sizeof(int32_t) * 2 * (size_t)n;                          // touched (both directions)
+    } else {
+        b += sizeof(unsigned long long) * recs * (pair ? 4 : 1);  // state
+        if (!pair) b += sizeof(int32_t) * (size_t)n;              // touched
+    }
     if (kind & SLOT_HOPS) b += sizeof(uint32_t) * (size_t)n;
     b += (pair ? 1 : 2) * sizeof(uint2) * (size_t)cap_q;
     b += 2 * (pair ? sizeof(uint2) : sizeof(uint4)) * (size_t)cap_f;
@@ -52,17 +58,22 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
                 cudaStream_t st, int hbits) {
     sa = SlotArrays();
     const bool hops = (kind & SLOT_HOPS) != 0;
-    const bool pair = (kind & SLOT_PAIR) != 0;
+    const bool p16 = (kind & SLOT_PAIR16) != 0;
+    const bool pair = (kind & SLOT_PAIR) != 0 || p16;
     sa.n = n;
-    sa.words = pair ? 4 : 1;
+    sa.pair = pair;
+    sa.words = p16 ? 2 : pair ? 4 : 1;
     sa.hbits = (kind & SLOT_HASH) ? hbits : 0;
-    sa.sstride = (sa.hbits ? ((int64_t)1 << sa.hbits) : (int64_t)n) * sa.words;
+    // 16-byte pairs: an even node count per slot, so that every slot (and
+    // every node's 32-byte sector) starts on a 32-byte boundary
+    sa.sstride = p16 ? 2 * (int64_t)((n + 1) & ~1)
+                     : (sa.hbits ? ((int64_t)1 << sa.hbits) : (int64_t)n) * sa.words;
     sa.nslots = nslots;
     sa.cap_q = cap_q;
     sa.cap_f = cap_f;
     const size_t S = (size_t)nslots;
     DDP_CUDA(cudaMalloc(&sa.state, sizeof(unsigned long long) * (size_t)sa.sstride * S));
-    if (!pair) DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * S));
+    if (!pair || p16) DDP_CUDA(cudaMalloc(&sa.touched, sizeof(int32_t) * (size_t)n * (p16 ? 2 : 1) * S));
     if (hops) DDP_CUDA(cudaMalloc(&sa.hops, sizeof(uint32_t) * (size_t)n * S));
     const size_t qn = pair ? 1 : 2;                             // rings per slot
     const size_t fb = pair ? sizeof(uint2) : sizeof(uint4);     // bytes per far entry
@@ -71,9 +82,10 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
     DDP_CUDA(cudaMalloc(&sa.ctl, sizeof(SearchCtl) * S));
     DDP_CUDA(cudaMalloc(&sa.epoch, sizeof(uint32_t) * S));
     DDP_CUDA(cudaMemsetAsync(sa.epoch, 0, sizeof(uint32_t) * S, st));
-    // unreached: all-ones words, or (paired records) epoch 0, which no
-    // query uses
-    DDP_CUDA(cudaMemsetAsync(sa.state, pair ? 0 : 0xFF, sizeof(unsigned long long) * (size_t)sa.sstride * S, st));
+    // unreached: all-ones words, or (epoch-tagged records) epoch 0, which
+    // no query uses
+    DDP_CUDA(cudaMemsetAsync(sa.state, (pair && !p16) ? 0 : 0xFF,
+                             sizeof(unsigned long long) * (size_t)sa.sstride * S, st));
     if (hops) DDP_CUDA(cudaMemsetAsync(sa.hops, 0, sizeof(uint32_t) * (size_t)n * S, st));
     // queue slots start as "empty" (the asynchronous engine's ring marker)
     DDP_CUDA(cudaMemsetAsync(sa.q, 0xFF, sizeof(uint2) * (size_t)cap_q * qn * S, st));
@@ -96,9 +108,9 @@ __device__ __forceinline__ SlotBufs slot_of(const SlotArrays &sa, int i) {
     SlotBufs b;
     const size_t n = (size_t)sa.n;
     b.state = sa.state + (size_t)sa.sstride * i;
-    b.touched = sa.touched ? sa.touched + n * i : nullptr;
+    b.touched = sa.touched ? sa.touched + n * (sa.words == 2 ? 2 : 1) * i : nullptr;
     b.hops = sa.hops ? sa.hops + n * i : nullptr;
-    if (sa.words == 4) {
+    if (sa.pair) {
         // paired slots: one ring; far piles of 8-byte entries (the uint4
         // pointers only carry the address)
         b.q0 = sa.q + (size_t)sa.cap_q * i;
@@ -306,7 +318,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
                 *epoch = ep;
                 ctl->tag = ep << 8;
             }
-            if (bidir_hk(HK)) {
+            if (bidir_hk(HK) && !pair16_hk(HK)) {
                 // per-query epoch of the slot's records (0 = never used);
                 // tag 0 asks for the records to be cleared once the
                 // 32-bit epoch wraps
@@ -317,7 +329,7 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             t0 = global_ns();
         }
         grp.sync();
-        if (bidir_hk(HK) && *(volatile uint32_t *)&ctl->tag == 0) {
+        if (bidir_hk(HK) && !pair16_hk(HK) && *(volatile uint32_t *)&ctl->tag == 0) {
             for (size_t i = grp.rank(); i < (size_t)B.swords; i += grp.size()) B.state[i] = 0ull;
             grp.sync();
             if (grp.rank() == 0) ctl->tag = 1;
@@ -377,19 +389,21 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             if constexpr (std::is_same<Grp, CtaGroup>::value) {
                 const uint32_t ep = *(volatile uint32_t *)&ctl->tag;
                 if constexpr (HK == 5) {
-                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{}, RecDense{B.state});
+                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{}, RecDense{{}, B.state});
                 } else if constexpr (HK == 8) {
-                    const RecHash R{B.state, (1u << B.hbits) - 1u, 32 - B.hbits};
+                    const RecHash R{{}, B.state, (1u << B.hbits) - 1u, 32 - B.hbits};
                     r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{}, R);
+                } else if constexpr (HK == 9) {
+                    r = run_bidir_cta(G, B, P, ep, wrows, bq, PotNone{}, RecPair16{B.state});
                 } else {
                     const int2 sp = reinterpret_cast<const int2 *>(G.xy)[s];
                     const int2 tp = reinterpret_cast<const int2 *>(G.xy)[t];
                     if constexpr (HK == 6)
                         r = run_bidir_cta(G, B, P, ep, wrows, bq, PotEuclid{G.xy, sp, tp, G.rho_fp / 65536.0},
-                                          RecDense{B.state});
+                                          RecDense{{}, B.state});
                     else
                         r = run_bidir_cta(G, B, P, ep, wrows, bq, PotManhattan{G.xy, sp, tp, G.wmin},
-                                          RecDense{B.state});
+                                          RecDense{{}, B.state});
                 }
             }
         } else {
@@ -406,10 +420,13 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
             int32_t len = 0;
             if (!(st & (ST_OVERFLOW | ST_TIMEOUT)) && A.paths) {
                 if (HK == 8)
-                    len = write_path_bidir(G, RecHash{B.state, (1u << B.hbits) - 1u, 32 - B.hbits}, ctl->tag, s,
+                    len = write_path_bidir(G, RecHash{{}, B.state, (1u << B.hbits) - 1u, 32 - B.hbits}, ctl->tag, s,
                                            t, bq->mu, A.paths + (size_t)q * A.path_cap, A.path_cap, &ctl->status);
+                else if (pair16_hk(HK))
+                    len = write_path_bidir(G, RecPair16{B.state}, ctl->tag, s, t, bq->mu,
+                                           A.paths + (size_t)q * A.path_cap, A.path_cap, &ctl->status);
                 else if (bidir_hk(HK))
-                    len = write_path_bidir(G, RecDense{B.state}, ctl->tag, s, t, bq->mu,
+                    len = write_path_bidir(G, RecDense{{}, B.state}, ctl->tag, s, t, bq->mu,
                                            A.paths + (size_t)q * A.path_cap, A.path_cap, &ctl->status);
                 else
                     len = write_path(B, s, t, A.paths + (size_t)q * A.path_cap, A.path_cap, G.n,
@@ -446,7 +463,16 @@ __device__ void batch_loop(const Grp &grp, const DevGraph &G0, const SlotBufs &B
         }
         grp.sync();
         const int cnt = *(volatile int *)&ctl->touched;
-        if (!bidir_hk(HK)) {  // paired records need no reset: the next query has a new epoch
+        if (pair16_hk(HK)) {
+            // every word of a finished slot returns to all-ones, so the whole
+            // 32-byte sector holding a logged node (it and its neighbour
+            // node) is written: a full-sector store needs no read of the
+            // old sector
+            ulonglong4_32a ones;
+            ones.x = ones.y = ones.z = ones.w = ~0ull;
+            for (int i = grp.rank(); i < cnt; i += grp.size())
+                reinterpret_cast<ulonglong4_32a *>(B.state)[B.touched[i] >> 1] = ones;
+        } else if (!bidir_hk(HK)) {  // epoch-tagged records need no reset: the next query has a new epoch
             for (int i = grp.rank(); i < cnt; i += grp.size()) B.state[B.touched[i]] = ~0ull;
         }
         grp.sync();
@@ -653,27 +679,58 @@ static cudaError_t coop_launch(K kernel, int grid, int block, void **args, cudaS
 
 static bool is_bfs_kind(int k) { return k == DDP_H_BFS_HOPS || k == DDP_H_BFS_CAPPED; }
 
-// Slot layout a batch heuristic kind needs.
-static int slot_kind(int hkind) {
-    return (is_bfs_kind(hkind) ? SLOT_HOPS : 0) | (is_bidir_kind(hkind) ? SLOT_PAIR : 0);
-}
-
 // Heuristic kind of the single-query engine that re-runs a batch query
 // (the bidirectional form has no single-query counterpart: plain Dijkstra
 // order gives the same cost).
 static int rerun_kind(int hkind) { return is_bidir_kind(hkind) ? DDP_H_ZERO : hkind; }
 
-// The batch kernel instance for a heuristic kind.
-static const void *batch_kernel(int hkind, bool hashed = false) {
-    if (hashed && hkind == DDP_H_BIDIR) return (const void *)k_batch<8>;
-    if (is_bfs_kind(hkind)) return (const void *)k_batch<1>;
-    if (hkind == DDP_H_MANHATTAN) return (const void *)k_batch<2>;
-    if (hkind == DDP_H_EUCLID) return (const void *)k_batch<3>;
-    if (hkind == DDP_H_LANDMARK) return (const void *)k_batch<4>;
-    if (hkind == DDP_H_BIDIR) return (const void *)k_batch<5>;
-    if (hkind == DDP_H_BIDIR_EUCLID) return (const void *)k_batch<6>;
-    if (hkind == DDP_H_BIDIR_MANHATTAN) return (const void *)k_batch<7>;
-    return (const void *)k_batch<0>;
+// The k_batch instance of a heuristic kind.  Bidirectional kinds also pick
+// their record layout: hashed records on request (DDP_OPT_HASH, plain
+// kind); for the plain kind on graphs with coordinates, whose numbering
+// (Morton order of points) puts a search's neighbours in shared sectors,
+// 16-byte pairs (8-9 % more serving capacity on the 8M-point graph); else
+// 32-byte epoch-tagged records (the potential-steered kinds too: on the
+// 2048^2 maze they were faster, 16.4 against 17.8 ms).
+int kernel_hk(int hkind, bool has_xy, bool hash) {
+    if (is_bfs_kind(hkind)) return 1;
+    if (hkind == DDP_H_MANHATTAN) return 2;
+    if (hkind == DDP_H_EUCLID) return 3;
+    if (hkind == DDP_H_LANDMARK) return 4;
+#ifdef DDP_BIDIR_RECORDS32
+    has_xy = false;  // build option: 32-byte records on every graph
+#endif
+    if (hkind == DDP_H_BIDIR) return hash ? 8 : has_xy ? 9 : 5;
+    if (hkind == DDP_H_BIDIR_EUCLID) return 6;
+    if (hkind == DDP_H_BIDIR_MANHATTAN) return 7;
+    return 0;
+}
+
+// Slot layout of a k_batch instance.
+int hk_slot_kind(int hk) {
+    switch (hk) {
+    case 1: return SLOT_HOPS;
+    case 5:
+    case 6:
+    case 7: return SLOT_PAIR;
+    case 8: return SLOT_PAIR | SLOT_HASH;
+    case 9: return SLOT_PAIR16;
+    default: return 0;
+    }
+}
+
+static const void *batch_kernel_hk(int hk) {
+    switch (hk) {
+    case 1: return (const void *)k_batch<1>;
+    case 2: return (const void *)k_batch<2>;
+    case 3: return (const void *)k_batch<3>;
+    case 4: return (const void *)k_batch<4>;
+    case 5: return (const void *)k_batch<5>;
+    case 6: return (const void *)k_batch<6>;
+    case 7: return (const void *)k_batch<7>;
+    case 8: return (const void *)k_batch<8>;
+    case 9: return (const void *)k_batch<9>;
+    default: return (const void *)k_batch<0>;
+    }
 }
 
 // Nodes a capped heuristic BFS reaches before it stops (at the end of the
@@ -692,28 +749,31 @@ cudaError_t svc_run_direct(const SvcSub *subs, int nsub, cudaStream_t st) {
     return cudaStreamSynchronize(st);
 }
 
-cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
+cudaError_t launch_slots(int hk, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
                          cudaStream_t st) {
     void *args[] = {&G, &sa, &A};
-    const void *fn = batch_kernel(hkind);
+    const void *fn = batch_kernel_hk(hk);
     if (coop) return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, st);
     return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, st);
 }
 
-int slots_per_sm(int hkind, int block) {
+int slots_per_sm(int hk, int block) {
     int per_sm = 0;
-    const void *fn = batch_kernel(hkind);
+    const void *fn = batch_kernel_hk(hk);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
     return per_sm;
 }
 
 int device_sms() { return sm_count(); }
 
-// The bidirectional search keys its buckets by g and each side only runs
-// to about half the distance, so narrower buckets pay (C4 family, 4,096
-// pairs: width 5 -> 319k queries/s, 8 -> 338k, 12 -> 314k, 25 -> 199k).
+// The bidirectional search keys its buckets by g.  On random digraphs (huge
+// frontiers) narrow buckets pay (C4 family, 4,096 pairs: width 5 -> 319k
+// queries/s, 8 -> 338k, 12 -> 314k, 25 -> 199k); on graphs with
+// coordinates (thin frontiers) wide ones do (8M-point geometric graph,
+// serving: width 27k -> 1.58k, 82k -> 1.90k queries/s; 2048^2 maze with unit
+// weights: width 1-2 best).
 uint32_t auto_delta_bidir(const ddp_graph *g) {
-    const uint32_t d = (g->wmin + g->wmax) / 12;
+    const uint32_t d = (g->wmin + g->wmax) / (g->d_xy ? 4 : 12);
     return d < 1 ? 1 : d;
 }
 
@@ -1231,7 +1291,7 @@ struct ddp_batch {
     int32_t launches = 0;
     int group = 1;  // CTAs per query slot
     bool no_graph = false;
-    bool hashed = false;  // DDP_OPT_HASH: hashed records in bidirectional slots
+    int hk = 0;  // k_batch instance (heuristic kind and record layout)
     // CUDA graph of the last device-pointer solve and the kernel arguments
     // it was captured with: a replay is valid only while a fresh launch
     // would pass exactly the same arguments (graph arrays, landmark table,
@@ -1314,7 +1374,7 @@ static cudaError_t batch_launch_args(ddp_batch *b, DevGraph G, BatchArgs A) {
     const int grid = b->sa.nslots * b->group;
     SlotArrays sa = b->sa;
     void *args[] = {&G, &sa, &A};
-    const void *fn = batch_kernel(b->hkind, b->hashed);
+    const void *fn = batch_kernel_hk(b->hk);
     if (b->group > 1)
         return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
     return cudaLaunchKernel(fn, dim3(grid), dim3(b->block), args, 0, b->stream);
@@ -1369,8 +1429,8 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     }
     // slots: occupancy-limited, then memory-limited (half of free memory)
     int per_sm = 0;
-    b->hashed = hkind == DDP_H_BIDIR && (b->o.flags & DDP_OPT_HASH) != 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(hkind, b->hashed), b->block, 0);
+    b->hk = kernel_hk(hkind, g->d_xy != nullptr, (b->o.flags & DDP_OPT_HASH) != 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_hk(b->hk), b->block, 0);
     b->group = is_bidir_kind(hkind) ? 1 : std::max(1, b->o.group);  // bidirectional slots are one CTA
     const int coresident = std::max(1, per_sm) * sm_count();
     if (b->group > coresident) b->group = coresident;
@@ -1386,8 +1446,8 @@ int ddp_batch_create(ddp_graph *g, int32_t hkind, const ddp_opts *opts, ddp_batc
     // the far pile holds every open node beyond the current bucket: twice the
     // node count leaves room for stale copies between compactions
     const int64_t cap_f = b->o.queue_cap > 0 ? b->o.queue_cap : 2 * (int64_t)g->n + 4096;
-    const int skind = slot_kind(hkind) | (b->hashed ? SLOT_HASH : 0);
-    const int hb = b->hashed ? hash_bits(g->n) : 0;
+    const int skind = hk_slot_kind(b->hk);
+    const int hb = (skind & SLOT_HASH) ? hash_bits(g->n) : 0;
     const size_t per = slot_bytes(g->n, cap, cap_f, skind, hb);
     const size_t budget = freeb / 2;
     if ((size_t)nslots * per > budget) nslots = (int)std::max<size_t>(1, budget / per);

@@ -14,6 +14,7 @@ struct SlotArrays {
     int words = 1;        // 64-bit state words per node: 1, or 4 (paired slots: a 32-byte record)
     int64_t sstride = 0;  // state words per slot
     int hbits = 0;        // hashed paired slots: log2 of the records per slot
+    bool pair = false;    // bidirectional queue layout (one ring, 8-byte far entries)
     int64_t cap_q = 0, cap_f = 0;
     unsigned long long *state = nullptr;  // nslots x n x words
     int32_t *touched = nullptr;           // nslots x n (null for paired slots)
@@ -84,12 +85,18 @@ struct BatchArgs {
 inline bool is_bidir_kind(int k) {
     return k == DDP_H_BIDIR || k == DDP_H_BIDIR_EUCLID || k == DDP_H_BIDIR_MANHATTAN;
 }
-// 8: DDP_H_BIDIR with hashed records (DDP_OPT_HASH)
-constexpr bool bidir_hk(int hk) { return hk >= 5 && hk <= 8; }
+// 8: DDP_H_BIDIR with hashed records (DDP_OPT_HASH); 9: DDP_H_BIDIR with
+// 16-byte pairs (graphs with coordinates)
+constexpr bool bidir_hk(int hk) { return hk >= 5 && hk <= 9; }
+constexpr bool pair16_hk(int hk) { return hk == 9; }
+int kernel_hk(int hkind, bool has_xy, bool hash);
+int hk_slot_kind(int hk);
 
 // Slot kinds (bits): a per-target hop array; paired forward/reverse state;
 // paired records in a hash table of 2^hbits records instead of one per node.
-enum { SLOT_HOPS = 1, SLOT_PAIR = 2, SLOT_HASH = 4 };
+// SLOT_PAIR16: 16-byte pairs (one 64-bit word per direction), a touched
+// log of 2n entries and the paired queue layout.
+enum { SLOT_HOPS = 1, SLOT_PAIR = 2, SLOT_HASH = 4, SLOT_PAIR16 = 8 };
 size_t slot_bytes(int32_t n, int64_t cap_q, int64_t cap_f, int kind, int hbits = 0);
 // log2 of the hashed records per slot for an n-node graph
 int hash_bits(int32_t n);
@@ -99,9 +106,9 @@ int slots_alloc(SlotArrays &sa, int32_t n, int nslots, int64_t cap_q, int64_t ca
                 cudaStream_t st, int hbits = 0);
 void slots_free(SlotArrays &sa);
 uint32_t *heuristic_hops_ptr(const ddp_heuristic *h);
-cudaError_t launch_slots(int hkind, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
+cudaError_t launch_slots(int hk, int grid, int block, bool coop, DevGraph G, SlotArrays sa, BatchArgs A,
                          cudaStream_t st);
-int slots_per_sm(int hkind, int block);
+int slots_per_sm(int hk, int block);
 int device_sms();
 uint32_t auto_delta(const ddp_graph *g);
 uint32_t auto_delta_bidir(const ddp_graph *g);
