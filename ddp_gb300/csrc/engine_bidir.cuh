@@ -1,20 +1,29 @@
 // Bidirectional one-CTA search: a forward search from s over the CSR and a
 // reverse search from t over the reverse CSR, run together by one CTA until
-// they meet.  No heuristic and no per-graph table: both searches are keyed
-// by g, so on graphs of small hop diameter two balls of half the radius
-// replace one ball of the full radius (orders of magnitude fewer nodes on
-// random digraphs).
+// they meet.  No per-graph table: the plain kind keys both searches by g,
+// so on graphs of small hop diameter two balls of half the radius replace
+// one ball of the full radius (orders of magnitude fewer nodes on random
+// digraphs); on graphs with coordinates the searches may key by g plus the
+// average of two coordinate potentials (bidirectional A*, section
+// "potentials" below).
 //
-// Layout: one 32-byte record per node (one DRAM sector), two 16-byte units,
-// forward then reverse, each {epoch, g, parent (reverse: successor), 0}.
-// Loading v's record gives the label being relaxed and the other side's
-// label for the meeting test.  A unit whose epoch is not the current
-// query's reads as unreached, so a slot is never reset between queries:
-// each query only advances the slot's epoch.  A label changes by one
-// 128-bit compare-and-swap of its unit (epoch, g and parent together).
+// Labels: each node has a record of two units, forward then reverse, each a
+// (g, parent) label (reverse: successor toward t).  Loading v's record gives
+// the label being relaxed and the other side's label for the meeting test;
+// a label changes by one compare-and-swap of its unit.  Three layouts
+// (section "record layouts" below):
+//   RecDense   32 bytes per node (one DRAM sector), 16-byte units
+//              {epoch, g, parent, 0}.  A unit whose epoch is not the current
+//              query's reads as unreached, so a slot is never reset between
+//              queries: each query only advances the slot's epoch.
+//   RecPair16  16 bytes per node, a 64-bit (g << 32 | parent) word per
+//              direction; two nodes share a sector, which pays where node
+//              ids have spatial locality.  Needs a touched log and a reset.
+//   RecHash    an open-addressing table of epoch-tagged records sized to the
+//              touched set instead of n.
 // Entries carry their direction in the top bit of the node id: ring and far
-// entries are {v | dir << 31, g} (the key is g).  The ring holds one bucket;
-// when it is full, entries stay in the far pile.
+// entries are {v | dir << 31, key}.  The ring holds one bucket; when it is
+// full, entries stay in the far pile.
 //
 // Work distribution is the asynchronous engine's (engine_async.cuh): the
 // current bucket (keys below the thresholds) is a pool that warps drain
@@ -36,10 +45,11 @@
 // heavy out-arcs then advances the forward side alone instead of letting the
 // reverse ball grow far past the meeting radius.
 //
-// Stop rule (bidirectional Dijkstra): after a bucket is drained, every node
-// with a forward distance below the smallest open forward key a is final
-// and expanded, and likewise below b in reverse.  When a + b >= mu, a
-// shorter s-t path P would hold an arc (x, y) with d_s(x) < a and
+// Stop rule (bidirectional Dijkstra; stated here for keys equal to g, and
+// with 2 mu in place of mu for potential keys): after a bucket is drained,
+// every node with a forward distance below the smallest open forward key a
+// is final and expanded, and likewise below b in reverse.  When
+// a + b >= mu, a shorter s-t path P would hold an arc (x, y) with d_s(x) < a and
 // d_t(y) < b; both ends were expanded with final labels, and whichever
 // expansion read the other's word second saw it final (labels are
 // installed by an atomic that completes before the entry is pushed, and
