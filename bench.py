@@ -93,7 +93,8 @@ def args_parse():
     p.add_argument("--hash", action="store_true",
                    help="bidirectional slots keep their closed set in a hash table (DDP_OPT_HASH)")
     p.add_argument("--dyn-group", type=int, default=0,
-                   help="dynamic configs: CTAs of each update batch (0/1 = one CTA, more = cooperative grid)")
+                   help="dynamic configs: CTAs of each update batch (0 = the initial search's grid, "
+                        "1 = the one-CTA kernel, more = a cooperative grid of that many)")
     p.add_argument("--group", type=int, default=19, help="CTAs per query slot (with --no-tune)")
     p.add_argument("--no-tune", action="store_true",
                    help="take group/block/delta/K from the flags instead of the autotuner")
@@ -487,6 +488,7 @@ def bench_dynamic(a, c):
     dyn = d.DynamicSearch(dg, s, t, d.H_BFS_HOPS, grid=a.slots, group=a.dyn_group)
     t_init = time.perf_counter() - t0
     cost0 = dyn.cost
+    search_ctas, update_ctas = dyn.grid
     nb = c["batches"]
     sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}
     off, col, ww = g.off[:-1].copy(), g.col.copy(), g.w.copy()
@@ -531,7 +533,7 @@ def bench_dynamic(a, c):
            "dtype": "int32", "data": "synthetic (seeded generators)",
            "config": {"workload": workload, "n": g.n, "e": g.e,
                       "updates_per_batch_mean": float(np.mean(np.diff(bounds))),
-                      "update_ctas": max(1, a.dyn_group)},
+                      "search_ctas": search_ctas, "update_ctas": update_ctas},
            "batch_ms": {"p50": 1000 * _pct(dyn_t, 50), "p99": 1000 * _pct(dyn_t, 99),
                         "initial_search_ms": 1000 * t_init},
            "gpu_from_scratch_ms_per_batch": 1000 * float(np.mean(scratch_t)),

@@ -611,6 +611,13 @@ class DynamicSearch:
                 "expanded", "scanned"]
         return dict(zip(keys, st.tolist()))
 
+    @property
+    def grid(self) -> tuple:
+        """(CTAs of the initial search, CTAs of each update batch)."""
+        a, b = C.c_int32(), C.c_int32()
+        check(lib().ddp_dyn_grid(self.handle, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def close(self):
         if self.handle:
             lib().ddp_dyn_free(self.handle)

@@ -58,6 +58,7 @@ SIGNATURES = {
     "ddp_dyn_cost": (C.c_int, [vp, i32p]),
     "ddp_dyn_path": (C.c_int, [vp, i32p, C.c_int32, i32p]),
     "ddp_dyn_stats": (C.c_int, [vp, i64p]),
+    "ddp_dyn_grid": (C.c_int, [vp, i32p, i32p]),
     "ddp_kpaths": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, i32p, i32p, C.c_int64,
                               C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "ddp_dyn_free": (C.c_int, [vp]),

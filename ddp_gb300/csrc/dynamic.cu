@@ -854,6 +854,13 @@ int ddp_dyn_stats(const ddp_dyn *d, int64_t *stats) {
     return DDP_OK;
 }
 
+int ddp_dyn_grid(const ddp_dyn *d, int32_t *search_ctas, int32_t *update_ctas) {
+    if (!d || !search_ctas || !update_ctas) return fail(DDP_ERR_INVALID, "null argument");
+    *search_ctas = d->grid;
+    *update_ctas = d->upd_grid;
+    return DDP_OK;
+}
+
 int ddp_dyn_free(ddp_dyn *d) {
     if (!d) return DDP_OK;
     slots_free(d->sa);

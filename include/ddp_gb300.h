@@ -253,6 +253,9 @@ int ddp_dyn_path(ddp_dyn *d, int32_t *buf, int32_t cap, int32_t *len);
  * phases, invalidated nodes, re-seeded nodes, relaxed arc heads, lowered hop
  * counts, expanded nodes, scanned arcs (10 values). */
 int ddp_dyn_stats(const ddp_dyn *d, int64_t *stats);
+/* CTAs of the initial search and of each update batch's repair and resumed
+ * search (opts.grid and opts.group as resolved against the device). */
+int ddp_dyn_grid(const ddp_dyn *d, int32_t *search_ctas, int32_t *update_ctas);
 int ddp_dyn_free(ddp_dyn *d);
 
 /* Up to k successive source -> target paths by last-arc deletion

@@ -21,6 +21,12 @@ def _run(d, O, g, batches, s, t, hkind=None, check_csr_every=1, **opts):
     hkind = d.H_BFS_HOPS if hkind is None else hkind
     dg = d.DeviceGraph.from_csr(g)
     dyn = d.DynamicSearch(dg, s, t, hkind, **opts)
+    search_ctas, update_ctas = dyn.grid
+    assert search_ctas >= 1 and update_ctas >= 1
+    if opts.get("group", 0) > 0:
+        assert update_ctas == opts["group"]  # far below the co-resident limit here
+    else:
+        assert update_ctas == search_ctas  # default: the initial search's grid
     off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
     assert dyn.cost == _scratch_cost(O, off, col, w, s, t)
     for bi, (fl, uu, vv, ww) in enumerate(batches):
@@ -43,12 +49,13 @@ def _split(fl, u, v, w, per):
     return [(fl[i:i + per], u[i:i + per], v[i:i + per], w[i:i + per]) for i in range(0, len(fl), per)]
 
 
-@pytest.mark.parametrize("group", [1, 8])
+@pytest.mark.parametrize("group", [0, 1, 8])
 def test_dynamic_random_batches(gpu, oracle, group):
     """The 1M-node update workload's shape at 1/50 scale (20k nodes, avg
     out-degree 10): inserts of new arcs and deletes of existing non-chain
-    arcs, weights in [1,1000].  Update batches on one CTA (the default) and
-    on a cooperative grid of 8 CTAs."""
+    arcs, weights in [1,1000].  Update batches on the initial search's grid
+    (the default), on the one-CTA kernel and on a cooperative grid of 8
+    CTAs."""
     d = gpu
     base = d.gen_random_chain(20000, 10, 1, 1000, 303)
     fl, u, v, w = d.gen_updates(base, 25, 200, 100, 1, 1000, 304)
