@@ -644,6 +644,12 @@ int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32
     const int32_t n = g->n;
     ups.clear();
     ups.reserve((size_t)nupd);
+    // forward arc slots hit by deletes and weight changes, each with its
+    // weight before the batch ({slot, u, v, w0}); an arc hit more than once
+    // (say lighter, then heavier than before) is classified once, from its
+    // pre-batch and final state, so no repair record carries a weight the
+    // arc no longer has
+    std::vector<int4> hit;
     // deletes and weight changes resolve against the pre-batch graph
     // (removeDelEdges runs before mergeDiff, DA_dyn_cpu.cu:1473-1484)
     for (int32_t i = 0; i < nupd; i++) {
@@ -663,21 +669,28 @@ int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32
                 jr = j;
                 break;
             }
-        const uint32_t wold = m->arc[(size_t)jf].y;
+        hit.push_back(make_int4(jf, a, b, (int)m->arc[(size_t)jf].y));
         if (flag[i] == 0) {
             m->arc[(size_t)jf].x = 0xFFFFFFFFu;
             if (jr >= 0) m->rarc[(size_t)jr].x = 0xFFFFFFFFu;
-            ups.push_back(make_int4(UPD_TREE, a, b, 0));
         } else {
             m->arc[(size_t)jf].y = w[i];
             if (jr >= 0) m->rarc[(size_t)jr].y = w[i];
-            if (w[i] < wold) ups.push_back(make_int4(UPD_LIGHTER, a, b, (int)w[i]));
-            else if (w[i] > wold) ups.push_back(make_int4(UPD_TREE, a, b, 0));
             if (w[i] < g->wmin) g->wmin = w[i];
             if (w[i] > g->wmax) g->wmax = w[i];
         }
         m->dirty_arc.push_back(jf);
         if (jr >= 0) m->dirty_rarc.push_back(jr);
+    }
+    // repair records: a deleted or heavier arc may be a tree arc of its head
+    // (subtree check); a lighter one relaxes its head with its final weight
+    std::stable_sort(hit.begin(), hit.end(), [](const int4 &x, const int4 &y) { return x.x < y.x; });
+    for (size_t k = 0; k < hit.size(); k++) {
+        if (k > 0 && hit[k].x == hit[k - 1].x) continue;  // the first hit holds the pre-batch weight
+        const uint2 fin = m->arc[(size_t)hit[k].x];
+        const uint32_t w0 = (uint32_t)hit[k].w;
+        if ((int32_t)fin.x < 0 || fin.y > w0) ups.push_back(make_int4(UPD_TREE, hit[k].y, hit[k].z, 0));
+        else if (fin.y < w0) ups.push_back(make_int4(UPD_LIGHTER, hit[k].y, hit[k].z, (int)fin.y));
     }
     // inserts, appended to their rows in batch order (createDiffGraph).  When
     // a row cannot grow, everything is laid out again with fresh slack and a

@@ -69,6 +69,14 @@ namespace ddp {
 #define DDP_BIDIR_SPIN_CAP 1024
 #endif
 
+// Fewest ring entries a warp claims at once (at most 32).  A warp claims
+// ceil(available / warps) entries, clamped to [DDP_BIDIR_CLAIM_MIN, 32]:
+// a bucket of a few hundred entries then keeps every warp busy instead of
+// queueing 32-entry chunks (8 dependent rounds of arcs each) on a few.
+#ifndef DDP_BIDIR_CLAIM_MIN
+#define DDP_BIDIR_CLAIM_MIN 4
+#endif
+
 constexpr uint32_t DIR_BIT = 0x80000000u;
 constexpr uint32_t NODE_MASK = 0x7FFFFFFFu;
 
@@ -397,6 +405,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
     SearchCtl *ctl = B.ctl;
     const int lane = lane_id();
     const int warp = threadIdx.x >> 5;
+    const int nw = (int)(blockDim.x >> 5);
     WarpRows &wr = wrows[warp];
     uint2 *ring = B.q0;
     const int cap = (int)min(B.cap_q, (int64_t)0x3FFFFFFF);
@@ -484,7 +493,9 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         for (uint32_t spins = 0;; spins++) {
                             const int h = *(volatile int *)&sq->head, t = *(volatile int *)&sq->tail;
                             if (h < t) {
-                                const int k = min(32, t - h);
+                                // a small bucket is spread over the CTA's
+                                // warps instead of going to the first few
+                                const int k = min(t - h, min(32, max(DDP_BIDIR_CLAIM_MIN, (t - h + nw - 1) / nw)));
                                 if (atomicCAS(&sq->head, h, h + k) == h) {
                                     n = k;
                                     h0 = h;

@@ -134,6 +134,47 @@ def test_dynamic_weight_changes_and_unreachable(gpu, oracle):
     dyn.close()
 
 
+@pytest.mark.parametrize("heur", ["hops", "zero"])
+def test_dynamic_same_arc_twice_in_one_batch(gpu, oracle, heur):
+    """One batch changes a tree arc's weight twice: lighter, then heavier
+    than before (the arc's final weight is what the repair may use), and
+    heavier, then lighter than before; also a delete plus a weight change of
+    the same pair (the change then hits the next live parallel arc, if any).
+    Every cost equals a from-scratch oracle search on the updated graph."""
+    d = gpu
+    base = d.gen_random_chain(4000, 4, 20, 60, 77)
+    g = base.with_sentinel()
+    s, t = int(base.perm[0]), int(base.perm[-1])
+    dg = d.DeviceGraph.from_csr(g)
+    hk = d.H_BFS_HOPS if heur == "hops" else d.H_ZERO
+    dyn = d.DynamicSearch(dg, s, t, hk)
+    off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
+    rng = np.random.default_rng(5)
+    for rnd in range(9):
+        p = dyn.path()
+        assert len(p) >= 2
+        k = int(rng.integers(0, len(p) - 1))
+        a, b = int(p[k]), int(p[k + 1])
+        ends = np.append(off[1:], len(col))
+        row = np.arange(off[a], ends[a])
+        w0 = int(w[row[col[row] == b][0]])
+        if rnd % 3 == 0:
+            fl, ww = [2, 2], [1, w0 + 400]           # lighter, then heavier than before
+        elif rnd % 3 == 1:
+            fl, ww = [2, 2], [w0 + 400, max(1, w0 - 7)]  # heavier, then lighter than before
+        else:
+            fl, ww = [0, 2], [0, 1]                  # delete, then change the next parallel arc
+        cost = dyn.update(fl, [a, a], [b, b], ww)
+        off, col, w, _ = oracle.apply_batch(len(off), off, col, w, fl, [a, a], [b, b], ww)
+        want = _scratch_cost(oracle, off, col, w, s, t)
+        assert cost == want, (rnd, fl, ww, dyn.stats())
+        if want != d.INF:
+            full_off = np.concatenate([off, [len(col)]]).astype(np.int32)
+            ok, why = oracle.check_path(full_off, col, w, dyn.path(), s, t, cost)
+            assert ok, why
+    dyn.close()
+
+
 def test_dynamic_row_growth_and_relayout(gpu, oracle):
     """Many inserts into a few rows: rows move to the end of the arc array
     and the array is laid out again when it fills; the CSR stays exact."""
