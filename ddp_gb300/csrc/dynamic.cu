@@ -59,6 +59,17 @@ struct DynMirror {
     bool full = true;  // next upload sends everything
     // device side: capacities of the arc arrays and scatter staging buffers
     int64_t arc_cap = 0, rarc_cap = 0;
+    // Batches applied on the device (k_apply) leave the device arrays
+    // authoritative: `stale` says the host copy is behind them (it is read
+    // back on demand), `dev_meta` that the device row capacities and tails
+    // match the host copy (host-side changes clear it).
+    bool stale = false;
+    bool dev_meta = false;
+    int32_t *d_cap = nullptr, *d_rcap = nullptr;  // row capacities, n each
+    long long *d_tails = nullptr;                 // first unused slot: forward, reverse
+    int4 *h_ops = nullptr, *d_ops = nullptr;      // one batch {flag, u, v, w}
+    int *d_res = nullptr;                         // k_apply: records written, status
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // DDP_TRACE: around k_apply and k_dyn
     // staging of a batch's scatter lists: pinned host memory (the copy is
     // asynchronous; the buffer is reused once the graph's stream has been
     // synchronised, which every update path does) and its device twin
@@ -68,6 +79,14 @@ struct DynMirror {
     ~DynMirror() {
         cudaFree(d_stage);
         cudaFreeHost(h_stage);
+        cudaFree(d_cap);
+        cudaFree(d_rcap);
+        cudaFree(d_tails);
+        cudaFreeHost(h_ops);
+        cudaFree(d_ops);
+        cudaFree(d_res);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -172,9 +191,226 @@ __global__ void k_scatter_all(ScatterAll j) {
     else if (i < j.ka + j.kra) j.rarc[j.slots[i]] = j.vals[i];
 }
 
+// ---- update batches applied on the device ----------------------------------
+// One CTA resolves and applies a batch of at most APPLY_MAX updates with the
+// host path's semantics (the reference's: deletes and weight changes first,
+// each on the first live u->v arc of the graph as the earlier updates left
+// it; inserts appended to their rows in batch order), and writes the repair
+// records.  Ops are sorted by (tail, index) and inserts also by (head,
+// index), so each row's updates run in batch order on one thread (the
+// row's leader) while different rows run in parallel.  A first pass checks
+// that the rows that outgrow their capacity fit at the arrays' tails; if
+// not, nothing is changed and the status asks for the host path (which lays
+// the arrays out again).
+constexpr int APPLY_MAX = 4096;
+constexpr int APPLY_THREADS = 1024;
+enum { APPLY_NO_ROOM = 1 };
+
+struct ApplyArgs {
+    const int4 *ops;  // {flag, u, v, w}, batch order
+    int nops;
+    int32_t n;
+    uint2 *arc, *rarc;
+    int32_t *off, *oend, *cap, *roff, *roend, *rcap;
+    long long *tails;           // first unused slot: forward, reverse
+    long long arc_lim, rarc_lim;  // slots of the laid-out arrays
+    int4 *ups;                  // repair records {kind, u, v, w}
+    int *res;                   // [0] records written, [1] status
+};
+
+__device__ __forceinline__ bool apply_valid(const int4 &o, int32_t n) {
+    return o.x >= 0 && o.x <= 2 && o.y >= 0 && o.y < n && o.z >= 0 && o.z < n;
+}
+
+// Capacity of a row that holds `used` slots and receives `add` more:
+// unchanged when they fit, else doubled (at least 4) until they do.
+__device__ __forceinline__ long long grown_cap(int32_t used, int32_t cap, int32_t add) {
+    if ((long long)used + add <= cap) return cap;
+    long long c = max(4LL, 2LL * cap);
+    while (c < (long long)used + add) c *= 2;
+    return c;
+}
+
+// Sorts a and b (P = power of two entries each) ascending, bitonic.
+__device__ void apply_sort2(unsigned long long *a, unsigned long long *b, int P) {
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    unsigned long long x = a[i], y = a[l];
+                    if ((x > y) == up) {
+                        a[i] = y;
+                        a[l] = x;
+                    }
+                    x = b[i];
+                    y = b[l];
+                    if ((x > y) == up) {
+                        b[i] = y;
+                        b[l] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+// Moves row r (slots [beg, end)) to a fresh region of ncap slots at the
+// array's tail when ncap exceeds its capacity.
+__device__ void apply_grow_row(uint2 *arc, int32_t *beg, int32_t *end, int32_t *cap, long long *tail, int r,
+                               long long ncap) {
+    if (ncap <= cap[r]) return;
+    const int32_t b = beg[r], used = end[r] - b;
+    const long long base = atomicAdd(reinterpret_cast<unsigned long long *>(tail), (unsigned long long)ncap);
+    for (int32_t j = 0; j < used; j++) arc[base + j] = arc[b + j];
+    beg[r] = (int32_t)base;
+    end[r] = (int32_t)(base + used);
+    cap[r] = (int32_t)ncap;
+}
+
+__global__ void __launch_bounds__(APPLY_THREADS) k_apply(ApplyArgs A) {
+    extern __shared__ unsigned long long apply_smem[];
+    __shared__ unsigned long long need[2];
+    __shared__ int nrec;
+    int P = 32;
+    while (P < A.nops) P <<= 1;
+    unsigned long long *ka = apply_smem;        // (u << 32 | i), every valid op
+    unsigned long long *kb = ka + P;            // (v << 32 | i), valid inserts
+    int *hit = reinterpret_cast<int *>(kb + P);  // forward slot op i hit (-1: none)
+    uint32_t *w0 = reinterpret_cast<uint32_t *>(hit + P);  // that slot's weight before op i
+    const unsigned long long NONE = ~0ull;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        ka[i] = kb[i] = NONE;
+        if (i < A.nops) {
+            const int4 o = A.ops[i];
+            hit[i] = -1;
+            if (apply_valid(o, A.n)) {
+                ka[i] = ((unsigned long long)(uint32_t)o.y << 32) | (uint32_t)i;
+                if (o.x == 1) kb[i] = ((unsigned long long)(uint32_t)o.z << 32) | (uint32_t)i;
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        need[0] = need[1] = 0;
+        nrec = 0;
+    }
+    __syncthreads();
+    apply_sort2(ka, kb, P);
+    // room: every row that outgrows its capacity moves to the tail
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        for (int side = 0; side < 2; side++) {
+            const unsigned long long *k = side ? kb : ka;
+            if (k[p] == NONE || (p > 0 && (k[p - 1] >> 32) == (k[p] >> 32))) continue;  // not a leader
+            const int r = (int)(k[p] >> 32);
+            int32_t add = 0;
+            for (int q = p; q < P && k[q] != NONE && (k[q] >> 32) == (unsigned long long)r; q++)
+                add += A.ops[(uint32_t)k[q]].x == 1;
+            const int32_t *beg = side ? A.roff : A.off, *end = side ? A.roend : A.oend,
+                          *cap = side ? A.rcap : A.cap;
+            const long long c = grown_cap(end[r] - beg[r], cap[r], add);
+            if (c > cap[r]) atomicAdd(&need[side], (unsigned long long)c);
+        }
+    }
+    __syncthreads();
+    const bool room = A.tails[0] + (long long)need[0] <= min(A.arc_lim, (long long)INT32_MAX) &&
+                      A.tails[1] + (long long)need[1] <= min(A.rarc_lim, (long long)INT32_MAX);
+    if (!room) {
+        if (threadIdx.x == 0) {
+            A.res[0] = 0;
+            A.res[1] = APPLY_NO_ROOM;
+        }
+        return;
+    }
+    // deletes and weight changes, per tail row in batch order; then each
+    // arc hit is classified once, from its weight before the batch and its
+    // final state (deleted or heavier: subtree check; lighter: relax)
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        if (ka[p] == NONE || (p > 0 && (ka[p - 1] >> 32) == (ka[p] >> 32))) continue;
+        const int a = (int)(ka[p] >> 32);
+        int q1 = p;
+        while (q1 < P && ka[q1] != NONE && (int)(ka[q1] >> 32) == a) q1++;
+        for (int q = p; q < q1; q++) {
+            const int i = (int)(uint32_t)ka[q];
+            const int4 o = A.ops[i];
+            if (o.x == 1) continue;
+            const int b = o.z;
+            int jf = -1;
+            for (int j = A.off[a]; j < A.oend[a]; j++)
+                if ((int)A.arc[j].x == b) {
+                    jf = j;
+                    break;
+                }
+            if (jf < 0) continue;  // no such arc: nothing to do
+            const uint32_t wold = A.arc[jf].y;
+            hit[i] = jf;
+            w0[i] = wold;
+            int jr = -1;
+            for (int j = A.roff[b]; j < A.roend[b]; j++) {
+                const uint2 ra = A.rarc[j];
+                if ((int)ra.x == a && ra.y == wold) {
+                    jr = j;
+                    break;
+                }
+            }
+            if (o.x == 0) {
+                A.arc[jf].x = 0xFFFFFFFFu;
+                if (jr >= 0) A.rarc[jr].x = 0xFFFFFFFFu;
+            } else {
+                A.arc[jf].y = (uint32_t)o.w;
+                if (jr >= 0) A.rarc[jr].y = (uint32_t)o.w;
+            }
+        }
+        for (int q = p; q < q1; q++) {
+            const int i = (int)(uint32_t)ka[q];
+            if (hit[i] < 0) continue;
+            bool first = true;
+            for (int q0 = p; q0 < q && first; q0++) first = hit[(uint32_t)ka[q0]] != hit[i];
+            if (!first) continue;
+            const uint2 fin = A.arc[hit[i]];
+            int4 rec;
+            if ((int32_t)fin.x < 0 || fin.y > w0[i]) rec = make_int4(UPD_TREE, a, A.ops[i].z, 0);
+            else if (fin.y < w0[i]) rec = make_int4(UPD_LIGHTER, a, A.ops[i].z, (int)fin.y);
+            else continue;
+            A.ups[atomicAdd(&nrec, 1)] = rec;
+        }
+    }
+    __syncthreads();
+    // inserts: forward rows (leaders of ka), reverse rows (leaders of kb)
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        for (int side = 0; side < 2; side++) {
+            const unsigned long long *k = side ? kb : ka;
+            if (k[p] == NONE || (p > 0 && (k[p - 1] >> 32) == (k[p] >> 32))) continue;
+            const int r = (int)(k[p] >> 32);
+            int q1 = p;
+            int32_t add = 0;
+            for (; q1 < P && k[q1] != NONE && (int)(k[q1] >> 32) == r; q1++) add += A.ops[(uint32_t)k[q1]].x == 1;
+            if (!add) continue;
+            uint2 *arc = side ? A.rarc : A.arc;
+            int32_t *beg = side ? A.roff : A.off, *end = side ? A.roend : A.oend, *cap = side ? A.rcap : A.cap;
+            apply_grow_row(arc, beg, end, cap, A.tails + side, r, grown_cap(end[r] - beg[r], cap[r], add));
+            int32_t e = end[r];
+            for (int q = p; q < q1; q++) {
+                const int4 o = A.ops[(uint32_t)k[q]];
+                if (o.x != 1) continue;
+                arc[e++] = make_uint2((uint32_t)(side ? o.y : o.z), (uint32_t)o.w);
+                if (!side) A.ups[atomicAdd(&nrec, 1)] = make_int4(UPD_INS, o.y, o.z, o.w);
+            }
+            end[r] = e;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        A.res[0] = nrec;
+        A.res[1] = 0;
+    }
+}
+
 struct DynArgs {
     const int4 *upd;  // {kind, u, v, w}
     int nupd;
+    const int *nupd_dev;   // non-null: the record count is on the device (k_apply)
+    const int *apply_res;  // non-null: k_apply's result; a failed apply skips the launch
     int32_t *inv;     // invalidated nodes (n)
     int32_t *out;     // cost, path len, status, phases, invalidated, reseeded, relaxed, hops lowered
     int32_t *path;
@@ -230,6 +466,10 @@ __device__ __forceinline__ CtaGroup dyn_group(CtaGroup *, const SlotBufs &B) { r
 template <class Grp>
 __global__ void __launch_bounds__(512, 2)
     k_dyn(DevGraph G, SlotArrays sa, uint32_t *hops, SearchParams P, DynArgs A, DynCtl *dc) {
+    // a batch the device could not apply leaves graph and search untouched
+    // (every CTA returns here, before any barrier; the host takes over)
+    if (A.apply_res && *(volatile const int *)(A.apply_res + 1) != 0) return;
+    const int nupd = A.nupd_dev ? *(volatile const int *)A.nupd_dev : A.nupd;
     __shared__ WarpRows wrows[16];
     SlotBufs B = slot_of_dyn(sa);
     const Grp grp = dyn_group(static_cast<Grp *>(nullptr), B);
@@ -244,7 +484,7 @@ __global__ void __launch_bounds__(512, 2)
         int it = 0, nf = 0;
         // ---- A. heuristic repair: lower hops over inserted arcs ----------
         if (A.heur == 1) {
-            for (int i = rank; i < A.nupd; i += size) {
+            for (int i = rank; i < nupd; i += size) {
                 const int4 up = A.upd[i];
                 if (up.x != UPD_INS) continue;
                 const uint32_t hv = __ldcg(hops + up.z);
@@ -289,7 +529,7 @@ __global__ void __launch_bounds__(512, 2)
         // ---- B. invalidate subtrees hanging off removed / heavier tree arcs
         {
             const int PH = (it + 1) & 3;
-            for (int i = rank; i < A.nupd; i += size) {
+            for (int i = rank; i < nupd; i += size) {
                 const int4 up = A.upd[i];
                 if (up.x != UPD_TREE) continue;
                 const uint64_t sv = __ldcg(B.state + up.z);
@@ -358,7 +598,7 @@ __global__ void __launch_bounds__(512, 2)
         }
         grp.sync();
         // ---- D. relax heads of inserted / lighter arcs --------------------
-        for (int i = rank; i < A.nupd; i += size) {
+        for (int i = rank; i < nupd; i += size) {
             const int4 up = A.upd[i];
             if (up.x != UPD_INS && up.x != UPD_LIGHTER) continue;
             const uint32_t gu = st_g(__ldcg(B.state + up.y));
@@ -432,6 +672,7 @@ namespace ddp {
 int dyn_upload(ddp_graph *g, bool sync) {
     DynMirror *m = g->dyn;
     const int32_t n = g->n;
+    m->dev_meta = false;  // row capacities and tails may have changed here
     if (m->full) {
         if ((int64_t)m->arc.size() > m->arc_cap) {
             graph_free_dev(g, g->d_arc);
@@ -565,7 +806,103 @@ int dyn_upload(ddp_graph *g, bool sync) {
     return rc;
 }
 
-static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
+// Reads the device arrays back into the host copy after batches applied on
+// the device.
+int dyn_mirror_sync(ddp_graph *g) {
+    DynMirror *m = g->dyn;
+    if (!m || !m->stale) return DDP_OK;
+    const size_t n = (size_t)g->n;
+    long long tails[2];
+    DDP_CUDA(cudaStreamSynchronize(g->stream));
+    DDP_CUDA(cudaMemcpy(m->beg.data(), g->d_off, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(m->end.data(), g->d_oend, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(m->cap.data(), m->d_cap, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(m->rbeg.data(), g->d_roff, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(m->rend.data(), g->d_roend, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(m->rcap.data(), m->d_rcap, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(tails, m->d_tails, sizeof(tails), cudaMemcpyDeviceToHost));
+    m->tail = tails[0];
+    m->rtail = tails[1];
+    DDP_CUDA(cudaMemcpy(m->arc.data(), g->d_arc, sizeof(uint2) * (size_t)m->tail, cudaMemcpyDeviceToHost));
+    DDP_CUDA(cudaMemcpy(m->rarc.data(), g->d_rarc, sizeof(uint2) * (size_t)m->rtail, cudaMemcpyDeviceToHost));
+    m->stale = false;
+    return DDP_OK;
+}
+
+// Applies a batch on the device (k_apply on the graph's stream, no
+// synchronisation): the repair records go to d_ups and their count to
+// m->d_res[0]; m->d_res[1] != 0 means nothing was applied and the batch
+// must take the host path.  Returns 1 (nothing launched) when the batch is
+// too large for one CTA or a serving kernel owns the graph's updates.
+int dyn_apply_device(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
+                     const uint32_t *w, int4 *d_ups) {
+    DynMirror *m = g->dyn;
+    if (nupd > APPLY_MAX || g->hook.fn) return 1;
+    const int32_t n = g->n;
+    if (!m->h_ops) {
+        DDP_CUDA(cudaHostAlloc(&m->h_ops, sizeof(int4) * APPLY_MAX, cudaHostAllocDefault));
+        DDP_CUDA(cudaMalloc(&m->d_ops, sizeof(int4) * APPLY_MAX));
+        DDP_CUDA(cudaMalloc(&m->d_res, sizeof(int) * 2));
+        DDP_CUDA(cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      24 * APPLY_MAX));
+    }
+    if (!m->dev_meta) {
+        // the host copy is current here (only device batches make it stale,
+        // and they keep the device capacities current)
+        const long long tails[2] = {m->tail, m->rtail};
+        DDP_CUDA(cudaMemcpyAsync(m->d_cap, m->cap.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
+        DDP_CUDA(cudaMemcpyAsync(m->d_rcap, m->rcap.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
+        DDP_CUDA(cudaMemcpyAsync(m->d_tails, tails, sizeof(tails), cudaMemcpyHostToDevice, g->stream));
+        DDP_CUDA(cudaStreamSynchronize(g->stream));  // the sources are pageable
+        m->dev_meta = true;
+    }
+    // the pinned staging buffer is free: every update path synchronises the
+    // graph's stream before returning
+    for (int32_t i = 0; i < nupd; i++) {
+        m->h_ops[i] = make_int4(flag[i], u[i], v[i], (int)w[i]);
+        // admissible either way: a weight that found no arc only makes
+        // wmin smaller than it needs to be
+        if ((flag[i] == 1 || flag[i] == 2) && u[i] >= 0 && u[i] < n && v[i] >= 0 && v[i] < n) {
+            if (w[i] < g->wmin) g->wmin = w[i];
+            if (w[i] > g->wmax) g->wmax = w[i];
+        }
+    }
+    if (nupd) DDP_CUDA(cudaMemcpyAsync(m->d_ops, m->h_ops, sizeof(int4) * nupd, cudaMemcpyHostToDevice, g->stream));
+    ApplyArgs A;
+    A.ops = m->d_ops;
+    A.nops = nupd;
+    A.n = n;
+    A.arc = g->d_arc;
+    A.rarc = g->d_rarc;
+    A.off = g->d_off;
+    A.oend = g->d_oend;
+    A.cap = m->d_cap;
+    A.roff = g->d_roff;
+    A.roend = g->d_roend;
+    A.rcap = m->d_rcap;
+    A.tails = m->d_tails;
+    A.arc_lim = (long long)m->arc.size();
+    A.rarc_lim = (long long)m->rarc.size();
+    A.ups = d_ups;
+    A.res = m->d_res;
+    int P = 32;
+    while (P < nupd) P <<= 1;
+    const bool timed = trace_on();
+    if (timed && !m->ev[0])
+        for (cudaEvent_t &e : m->ev) DDP_CUDA(cudaEventCreate(&e));
+    if (timed) DDP_CUDA(cudaEventRecord(m->ev[0], g->stream));
+    k_apply<<<1, APPLY_THREADS, 24 * (size_t)P, g->stream>>>(A);
+    DDP_CUDA(cudaGetLastError());
+    if (timed) DDP_CUDA(cudaEventRecord(m->ev[1], g->stream));
+    g->update_count++;  // landmark distances no longer hold
+    m->stale = true;
+    return DDP_OK;
+}
+
+// dres: k_apply's result when the batch was applied on the device (the
+// record count is read there, and *apply_status receives its status; a
+// failed apply leaves the search untouched), else null.
+static int dyn_launch(ddp_dyn *d, int initial, int nupd, const int *dres = nullptr, int *apply_status = nullptr) {
     const bool one_cta = !initial && d->upd_grid == 1;
     ddp_graph *g = d->g;
     DevGraph G = graph_view(g);
@@ -574,6 +911,8 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
     DynArgs A;
     A.upd = d->d_upd;
     A.nupd = nupd;
+    A.nupd_dev = dres;
+    A.apply_res = dres;
     A.inv = d->d_inv;
     A.out = d->d_out;
     A.path = d->d_path;
@@ -590,9 +929,14 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd) {
     else
         DDP_CUDA(cudaLaunchCooperativeKernel((const void *)k_dyn<GridGroup>, dim3(initial ? d->grid : d->upd_grid),
                                              dim3(512), args, 0, g->stream));
+    if (dres && trace_on() && g->dyn->ev[2]) DDP_CUDA(cudaEventRecord(g->dyn->ev[2], g->stream));
     int32_t out[10];
+    int res[2] = {0, 0};
     DDP_CUDA(cudaMemcpyAsync(out, d->d_out, sizeof(out), cudaMemcpyDeviceToHost, g->stream));
+    if (dres) DDP_CUDA(cudaMemcpyAsync(res, dres, sizeof(res), cudaMemcpyDeviceToHost, g->stream));
     DDP_CUDA(cudaStreamSynchronize(g->stream));
+    if (apply_status) *apply_status = res[1];
+    if (res[1]) return DDP_OK;  // nothing ran: the caller applies the batch on the host
     if (out[2] & ST_TIMEOUT) return fail(DDP_ERR_TIMEOUT, "dynamic search: barrier wait timed out");
     if (out[2] & ST_OVERFLOW) return fail(DDP_ERR_QUEUE_OVERFLOW, "dynamic search: queue overflow");
     d->cost = out[0];
@@ -629,6 +973,9 @@ int dyn_graph_prepare(ddp_graph *g) {
     workspace_release(g);  // the single-query workspace was sized for the old arrays
     if (!g->d_oend) DDP_CUDA(cudaMalloc(&g->d_oend, sizeof(int32_t) * n));
     if (!g->d_roend) DDP_CUDA(cudaMalloc(&g->d_roend, sizeof(int32_t) * n));
+    DDP_CUDA(cudaMalloc(&m->d_cap, sizeof(int32_t) * std::max(n, 1)));
+    DDP_CUDA(cudaMalloc(&m->d_rcap, sizeof(int32_t) * std::max(n, 1)));
+    DDP_CUDA(cudaMalloc(&m->d_tails, sizeof(long long) * 2));
     return dyn_upload(g);
 }
 
@@ -637,9 +984,11 @@ int dyn_graph_prepare(ddp_graph *g) {
 int dyn_graph_apply(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
                     const uint32_t *w, std::vector<int4> &ups, bool sync) {
     const auto t0 = std::chrono::steady_clock::now();
-    g->update_count++;  // landmark distances no longer hold
     int rcp = dyn_graph_prepare(g);
     if (rcp) return rcp;
+    rcp = dyn_mirror_sync(g);
+    if (rcp) return rcp;
+    g->update_count++;  // landmark distances no longer hold
     DynMirror *m = g->dyn;
     const int32_t n = g->n;
     ups.clear();
@@ -821,10 +1170,41 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
     ddp_graph *g = d->g;
     std::lock_guard<std::mutex> lk(g->mu);
     std::vector<int4> ups;
+    const auto t0 = std::chrono::steady_clock::now();
+    if (nupd > d->upd_cap) {
+        cudaFree(d->d_upd);
+        d->d_upd = nullptr;
+        DDP_CUDA(cudaMalloc(&d->d_upd, sizeof(int4) * std::max(nupd, 1)));
+        d->upd_cap = nupd;
+    }
+    // on the device when the batch fits one CTA: k_apply, then k_dyn on the
+    // same stream (one upload, one synchronisation)
+    int rc = dyn_apply_device(g, nupd, flag, u, v, w, d->d_upd);
+    if (rc == DDP_OK) {
+        int st = 0;
+        rc = dyn_launch(d, 0, 0, g->dyn->d_res, &st);
+        if (rc) return rc;
+        if (!st) {
+            if (trace_on()) {
+                // ev[2] was recorded after k_dyn, before dyn_launch synchronised
+                float ka = 0.f, kd = 0.f;
+                cudaEventElapsedTime(&ka, g->dyn->ev[0], g->dyn->ev[1]);
+                cudaEventElapsedTime(&kd, g->dyn->ev[1], g->dyn->ev[2]);
+                trace("dyn_update: %d updates applied on the device, %.1f us in the call (k_apply %.1f us, "
+                      "k_dyn repair + search %.1f us)",
+                      nupd, std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count(),
+                      1000.0 * ka, 1000.0 * kd);
+            }
+            if (out_cost) *out_cost = d->cost;
+            return DDP_OK;
+        }
+        // no room at the arrays' tails: the host lays them out again
+    } else if (rc != 1) {
+        return rc;
+    }
     // no synchronisation after the graph scatters: k_dyn runs on the same
     // stream, and dyn_launch synchronises it before returning
-    const auto t0 = std::chrono::steady_clock::now();
-    int rc = dyn_graph_apply(g, nupd, flag, u, v, w, ups, false);
+    rc = dyn_graph_apply(g, nupd, flag, u, v, w, ups, false);
     if (rc) return rc;
     const auto t1 = std::chrono::steady_clock::now();
     const int32_t k = (int32_t)ups.size();
@@ -899,7 +1279,9 @@ namespace ddp {
 void dyn_mirror_free(DynMirror *m) { delete m; }
 
 // Compacted CSR of a dynamic graph (live arcs in row order), n+1 offsets.
-int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights) {
+int dyn_read_csr(ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights) {
+    const int rc = dyn_mirror_sync(g);
+    if (rc) return rc;
     const DynMirror *m = g->dyn;
     int64_t k = 0;
     for (int32_t u = 0; u < g->n; u++) {
@@ -916,7 +1298,8 @@ int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *
     return DDP_OK;
 }
 
-int64_t dyn_live_arcs(const ddp_graph *g) {
+int64_t dyn_live_arcs(ddp_graph *g) {
+    if (dyn_mirror_sync(g)) return -1;
     const DynMirror *m = g->dyn;
     int64_t k = 0;
     for (int32_t u = 0; u < g->n; u++)
@@ -967,6 +1350,8 @@ int ddp_kpaths(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, int3
         uint32_t w = 0;
         {
             std::lock_guard<std::mutex> lk(g->mu);
+            rc = dyn_mirror_sync(g);
+            if (rc) break;
             const DynMirror *m = g->dyn;
             for (int32_t j = m->beg[(size_t)u]; j < m->end[(size_t)u]; j++)
                 if ((int32_t)m->arc[(size_t)j].x == v) {

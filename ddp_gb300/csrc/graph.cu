@@ -266,7 +266,10 @@ int ddp_graph_info(const ddp_graph *g, int32_t *n, int64_t *e, uint32_t *wmin, u
     if (!g) return fail(DDP_ERR_INVALID, "null graph");
     std::lock_guard<std::mutex> lk(const_cast<ddp_graph *>(g)->mu);
     if (n) *n = g->n;
-    if (e) *e = g->dyn ? dyn_live_arcs(g) : g->e;
+    if (e) {
+        *e = g->dyn ? dyn_live_arcs(const_cast<ddp_graph *>(g)) : g->e;
+        if (*e < 0) return fail(DDP_ERR_CUDA, "reading the dynamic graph back");
+    }
     if (wmin) *wmin = g->wmin;
     if (wmax) *wmax = g->wmax;
     return DDP_OK;
@@ -275,7 +278,7 @@ int ddp_graph_info(const ddp_graph *g, int32_t *n, int64_t *e, uint32_t *wmin, u
 int ddp_graph_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights) {
     if (!g) return fail(DDP_ERR_INVALID, "null graph");
     std::lock_guard<std::mutex> lk(const_cast<ddp_graph *>(g)->mu);
-    if (g->dyn) return dyn_read_csr(g, offsets, cols, weights);
+    if (g->dyn) return dyn_read_csr(const_cast<ddp_graph *>(g), offsets, cols, weights);
     if (offsets)
         DDP_CUDA(cudaMemcpy(offsets, g->d_off, sizeof(int32_t) * ((size_t)g->n + 1),
                             cudaMemcpyDeviceToHost));

@@ -75,8 +75,9 @@ DevGraph graph_view(const ddp_graph *g);
 int ensure_device();
 void workspace_release(ddp_graph *g);
 void dyn_mirror_free(DynMirror *m);
-int dyn_read_csr(const ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights);
-int64_t dyn_live_arcs(const ddp_graph *g);
+int dyn_read_csr(ddp_graph *g, int32_t *offsets, int32_t *cols, uint32_t *weights);
+int64_t dyn_live_arcs(ddp_graph *g);  // -1 on a CUDA error
+int dyn_mirror_sync(ddp_graph *g);
 int dyn_upload(ddp_graph *g, bool sync = true);
 int dyn_graph_prepare(ddp_graph *g);
 // cudaFree now, or later (graph_flush_frees) while g->defer_free is set
