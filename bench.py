@@ -493,13 +493,17 @@ def bench_dynamic(a, c):
     sample = set(range(0, nb, max(1, nb // 5))) | {nb - 1}
     off, col, ww = g.off[:-1].copy(), g.col.copy(), g.w.copy()
     dyn_t, scratch_t, cpu_t, exact, costs, inval = [], [], [], True, [], []
+    phases, expanded = [], []
     for b in range(nb):
         sl = slice(int(bounds[b]), int(bounds[b + 1]))
         t0 = time.perf_counter()
         cost = dyn.update(fl[sl], u[sl], v[sl], w[sl])
         dyn_t.append(time.perf_counter() - t0)
         costs.append(cost)
-        inval.append(dyn.stats()["invalidated"])
+        stt = dyn.stats()
+        inval.append(stt["invalidated"])
+        phases.append(stt["phases"])
+        expanded.append(stt["expanded"])
         off, col, ww, _ = O.apply_batch(len(off), off, col, ww, fl[sl], u[sl], v[sl], w[sl])
         if b in sample:
             # GPU from-scratch GA* on the updated graph (heuristic + search)
@@ -541,7 +545,9 @@ def bench_dynamic(a, c):
                                              "sample": f"{len(cpu_t)} sampled batches, search loop only"},
            "exact_on_sampled_batches": exact, "sampled_batches": sorted(sample),
            "exact_vs_oracle_all": fx["exact"] if fx else None, "oracle_fixture": fx,
-           "invalidated_nodes_mean": float(np.mean(inval)), "costs_first_last": [costs[0], costs[-1]]}
+           "invalidated_nodes_mean": float(np.mean(inval)),
+           "resumed_search": {"phases_mean": float(np.mean(phases)), "expanded_mean": float(np.mean(expanded))},
+           "costs_first_last": [costs[0], costs[-1]]}
     dyn.close()
     dg.close()
     return out

@@ -68,7 +68,6 @@ struct DynMirror {
     int32_t *d_cap = nullptr, *d_rcap = nullptr;  // row capacities, n each
     long long *d_tails = nullptr;                 // first unused slot: forward, reverse
     int4 *h_ops = nullptr, *d_ops = nullptr;      // one batch {flag, u, v, w}
-    int *d_res = nullptr;                         // k_apply: records written, status
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // DDP_TRACE: around k_apply and k_dyn
     // staging of a batch's scatter lists: pinned host memory (the copy is
     // asynchronous; the buffer is reused once the graph's stream has been
@@ -84,7 +83,6 @@ struct DynMirror {
         cudaFree(d_tails);
         cudaFreeHost(h_ops);
         cudaFree(d_ops);
-        cudaFree(d_res);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -203,6 +201,7 @@ __global__ void k_scatter_all(ScatterAll j) {
 // not, nothing is changed and the status asks for the host path (which lays
 // the arrays out again).
 constexpr int APPLY_MAX = 4096;
+constexpr int DYN_OUT_APPLY = 12;  // words of the dyn output block k_apply writes (of 16)
 constexpr int APPLY_THREADS = 1024;
 enum { APPLY_NO_ROOM = 1 };
 
@@ -216,6 +215,10 @@ struct ApplyArgs {
     long long arc_lim, rarc_lim;  // slots of the laid-out arrays
     int4 *ups;                  // repair records {kind, u, v, w}
     int *res;                   // [0] records written, [1] status
+    // words the repair kernel that follows wants zeroed (its counters,
+    // barrier and status): cleared here instead of by separate memsets
+    uint32_t *zero[3];
+    int zero_n[3];
 };
 
 __device__ __forceinline__ bool apply_valid(const int4 &o, int32_t n) {
@@ -256,6 +259,22 @@ __device__ void apply_sort2(unsigned long long *a, unsigned long long *b, int P)
         }
 }
 
+// First slot in [b, e) whose arc has head x (and weight wt when `weighted`),
+// -1 if none.  Eight loads are in flight per step: the rows are scanned by
+// one thread, and a dependent load per arc would make the scan a chain of
+// memory latencies.
+__device__ __forceinline__ int apply_find(const uint2 *arc, int b, int e, uint32_t x, uint32_t wt, bool weighted) {
+    for (int j0 = b; j0 < e; j0 += 8) {
+        uint2 c[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) c[k] = j0 + k < e ? arc[j0 + k] : make_uint2(0xFFFFFFFFu, 0u);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (c[k].x == x && (!weighted || c[k].y == wt) && j0 + k < e) return j0 + k;
+    }
+    return -1;
+}
+
 // Moves row r (slots [beg, end)) to a fresh region of ncap slots at the
 // array's tail when ncap exceeds its capacity.
 __device__ void apply_grow_row(uint2 *arc, int32_t *beg, int32_t *end, int32_t *cap, long long *tail, int r,
@@ -280,6 +299,8 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(ApplyArgs A) {
     int *hit = reinterpret_cast<int *>(kb + P);  // forward slot op i hit (-1: none)
     uint32_t *w0 = reinterpret_cast<uint32_t *>(hit + P);  // that slot's weight before op i
     const unsigned long long NONE = ~0ull;
+    for (int z = 0; z < 3; z++)
+        for (int i = threadIdx.x; i < A.zero_n[z]; i += blockDim.x) A.zero[z][i] = 0u;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
         ka[i] = kb[i] = NONE;
         if (i < A.nops) {
@@ -335,24 +356,12 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(ApplyArgs A) {
             const int4 o = A.ops[i];
             if (o.x == 1) continue;
             const int b = o.z;
-            int jf = -1;
-            for (int j = A.off[a]; j < A.oend[a]; j++)
-                if ((int)A.arc[j].x == b) {
-                    jf = j;
-                    break;
-                }
+            const int jf = apply_find(A.arc, A.off[a], A.oend[a], (uint32_t)b, 0u, false);
             if (jf < 0) continue;  // no such arc: nothing to do
             const uint32_t wold = A.arc[jf].y;
             hit[i] = jf;
             w0[i] = wold;
-            int jr = -1;
-            for (int j = A.roff[b]; j < A.roend[b]; j++) {
-                const uint2 ra = A.rarc[j];
-                if ((int)ra.x == a && ra.y == wold) {
-                    jr = j;
-                    break;
-                }
-            }
+            const int jr = apply_find(A.rarc, A.roff[b], A.roend[b], (uint32_t)a, wold, true);
             if (o.x == 0) {
                 A.arc[jf].x = 0xFFFFFFFFu;
                 if (jr >= 0) A.rarc[jr].x = 0xFFFFFFFFu;
@@ -660,6 +669,8 @@ struct ddp_dyn {
     DynCtl *d_dc = nullptr;
     int4 *d_upd = nullptr;
     int32_t upd_cap = 0;
+    uint2 *d_cold = nullptr;  // cold tier of the retained far pile
+    int64_t cold_cap = 0;
     int32_t cost = DDP_INF;
     int32_t path_len = 0;
     int64_t stats[10] = {0};
@@ -829,20 +840,22 @@ int dyn_mirror_sync(ddp_graph *g) {
     return DDP_OK;
 }
 
-// Applies a batch on the device (k_apply on the graph's stream, no
-// synchronisation): the repair records go to d_ups and their count to
-// m->d_res[0]; m->d_res[1] != 0 means nothing was applied and the batch
-// must take the host path.  Returns 1 (nothing launched) when the batch is
-// too large for one CTA or a serving kernel owns the graph's updates.
-int dyn_apply_device(ddp_graph *g, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
-                     const uint32_t *w, int4 *d_ups) {
+// Applies a batch of d's graph on the device (k_apply on the graph's
+// stream, no synchronisation): the repair records go to d->d_upd, their
+// count to d->d_out[DYN_OUT_APPLY] and k_apply's status to the next word
+// (non-zero: nothing was applied, the batch must take the host path).
+// k_apply also clears the counters, barrier and status of the k_dyn launch
+// that follows.  Returns 1 (nothing launched) when the batch is too large
+// for one CTA or a serving kernel owns the graph's updates.
+int dyn_apply_device(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t *u, const int32_t *v,
+                     const uint32_t *w) {
+    ddp_graph *g = d->g;
     DynMirror *m = g->dyn;
     if (nupd > APPLY_MAX || g->hook.fn) return 1;
     const int32_t n = g->n;
     if (!m->h_ops) {
         DDP_CUDA(cudaHostAlloc(&m->h_ops, sizeof(int4) * APPLY_MAX, cudaHostAllocDefault));
         DDP_CUDA(cudaMalloc(&m->d_ops, sizeof(int4) * APPLY_MAX));
-        DDP_CUDA(cudaMalloc(&m->d_res, sizeof(int) * 2));
         DDP_CUDA(cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       24 * APPLY_MAX));
     }
@@ -883,8 +896,14 @@ int dyn_apply_device(ddp_graph *g, int32_t nupd, const int32_t *flag, const int3
     A.tails = m->d_tails;
     A.arc_lim = (long long)m->arc.size();
     A.rarc_lim = (long long)m->rarc.size();
-    A.ups = d_ups;
-    A.res = m->d_res;
+    A.ups = d->d_upd;
+    A.res = d->d_out + DYN_OUT_APPLY;
+    A.zero[0] = reinterpret_cast<uint32_t *>(d->d_dc);
+    A.zero_n[0] = (int)(sizeof(DynCtl) / sizeof(uint32_t));
+    A.zero[1] = &d->sa.ctl->bar_count;  // bar_count, bar_gen
+    A.zero_n[1] = 2;
+    A.zero[2] = reinterpret_cast<uint32_t *>(&d->sa.ctl->status);
+    A.zero_n[2] = 1;
     int P = 32;
     while (P < nupd) P <<= 1;
     const bool timed = trace_on();
@@ -899,15 +918,22 @@ int dyn_apply_device(ddp_graph *g, int32_t nupd, const int32_t *flag, const int3
     return DDP_OK;
 }
 
-// dres: k_apply's result when the batch was applied on the device (the
-// record count is read there, and *apply_status receives its status; a
-// failed apply leaves the search untouched), else null.
+// dres: k_apply's result (d_out + DYN_OUT_APPLY) when the batch was applied
+// on the device (the record count is read there, and *apply_status receives
+// its status; a failed apply leaves the search untouched), else null.
 static int dyn_launch(ddp_dyn *d, int initial, int nupd, const int *dres = nullptr, int *apply_status = nullptr) {
     const bool one_cta = !initial && d->upd_grid == 1;
     ddp_graph *g = d->g;
     DevGraph G = graph_view(g);
     SearchParams P{d->s, d->t, d->o.delta > 0 ? (uint32_t)d->o.delta : std::max(1u, (g->wmin + g->wmax) / 4),
                    d->o.K, 1, initial ? 0 : 1, 1};
+    // a resumed search leaves entries with g >= the last cost (f >= g)
+    // unexamined until it needs them
+    if (!initial && d->cost >= 0 && d->cost != DDP_INF) {
+        P.cold = d->d_cold;
+        P.cold_cap = d->cold_cap;
+        P.cold_x = (uint32_t)d->cost;
+    }
     DynArgs A;
     A.upd = d->d_upd;
     A.nupd = nupd;
@@ -919,10 +945,13 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd, const int *dres = nullp
     A.path_cap = g->n;
     A.heur = d->hkind == DDP_H_BFS_HOPS ? 1 : 0;
     A.initial = initial;
-    // fresh barrier / counters; the far pile position survives in ctl
-    DDP_CUDA(cudaMemsetAsync(d->d_dc, 0, sizeof(DynCtl), g->stream));
-    DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->bar_count, 0, 2 * sizeof(unsigned int), g->stream));
-    DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->status, 0, sizeof(int), g->stream));
+    // fresh barrier / counters (k_apply cleared them on the device path);
+    // the far pile position survives in ctl
+    if (!dres) {
+        DDP_CUDA(cudaMemsetAsync(d->d_dc, 0, sizeof(DynCtl), g->stream));
+        DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->bar_count, 0, 2 * sizeof(unsigned int), g->stream));
+        DDP_CUDA(cudaMemsetAsync(&d->sa.ctl->status, 0, sizeof(int), g->stream));
+    }
     void *args[] = {&G, &d->sa, &d->d_hops, &P, &A, &d->d_dc};
     if (one_cta)
         DDP_CUDA(cudaLaunchKernel((const void *)k_dyn<CtaGroup>, dim3(1), dim3(512), args, 0, g->stream));
@@ -930,13 +959,13 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd, const int *dres = nullp
         DDP_CUDA(cudaLaunchCooperativeKernel((const void *)k_dyn<GridGroup>, dim3(initial ? d->grid : d->upd_grid),
                                              dim3(512), args, 0, g->stream));
     if (dres && trace_on() && g->dyn->ev[2]) DDP_CUDA(cudaEventRecord(g->dyn->ev[2], g->stream));
-    int32_t out[10];
-    int res[2] = {0, 0};
-    DDP_CUDA(cudaMemcpyAsync(out, d->d_out, sizeof(out), cudaMemcpyDeviceToHost, g->stream));
-    if (dres) DDP_CUDA(cudaMemcpyAsync(res, dres, sizeof(res), cudaMemcpyDeviceToHost, g->stream));
+    // out[0..9] from k_dyn; out[DYN_OUT_APPLY..+1] from k_apply (device path)
+    int32_t out[DYN_OUT_APPLY + 2] = {0};
+    DDP_CUDA(cudaMemcpyAsync(out, d->d_out, sizeof(int32_t) * (dres ? DYN_OUT_APPLY + 2 : 10),
+                             cudaMemcpyDeviceToHost, g->stream));
     DDP_CUDA(cudaStreamSynchronize(g->stream));
-    if (apply_status) *apply_status = res[1];
-    if (res[1]) return DDP_OK;  // nothing ran: the caller applies the batch on the host
+    if (apply_status) *apply_status = out[DYN_OUT_APPLY + 1];
+    if (dres && out[DYN_OUT_APPLY + 1]) return DDP_OK;  // nothing ran: the caller applies the batch on the host
     if (out[2] & ST_TIMEOUT) return fail(DDP_ERR_TIMEOUT, "dynamic search: barrier wait timed out");
     if (out[2] & ST_OVERFLOW) return fail(DDP_ERR_QUEUE_OVERFLOW, "dynamic search: queue overflow");
     d->cost = out[0];
@@ -1128,6 +1157,8 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_path, sizeof(int32_t) * n);
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_dc, sizeof(DynCtl));
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_hops, sizeof(uint32_t) * n);
+    d->cold_cap = capf;
+    if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_cold, sizeof(uint2) * (size_t)capf);
     if (e1 != cudaSuccess) return bail(cuda_fail(e1, "cudaMalloc(dynamic state)"));
     DDP_CUDA(cudaMemsetAsync(d->sa.ctl, 0, sizeof(SearchCtl), g->stream));
     int per_sm = 0, sms = 0, dev = 0;
@@ -1179,10 +1210,10 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
     }
     // on the device when the batch fits one CTA: k_apply, then k_dyn on the
     // same stream (one upload, one synchronisation)
-    int rc = dyn_apply_device(g, nupd, flag, u, v, w, d->d_upd);
+    int rc = dyn_apply_device(d, nupd, flag, u, v, w);
     if (rc == DDP_OK) {
         int st = 0;
-        rc = dyn_launch(d, 0, 0, g->dyn->d_res, &st);
+        rc = dyn_launch(d, 0, 0, d->d_out + DYN_OUT_APPLY, &st);
         if (rc) return rc;
         if (!st) {
             if (trace_on()) {
@@ -1258,6 +1289,7 @@ int ddp_dyn_free(ddp_dyn *d) {
     if (!d) return DDP_OK;
     slots_free(d->sa);
     cudaFree(d->d_hops);
+    cudaFree(d->d_cold);
     cudaFree(d->d_inv);
     cudaFree(d->d_out);
     cudaFree(d->d_path);

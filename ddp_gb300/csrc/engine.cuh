@@ -60,6 +60,7 @@ struct SearchCtl {
     int far_n, far_sel;   // far pile left by the last run (dynamic resume)
     int cur_ver;          // graph version of the current search (serving)
     unsigned int bar_count, bar_gen;  // grid barrier (single-query form)
+    int cold_n;           // entries in the far pile's cold tier (keep mode)
 };
 
 // Buffers of one slot.
@@ -394,6 +395,15 @@ struct SearchParams {
     int resume;    // continue from the slot's far pile instead of starting at s
     int no_touch_log;  // do not log first touches (slots that are never reset)
     // t < 0: no target, the search settles everything reachable from s
+    // Keep mode, resumed searches: cold tier of the far pile.  The first
+    // split moves live entries with g >= cold_x (their f is at least g) to
+    // `cold` unexamined; later splits scan the rest until min(f(t),
+    // threshold) passes cold_x, when one split takes the cold entries back.
+    // They rejoin the far pile when the search ends.  cold_x = 0xFFFFFFFF:
+    // no cold tier.
+    uint2 *cold = nullptr;
+    int64_t cold_cap = 0;
+    uint32_t cold_x = 0xFFFFFFFFu;
 };
 
 struct SearchResult {
@@ -422,6 +432,7 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
         ctl->iters = 0;
         ctl->expanded = ctl->scanned = ctl->relaxed = 0;
         ctl->far_scanned = 0;
+        ctl->cold_n = 0;
         if (!P.resume) {
             ctl->touched = 1;
             B.state[P.s] = st_make(0, -1);
@@ -452,6 +463,11 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     int it = 0;
     int status = 0;
     const int64_t max_phases = 4 * (int64_t)G.n + (1 << 22);
+    // cold tier (keep mode, resumed): made by the first split
+    uint32_t cold_x = (P.keep && P.resume && P.cold) ? P.cold_x : 0xFFFFFFFFu;
+    bool cold_pass = cold_x != 0xFFFFFFFFu;
+    int64_t ncold = 0;
+    uint2 *cold_stage = reinterpret_cast<uint2 *>(wr.snr);
 
     for (;;) {
         const int PH = (it + 1) & 3, RS = (it + 3) & 3;
@@ -594,24 +610,39 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             // stale entries) re-check the state and h.
             const uint32_t thr = compacting ? T : Tsplit;
             const bool recheck = P.keep || compacting;
-            if (grp.rank() == 0) ctl->far_scanned += (unsigned long long)nfar;
+            // cold tier: made here (first split of a resumed search), or
+            // scanned with the pile once min(f(t), threshold) passes cold_x
+            const bool to_cold = cold_pass && !compacting;
+            const bool merge_cold = !compacting && ncold > 0 && min(ft, thr) > cold_x;
+            const int64_t nscan = nfar + (merge_cold ? ncold : 0);
+            if (grp.rank() == 0) ctl->far_scanned += (unsigned long long)nscan;
             uint2 *dst = compacting ? qnxt : qcur;
             const int64_t dbase = compacting ? nnext : 0;
             unsigned int local_min = 0xFFFFFFFFu;
-            int c_n = 0, c_f = 0;
-            for (int64_t base = 32 * claim_chunk(&ctl->ck[PH]); base < nfar;
+            int c_n = 0, c_f = 0, c_c = 0;
+            for (int64_t base = 32 * claim_chunk(&ctl->ck[PH]); base < nscan;
                  base = 32 * claim_chunk(&ctl->ck[PH])) {
                 const int64_t idx = base + lane;
-                bool to_near = false, keep = false;
+                bool to_near = false, keep = false, cold = false;
                 uint4 en = make_uint4(0u, 0u, 0u, 0u);
-                if (idx < nfar) {
-                    en = __ldcg(fcur + idx);
+                if (idx < nscan) {
+                    if (idx < nfar) {
+                        en = __ldcg(fcur + idx);
+                    } else {
+                        const uint2 c = __ldcg(P.cold + (idx - nfar));
+                        en = make_uint4(c.x, c.y, 0u, 0u);  // f re-derived below (keep mode)
+                    }
                     bool live = true;
                     uint64_t f = en.z;
                     if (recheck) {
                         live = st_g(__ldcg(B.state + en.x)) == en.y;
-                        f = (uint64_t)en.y + H((int)en.x);
-                        en.z = f >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)f;
+                        if (live && to_cold && en.y >= cold_x) {
+                            cold = true;  // f >= g >= cold_x: h is not read
+                            live = false;
+                        } else {
+                            f = (uint64_t)en.y + H((int)en.x);
+                            en.z = f >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)f;
+                        }
                     }
                     if (live) {
                         if (f < ft && f < thr) {
@@ -625,9 +656,17 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
                 stage_push(to_near, make_uint2(en.x, en.y), wr.sn, c_n, &ctl->nq[PH], dst, dbase, B.cap_q, ctl, PH);
                 // compaction never grows the pile
                 stage_push(keep, en, wr.sf, c_f, &ctl->fq[PH], falt, 0, B.cap_f, ctl, PH);
+                if (to_cold)
+                    stage_push(cold, make_uint2(en.x, en.y), cold_stage, c_c, &ctl->cold_n, P.cold, 0, P.cold_cap,
+                               ctl, PH);
             }
             stage_flush(wr.sn, c_n, &ctl->nq[PH], dst, dbase, B.cap_q, ctl, PH);
             stage_flush(wr.sf, c_f, &ctl->fq[PH], falt, 0, B.cap_f, ctl, PH);
+            if (to_cold) stage_flush(cold_stage, c_c, &ctl->cold_n, P.cold, 0, P.cold_cap, ctl, PH);
+            if (merge_cold) {
+                ncold = 0;  // every cold entry was examined: none is left
+                cold_x = 0xFFFFFFFFu;
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) local_min = min(local_min, __shfl_xor_sync(FULL, local_min, o));
             if (lane == 0 && local_min != 0xFFFFFFFFu) atomicMin(&ctl->mf[PH], local_min);
@@ -690,13 +729,20 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
             nnear = a;
             head = 0;
             nnext = 0;
+            if (cold_pass) {
+                // pushes past the buffer raised an overflow (the loop ends below)
+                ncold = min((int64_t)*(volatile int *)&ctl->cold_n, P.cold_cap);
+                cold_pass = false;
+            }
+            // cold entries have f >= cold_x
+            const uint32_t mall = ncold > 0 ? min(m, cold_x) : m;
             if (nnear > 0) {
                 T = Tsplit;
                 splitting = false;
-            } else if (nfar == 0 || m >= ft) {
+            } else if ((nfar == 0 && ncold == 0) || mall >= ft) {
                 break;  // no open node with f < f(t): done
             } else {
-                Tsplit = sat_add(m, P.delta);
+                Tsplit = sat_add(mall, P.delta);
             }
         }
         if (nnear > B.cap_q || nfar > B.cap_f) {
@@ -715,6 +761,15 @@ __device__ SearchResult run_search(const Grp &grp, const DevGraph &G, const Slot
     if (lane == 0) {
         if (n_exp) atomicAdd(&ctl->expanded, n_exp);
         if (n_rel) atomicAdd(&ctl->relaxed, n_rel);
+    }
+    if (ncold > 0) {
+        // the cold tier rejoins the far pile (f re-derived by the next split)
+        for (int64_t i = grp.rank(); i < ncold; i += grp.size()) {
+            const uint2 c = __ldcg(P.cold + i);
+            if (nfar + i < B.cap_f) fcur[nfar + i] = make_uint4(c.x, c.y, 0u, 0u);
+            else atomicOr(&ctl->status, ST_OVERFLOW);
+        }
+        nfar = min(nfar + ncold, B.cap_f);
     }
     if (grp.rank() == 0) {
         ctl->far_n = (int)nfar;

@@ -77,6 +77,11 @@ namespace ddp {
 #define DDP_BIDIR_CLAIM_MIN 4
 #endif
 
+// Far entries a lane loads at once when a split scans the far pile.
+#ifndef DDP_BIDIR_SPLIT_UNROLL
+#define DDP_BIDIR_SPLIT_UNROLL 4
+#endif
+
 constexpr uint32_t DIR_BIT = 0x80000000u;
 constexpr uint32_t NODE_MASK = 0x7FFFFFFFu;
 
@@ -539,6 +544,10 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                     gu = en.y;  // the entry's key
                     const int u = (int)(ud & NODE_MASK);
                     const uint32_t dir = ud >> 31;
+                    // the row bounds load beside the record (used only when
+                    // the entry turns out current): one round trip less
+                    const int r0 = dir ? row_begin(G.roff, G.roend, u) : row_begin(G.off, G.oend, u);
+                    const int r1 = dir ? row_end(G.roff, G.roend, u) : row_end(G.off, G.oend, u);
                     const typename Rec::U *ru = R.find(u, ep);
                     const uint32_t gl = ru ? Rec::g(Rec::ld(ru + dir), ep) : INF_G;
                     bool cur = false;
@@ -551,8 +560,6 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         cur = gl == gu && gu < mu;
                     }
                     if (cur) {
-                        const int r0 = dir ? row_begin(G.roff, G.roend, u) : row_begin(G.off, G.oend, u);
-                        const int r1 = dir ? row_end(G.roff, G.roend, u) : row_end(G.off, G.oend, u);
                         rb = r0;
                         deg = r1 - r0;
                         n_exp++;
@@ -739,34 +746,46 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
             int kp0 = 0, kp1 = 0, mv0 = 0, mv1 = 0;  // kept / moved per direction (this lane)
             int c_n = 0, c_f = 0;
             if (threadIdx.x == 0) ctl->far_scanned += (unsigned long long)nfar;
-            for (int64_t base = (int64_t)warp * 32; base < nfar; base += (int64_t)(blockDim.x >> 5) * 32) {
-                const int64_t idx = base + lane;
-                bool to_near = false, keep = false;
-                uint2 en = make_uint2(0u, 0u);
-                if (idx < nfar) {
-                    en = __ldcg(fcur + idx);
-                    if ((uint64_t)en.y < kb) {
-                        const bool rev = (en.x >> 31) != 0;
-                        if (en.y < (rev ? Ts1 : Ts0)) to_near = true;
-                        else keep = true;
-                        if (rev) {
-                            kmin1 = min(kmin1, en.y);
-                            if (to_near) mv1++;
-                            else kp1++;
-                        } else {
-                            kmin0 = min(kmin0, en.y);
-                            if (to_near) mv0++;
-                            else kp0++;
+            // DDP_BIDIR_SPLIT_UNROLL entries per lane per step: their loads
+            // are issued together, then consumed one by one
+            constexpr int SU = DDP_BIDIR_SPLIT_UNROLL;
+            for (int64_t base0 = (int64_t)warp * 32 * SU; base0 < nfar; base0 += (int64_t)nw * 32 * SU) {
+                uint2 ens[SU];
+#pragma unroll
+                for (int k = 0; k < SU; k++) {
+                    const int64_t idx = base0 + 32 * k + lane;
+                    ens[k] = idx < nfar ? __ldcg(fcur + idx) : make_uint2(0u, 0u);
+                }
+#pragma unroll
+                for (int k = 0; k < SU; k++) {
+                    const int64_t idx = base0 + 32 * k + lane;
+                    bool to_near = false, keep = false;
+                    uint2 en = make_uint2(0u, 0u);
+                    if (idx < nfar) {
+                        en = ens[k];
+                        if ((uint64_t)en.y < kb) {
+                            const bool rev = (en.x >> 31) != 0;
+                            if (en.y < (rev ? Ts1 : Ts0)) to_near = true;
+                            else keep = true;
+                            if (rev) {
+                                kmin1 = min(kmin1, en.y);
+                                if (to_near) mv1++;
+                                else kp1++;
+                            } else {
+                                kmin0 = min(kmin0, en.y);
+                                if (to_near) mv0++;
+                                else kp0++;
+                            }
                         }
                     }
+                    {
+                        const unsigned m = __ballot_sync(FULL, to_near);
+                        if (to_near) wr.sn[c_n + __popc(m & ((1u << lane) - 1u))] = en;
+                        c_n += __popc(m);
+                        if (c_n >= 32) flush_ring_or_far(wr.sn, c_n, sq, ring, cap, falt, B.cap_f, ctl);
+                    }
+                    stage_push(keep, en, sf2, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
                 }
-                {
-                    const unsigned m = __ballot_sync(FULL, to_near);
-                    if (to_near) wr.sn[c_n + __popc(m & ((1u << lane) - 1u))] = en;
-                    c_n += __popc(m);
-                    if (c_n >= 32) flush_ring_or_far(wr.sn, c_n, sq, ring, cap, falt, B.cap_f, ctl);
-                }
-                stage_push(keep, en, sf2, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
             }
             flush_ring_or_far(wr.sn, c_n, sq, ring, cap, falt, B.cap_f, ctl);
             stage_flush(sf2, c_f, &sq->alt_cnt, falt, 0, B.cap_f, ctl, 0);
