@@ -45,6 +45,13 @@
 
 enum { UPD_INS = 1, UPD_TREE = 2, UPD_LIGHTER = 3 };
 
+// Arcs a repair thread loads at once when it walks a row: the loads of a
+// chunk (and then of its heads' words) are in flight together instead of
+// one dependent pair per arc.
+#ifndef DYN_ROW_UNROLL
+#define DYN_ROW_UNROLL 8
+#endif
+
 // Host mirror of a dynamic graph: rows with explicit [beg, end) and a
 // capacity, forward and reverse.
 struct DynMirror {
@@ -516,14 +523,20 @@ __global__ void __launch_bounds__(512, 2)
                     const int u = __ldcg(fa + i);
                     const uint32_t hu = __ldcg(hops + u);
                     const int b = row_begin(G.roff, G.roend, u), e = row_end(G.roff, G.roend, u);
-                    for (int j = b; j < e; j++) {
-                        const int p = (int)__ldcg(G.rarc + j).x;
-                        if (p < 0) continue;
-                        if (hu + 1 < __ldcg(hops + p)) {
-                            const uint32_t old = atomicMin(hops + p, hu + 1);
+                    for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
+                        int p[DYN_ROW_UNROLL];
+                        uint32_t hp[DYN_ROW_UNROLL];
+#pragma unroll
+                        for (int k = 0; k < DYN_ROW_UNROLL; k++) p[k] = j0 + k < e ? (int)__ldcg(G.rarc + j0 + k).x : -1;
+#pragma unroll
+                        for (int k = 0; k < DYN_ROW_UNROLL; k++) hp[k] = p[k] >= 0 ? __ldcg(hops + p[k]) : 0u;
+#pragma unroll
+                        for (int k = 0; k < DYN_ROW_UNROLL; k++) {
+                            if (p[k] < 0 || hu + 1 >= hp[k]) continue;
+                            const uint32_t old = atomicMin(hops + p[k], hu + 1);
                             if (hu + 1 < old) {
                                 const int s = atomicAdd(&dc->cnt[PH], 1);
-                                if (s < 2 * B.cap_q) fb[s] = p;
+                                if (s < 2 * B.cap_q) fb[s] = p[k];
                                 else atomicOr(&B.ctl->status, ST_OVERFLOW);
                                 atomicAdd(&dc->hops_lowered, 1);
                             }
@@ -558,13 +571,21 @@ __global__ void __launch_bounds__(512, 2)
                 for (int i = rank; i < nf; i += size) {
                     const int x = __ldcg(fa + i);
                     const int b = row_begin(G.off, G.oend, x), e = row_end(G.off, G.oend, x);
-                    for (int j = b; j < e; j++) {
-                        const int y = (int)__ldcg(G.arc + j).x;
-                        if (y < 0) continue;
-                        const uint64_t sy = __ldcg(B.state + y);
-                        if (st_g(sy) < INF_G && st_parent(sy) == x && atomicCAS(B.state + y, sy, ~0ull) == sy) {
-                            fb[atomicAdd(&dc->cnt[PH2], 1)] = y;  // each node invalidated once
-                            A.inv[atomicAdd(&dc->inv_n, 1)] = y;
+                    for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
+                        int y[DYN_ROW_UNROLL];
+                        uint64_t sy[DYN_ROW_UNROLL];
+#pragma unroll
+                        for (int k = 0; k < DYN_ROW_UNROLL; k++) y[k] = j0 + k < e ? (int)__ldcg(G.arc + j0 + k).x : -1;
+#pragma unroll
+                        for (int k = 0; k < DYN_ROW_UNROLL; k++) sy[k] = y[k] >= 0 ? __ldcg(B.state + y[k]) : ~0ull;
+#pragma unroll
+                        for (int k = 0; k < DYN_ROW_UNROLL; k++) {
+                            // a parallel arc's second CAS fails: each node is invalidated once
+                            if (y[k] >= 0 && st_g(sy[k]) < INF_G && st_parent(sy[k]) == x &&
+                                atomicCAS(B.state + y[k], sy[k], ~0ull) == sy[k]) {
+                                fb[atomicAdd(&dc->cnt[PH2], 1)] = y[k];
+                                A.inv[atomicAdd(&dc->inv_n, 1)] = y[k];
+                            }
                         }
                     }
                 }
@@ -580,16 +601,23 @@ __global__ void __launch_bounds__(512, 2)
             uint32_t bg = INF_G;
             int bp = -1;
             const int b = row_begin(G.roff, G.roend, x), e = row_end(G.roff, G.roend, x);
-            for (int j = b; j < e; j++) {
-                const uint2 a = __ldcg(G.rarc + j);
-                const int p = (int)a.x;
-                if (p < 0) continue;
-                const uint32_t gp = st_g(__ldcg(B.state + p));
-                if (gp >= INF_G) continue;
-                const uint64_t c = (uint64_t)gp + a.y;
-                if (c < bg) {
-                    bg = (uint32_t)c;
-                    bp = p;
+            for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
+                uint2 a[DYN_ROW_UNROLL];
+                uint32_t gp[DYN_ROW_UNROLL];
+#pragma unroll
+                for (int k = 0; k < DYN_ROW_UNROLL; k++)
+                    a[k] = j0 + k < e ? __ldcg(G.rarc + j0 + k) : make_uint2(0xFFFFFFFFu, 0u);
+#pragma unroll
+                for (int k = 0; k < DYN_ROW_UNROLL; k++)
+                    gp[k] = (int)a[k].x >= 0 ? st_g(__ldcg(B.state + (int)a[k].x)) : INF_G;
+#pragma unroll
+                for (int k = 0; k < DYN_ROW_UNROLL; k++) {
+                    if (gp[k] >= INF_G) continue;
+                    const uint64_t c = (uint64_t)gp[k] + a[k].y;
+                    if (c < bg) {
+                        bg = (uint32_t)c;
+                        bp = (int)a[k].x;
+                    }
                 }
             }
             best[i] = make_uint2(bg, (uint32_t)bp);
@@ -671,6 +699,8 @@ struct ddp_dyn {
     int32_t upd_cap = 0;
     uint2 *d_cold = nullptr;  // cold tier of the retained far pile
     int64_t cold_cap = 0;
+    int32_t *h_out = nullptr;  // pinned copy of d_out (16 words)
+    double t_wait_us = 0;      // DDP_TRACE: host wait of the last launch
     int32_t cost = DDP_INF;
     int32_t path_len = 0;
     int64_t stats[10] = {0};
@@ -960,10 +990,12 @@ static int dyn_launch(ddp_dyn *d, int initial, int nupd, const int *dres = nullp
                                              dim3(512), args, 0, g->stream));
     if (dres && trace_on() && g->dyn->ev[2]) DDP_CUDA(cudaEventRecord(g->dyn->ev[2], g->stream));
     // out[0..9] from k_dyn; out[DYN_OUT_APPLY..+1] from k_apply (device path)
-    int32_t out[DYN_OUT_APPLY + 2] = {0};
+    int32_t *out = d->h_out;
     DDP_CUDA(cudaMemcpyAsync(out, d->d_out, sizeof(int32_t) * (dres ? DYN_OUT_APPLY + 2 : 10),
                              cudaMemcpyDeviceToHost, g->stream));
+    const auto tw = std::chrono::steady_clock::now();
     DDP_CUDA(cudaStreamSynchronize(g->stream));
+    d->t_wait_us = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - tw).count();
     if (apply_status) *apply_status = out[DYN_OUT_APPLY + 1];
     if (dres && out[DYN_OUT_APPLY + 1]) return DDP_OK;  // nothing ran: the caller applies the batch on the host
     if (out[2] & ST_TIMEOUT) return fail(DDP_ERR_TIMEOUT, "dynamic search: barrier wait timed out");
@@ -1154,6 +1186,7 @@ int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind, 
     if (rc) return bail(rc);
     e1 = cudaMalloc(&d->d_inv, sizeof(int32_t) * n);
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_out, sizeof(int32_t) * 16);
+    if (e1 == cudaSuccess) e1 = cudaHostAlloc(&d->h_out, sizeof(int32_t) * 16, cudaHostAllocDefault);
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_path, sizeof(int32_t) * n);
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_dc, sizeof(DynCtl));
     if (e1 == cudaSuccess) e1 = cudaMalloc(&d->d_hops, sizeof(uint32_t) * n);
@@ -1222,9 +1255,9 @@ int ddp_dyn_update(ddp_dyn *d, int32_t nupd, const int32_t *flag, const int32_t 
                 cudaEventElapsedTime(&ka, g->dyn->ev[0], g->dyn->ev[1]);
                 cudaEventElapsedTime(&kd, g->dyn->ev[1], g->dyn->ev[2]);
                 trace("dyn_update: %d updates applied on the device, %.1f us in the call (k_apply %.1f us, "
-                      "k_dyn repair + search %.1f us)",
+                      "k_dyn repair + search %.1f us; host waited %.1f us)",
                       nupd, std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count(),
-                      1000.0 * ka, 1000.0 * kd);
+                      1000.0 * ka, 1000.0 * kd, d->t_wait_us);
             }
             if (out_cost) *out_cost = d->cost;
             return DDP_OK;
@@ -1290,6 +1323,7 @@ int ddp_dyn_free(ddp_dyn *d) {
     slots_free(d->sa);
     cudaFree(d->d_hops);
     cudaFree(d->d_cold);
+    cudaFreeHost(d->h_out);
     cudaFree(d->d_inv);
     cudaFree(d->d_out);
     cudaFree(d->d_path);
