@@ -186,10 +186,12 @@ def peak_hbm():
 # same launch), keyed by (workload family, method).  The capture runs a
 # smaller case of the same kernel (the 400k-node graph of the family, 1,024
 # pairs, one slot per SM), whose state still exceeds L2; a full launch's
-# traffic is this ratio times its own algorithmic bytes.  The summary and
-# the command are in profiles/k_batch5_c4_bidir.md.
+# traffic is this ratio times its own algorithmic bytes.  Capture:
+#   ncu --set full --clock-control none -k regex:k_batch -s 2 -c 1 -o prof \
+#       python bench.py --config c4-small --slots 152 --no-tune --delta 8 \
+#       --steps 1 --warmup 1 --plain-sample 0 --serve-rates= --no-cpu-baseline --other-configs=
 TRAFFIC_PER_ALG_BYTE = {
-    ("c4", "bidir"): (1.604023e9 + 0.638226e9) / 372947624,
+    ("c4", "bidir"): (1.607848e9 + 0.625154e9) / 372759272,
 }
 
 
