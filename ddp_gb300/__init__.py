@@ -664,6 +664,20 @@ class Server:
         flag, u, v, w = _i32(flag), _i32(u), _i32(v), _u32(w)
         check(lib().ddp_serve_update(self.handle, len(flag), ptr(flag), ptr(u), ptr(v), ptr(w, C.c_uint32)))
 
+    def record_paths(self, path_cap: int) -> None:
+        """Keep each request's path (at most path_cap nodes); before the first submit."""
+        check(lib().ddp_serve_record_paths(self.handle, int(path_cap)))
+
+    def path(self, request_id: int) -> np.ndarray:
+        """s..t path of a polled request over the graph version it ran on
+        (empty when t is unreachable)."""
+        ln = C.c_int32()
+        check(lib().ddp_serve_path(self.handle, int(request_id), None, 0, C.byref(ln)))
+        p = np.empty(ln.value, np.int32)
+        if ln.value:
+            check(lib().ddp_serve_path(self.handle, int(request_id), ptr(p), ln.value, C.byref(ln)))
+        return p
+
     def stats(self) -> dict:
         st = np.empty(6, np.int64)
         check(lib().ddp_serve_stats(self.handle, st.ctypes.data_as(C.POINTER(C.c_int64))))

@@ -67,6 +67,8 @@ SIGNATURES = {
     "ddp_serve_poll": (C.c_int, [vp, C.c_int32, i64p, i32p, i64p, i32p, i32p]),
     "ddp_serve_update": (C.c_int, [vp, C.c_int32, i32p, i32p, i32p, u32p]),
     "ddp_serve_stats": (C.c_int, [vp, i64p]),
+    "ddp_serve_record_paths": (C.c_int, [vp, C.c_int32]),
+    "ddp_serve_path": (C.c_int, [vp, C.c_int64, i32p, C.c_int32, i32p]),
     "ddp_serve_free": (C.c_int, [vp]),
     "ddp_bfs_hops_noalloc": (C.c_int, [C.c_int32, vp, vp, C.c_int32, vp, vp]),
     "ddp_io_read_graph_text": (C.c_int, [C.c_char_p, i32p, i64p, C.POINTER(i32p), C.POINTER(i32p), C.POINTER(u32p)]),

@@ -42,6 +42,7 @@
 #include <deque>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "engine.cuh"
@@ -93,7 +94,14 @@ struct ddp_server {
     int32_t *d_S = nullptr, *d_T = nullptr, *d_cost = nullptr, *d_ver = nullptr;
     int *d_done = nullptr, *d_ctl = nullptr;
     int *d_work = nullptr;  // claim counter (device)
-    int32_t *d_plen = nullptr, *d_paths = nullptr;
+    int32_t *d_plen = nullptr;
+    // paths (ddp_serve_record_paths): path_cap node ids per request in mapped
+    // host memory, written by the slot before the request's done flag;
+    // requests re-run on the host keep theirs in host_paths
+    int32_t path_cap = 0;
+    int32_t *h_paths = nullptr, *d_paths = nullptr;
+    int32_t *h_plen = nullptr;  // with paths: d_plen is the device view of this
+    std::unordered_map<int64_t, std::vector<int32_t>> host_paths;
     int64_t submitted = 0, scan_lo = 0, completed = 0;
     std::vector<int64_t> t_sub;
     std::vector<char> reported;
@@ -403,8 +411,8 @@ int launch(ddp_server *s) {
     A.nq = INT32_MAX;  // slots stop by pause / idle, not by count
     A.cost = s->d_cost;
     A.plen = s->d_plen;
-    A.paths = nullptr;
-    A.path_cap = 0;
+    A.paths = s->d_paths;  // null unless paths are recorded
+    A.path_cap = s->path_cap;
     A.work = s->d_work;
     A.status = s->d_work + 1;
     A.delta = s->o.delta > 0                ? (uint32_t)s->o.delta
@@ -619,6 +627,17 @@ int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int
             ddp_heuristic_free(h);
             if (rc) return rc;
             ddp_query_cost(q, &c);
+            if (s->path_cap > 0) {
+                int32_t l = 0;
+                rc = ddp_path_read(q, nullptr, 0, &l);
+                std::vector<int32_t> p((size_t)std::max(l, 0));
+                if (!rc && l > 0) rc = ddp_path_read(q, p.data(), l, &l);
+                if (rc) {
+                    ddp_query_free(q);
+                    return rc;
+                }
+                s->host_paths[i] = std::move(p);
+            }
             ddp_query_free(q);
             s->fallbacks++;
             ver = s->version;
@@ -659,6 +678,50 @@ int ddp_serve_stats(const ddp_server *s, int64_t *stats6) {
     return DDP_OK;
 }
 
+int ddp_serve_record_paths(ddp_server *s, int32_t path_cap) {
+    if (!s || path_cap <= 0) return fail(DDP_ERR_INVALID, "bad path capacity");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->submitted > 0 || s->h_paths) return fail(DDP_ERR_INVALID, "paths must be set up before the first request");
+    // no slot kernel runs before the first request: the lengths move to
+    // mapped host memory too, so reading them never waits for that kernel
+    const size_t bytes = sizeof(int32_t) * (size_t)s->cap * (size_t)path_cap;
+    int32_t *dl = nullptr;
+    cudaError_t e = cudaHostAlloc(&s->h_paths, bytes, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->d_paths, s->h_paths, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&s->h_plen, sizeof(int32_t) * (size_t)s->cap, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&dl, s->h_plen, 0);
+    if (e != cudaSuccess) {
+        cudaFreeHost(s->h_paths);
+        cudaFreeHost(s->h_plen);
+        s->h_paths = s->d_paths = s->h_plen = nullptr;
+        return cuda_fail(e, "cudaHostAlloc(paths)");
+    }
+    cudaFree(s->d_plen);
+    s->d_plen = dl;
+    s->path_cap = path_cap;
+    return DDP_OK;
+}
+
+int ddp_serve_path(ddp_server *s, int64_t id, int32_t *buf, int32_t cap, int32_t *len) {
+    if (!s || !len || cap < 0 || (cap > 0 && !buf)) return fail(DDP_ERR_INVALID, "bad path arguments");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->h_paths) return fail(DDP_ERR_INVALID, "paths are not recorded (ddp_serve_record_paths)");
+    if (id < 0 || id >= s->submitted || !s->reported[(size_t)id])
+        return fail(DDP_ERR_INVALID, "request not completed (poll it first)");
+    const auto it = s->host_paths.find(id);
+    if (it != s->host_paths.end()) {
+        *len = (int32_t)it->second.size();
+        std::memcpy(buf, it->second.data(), sizeof(int32_t) * (size_t)std::min(cap, *len));
+        return DDP_OK;
+    }
+    // written before the request's done flag, which poll has seen
+    const int32_t l = s->h_plen[id];
+    *len = l;
+    if (l > s->path_cap) return fail(DDP_ERR_INVALID, "path longer than the recorded capacity (*len holds its length)");
+    if (l > 0) std::memcpy(buf, s->h_paths + (size_t)id * s->path_cap, sizeof(int32_t) * (size_t)std::min(cap, l));
+    return DDP_OK;
+}
+
 int ddp_serve_free(ddp_server *s) {
     if (!s) return DDP_OK;
     trace("serve: free (kernel %s)", s->running ? "launched" : "not running");
@@ -696,7 +759,9 @@ int ddp_serve_free(ddp_server *s) {
     cudaFreeHost(s->h_ctl);
     cudaFreeHost(s->h_svc);
     cudaFree(s->d_work);
-    cudaFree(s->d_plen);
+    if (s->h_plen) cudaFreeHost(s->h_plen);
+    else cudaFree(s->d_plen);
+    cudaFreeHost(s->h_paths);
     if (s->stream) cudaStreamDestroy(s->stream);
     graph_unref(s->g);
     delete s;

@@ -295,6 +295,15 @@ int ddp_serve_poll(ddp_server *s, int32_t max, int64_t *ids, int32_t *costs, int
  * searches already running keep the version they started on. */
 int ddp_serve_update(ddp_server *s, int32_t n, const int32_t *flag, const int32_t *u, const int32_t *v,
                      const uint32_t *w);
+/* Records each request's s..t path (at most path_cap node ids per request,
+ * in host memory: max_requests x path_cap x 4 bytes).  Call before the
+ * first submit. */
+int ddp_serve_record_paths(ddp_server *s, int32_t path_cap);
+/* Path of a polled request (over the graph version it ran on): copies up to
+ * cap ids, *len = the length (0 when t is unreachable).  DDP_ERR_INVALID
+ * when paths are not recorded, the request was not polled yet, or its path
+ * is longer than path_cap (*len then holds the length). */
+int ddp_serve_path(ddp_server *s, int64_t id, int32_t *buf, int32_t cap, int32_t *len);
 /* submitted, completed, slots, kernel launches, graph version, re-runs */
 int ddp_serve_stats(const ddp_server *s, int64_t *stats6);
 int ddp_serve_free(ddp_server *s);

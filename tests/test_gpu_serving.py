@@ -65,6 +65,7 @@ def test_serving_with_updates(gpu, oracle, nver, rounds):
     d = gpu
     g, dg = _geo(d, 20_000, 41)
     srv = d.Server(dg, d.H_EUCLID, max_requests=4096, versions=nver, grid=32)
+    srv.record_paths(8192)
     rng = np.random.default_rng(5)
     versions = [(g.off.copy(), g.col.copy(), g.w.copy(), d.euclid_rho_fp(g))]
     off, col, w = g.off[:-1].copy(), g.col.copy(), g.w.copy()
@@ -101,6 +102,9 @@ def test_serving_with_updates(gpu, oracle, nver, rounds):
         gv = d.CSR(g.n, vo, vc, vw, xy=g.xy)
         want = _oracle(oracle, gv, s_, t_, 0)  # h = 0: the cost does not depend on h
         assert costs[k] == want, (i, int(ver[k]))
+        if want != d.INF:  # the path is one of that version's graph
+            ok, why = oracle.check_path(vo, vc, vw, srv.path(i), s_, t_, int(costs[k]))
+            assert ok, (i, int(ver[k]), why)
     assert srv.stats()["version"] == rounds
     srv.close()
 
@@ -169,4 +173,48 @@ def test_serving_with_landmarks_on_a_fixed_graph(gpu, oracle, count, bits):
         assert costs[k] == (c if f else d.INF)
     with pytest.raises(d.DdpError):
         srv.update([1], [0], [5], [1])
+    srv.close()
+
+
+def test_serving_paths(gpu, oracle):
+    """Recorded paths (ddp_serve_record_paths): every polled request's path is
+    an s..t path of its reported cost, for Euclidean A* and bidirectional
+    slots; asking before the poll, recording after the first submit, or a
+    path longer than the capacity is an error."""
+    d = gpu
+    g, dg = _geo(d, 30_000, 51)
+    for hk in (d.H_EUCLID, d.H_BIDIR):
+        srv = d.Server(dg, hk, max_requests=1024, grid=32)
+        srv.record_paths(4096)
+        rng = np.random.default_rng(7)
+        S = rng.integers(0, g.n, 120).astype(np.int32)
+        T = rng.integers(0, g.n, 120).astype(np.int32)
+        T[:3] = S[:3]
+        first = srv.submit(S, T)
+        with pytest.raises(d.DdpError):
+            srv.record_paths(4096)
+        with pytest.raises(d.DdpError):
+            srv.path(first)  # not polled yet
+        ids, costs, lat, ver = srv.drain()
+        assert len(ids) == 120
+        for k in range(len(ids)):
+            i = int(ids[k]) - first
+            p = srv.path(int(ids[k]))
+            if costs[k] == d.INF:
+                assert len(p) == 0, i
+                continue
+            ok, why = oracle.check_path(g.off, g.col, g.w, p, int(S[i]), int(T[i]), int(costs[k]))
+            assert ok, (hk, i, why)
+        srv.close()
+    srv = d.Server(dg, d.H_EUCLID, max_requests=64, grid=8)
+    srv.record_paths(2)
+    rng = np.random.default_rng(8)
+    S = rng.integers(0, g.n, 20).astype(np.int32)
+    T = rng.integers(0, g.n, 20).astype(np.int32)
+    srv.submit(S, T)
+    ids, costs, _, _ = srv.drain()
+    fin = [(int(c), int(i)) for i, c in zip(ids, costs) if c != d.INF]
+    assert fin
+    with pytest.raises(d.DdpError):
+        srv.path(max(fin)[1])  # the costliest random pair: far more than two nodes
     srv.close()
