@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "engine.cuh"
@@ -445,6 +446,7 @@ struct DynCtl {
     int relaxed;
     int reseeded;
     int pad[7];
+    int local_nf, local_odd;  // a walk's hand-back from CTA 0 (dyn_walk)
 };
 
 __device__ __forceinline__ SlotBufs slot_of_dyn(const SlotArrays &sa) {
@@ -475,6 +477,59 @@ __device__ __forceinline__ GridGroup dyn_group(GridGroup *, const SlotBufs &B) {
 }
 __device__ __forceinline__ CtaGroup dyn_group(CtaGroup *, const SlotBufs &B) { return CtaGroup{&B.ctl->status}; }
 
+// Small frontiers in the repair walks (hop lowering, invalidation): a level
+// of at most DYN_LOCAL_MAX nodes gives a few dozen threads work and still
+// costs a grid barrier, so CTA 0 takes the walk's next levels alone (block
+// barriers, a shared counter) while the grid waits once, and hands the walk
+// back when a level outgrows DYN_LOCAL_BAIL.  step(x, out, counter) expands
+// frontier node x, pushing into out at atomicAdd(counter).  On entry the
+// frontier is in fb (nf nodes); returns true when the walk is over, else
+// leaves the remaining frontier in fb with its size in nf for the grid.
+#ifndef DYN_LOCAL_MAX
+#define DYN_LOCAL_MAX 256
+#endif
+#ifndef DYN_LOCAL_BAIL
+#define DYN_LOCAL_BAIL 2048
+#endif
+template <class Grp, class Step>
+__device__ bool dyn_walk_local(const Grp &grp, int &nf, int32_t *&fa, int32_t *&fb, DynCtl *dc, int *lcnt,
+                               Step &step) {
+    if constexpr (!std::is_same<Grp, GridGroup>::value) {
+        return false;  // one CTA: the grid loop already uses block barriers
+    } else {
+        if (nf > DYN_LOCAL_MAX) return false;
+        if (blockIdx.x == 0) {
+            int lnf = nf, odd = 0;
+            int32_t *la = fa, *lb = fb;
+            for (;;) {
+                int32_t *t = la;
+                la = lb;
+                lb = t;
+                odd ^= 1;
+                if (threadIdx.x == 0) *lcnt = 0;
+                __syncthreads();
+                for (int i = threadIdx.x; i < lnf; i += blockDim.x) step(__ldcg(la + i), lb, lcnt);
+                __syncthreads();
+                lnf = *(volatile int *)lcnt;
+                __syncthreads();  // every thread has read the count before the next reset
+                if (lnf == 0 || lnf > DYN_LOCAL_BAIL) break;
+            }
+            if (threadIdx.x == 0) {
+                dc->local_nf = lnf;
+                dc->local_odd = odd;
+            }
+        }
+        grp.sync();  // CTA 0's pushes and hand-back are visible to every CTA
+        nf = *(volatile int *)&dc->local_nf;
+        if (*(volatile int *)&dc->local_odd) {
+            int32_t *t = fa;  // CTA 0 swapped its buffers an odd number of times
+            fa = fb;
+            fb = t;
+        }
+        return nf == 0;
+    }
+}
+
 // Grp = GridGroup: every CTA of a cooperative launch (the initial search);
 // Grp = CtaGroup: one CTA (update batches: the repair and the resumed
 // search touch little of the graph, and block barriers are far cheaper than
@@ -487,6 +542,7 @@ __global__ void __launch_bounds__(512, 2)
     if (A.apply_res && *(volatile const int *)(A.apply_res + 1) != 0) return;
     const int nupd = A.nupd_dev ? *(volatile const int *)A.nupd_dev : A.nupd;
     __shared__ WarpRows wrows[16];
+    __shared__ int lsh[1];  // level counter of a walk on one CTA
     SlotBufs B = slot_of_dyn(sa);
     const Grp grp = dyn_group(static_cast<Grp *>(nullptr), B);
     const int rank = grp.rank(), size = grp.size();
@@ -514,35 +570,40 @@ __global__ void __launch_bounds__(512, 2)
             }
             dyn_level_end(grp, dc, it, nf);
             it++;
+            // lowers the hops of u's in-neighbours from u's; pushes each
+            // lowered node once per lowering (bounded by 2 cap_q)
+            auto lower_from = [&](int u, int32_t *out, int *counter) {
+                const uint32_t hu = __ldcg(hops + u);
+                const int b = row_begin(G.roff, G.roend, u), e = row_end(G.roff, G.roend, u);
+                for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
+                    int p[DYN_ROW_UNROLL];
+                    uint32_t hp[DYN_ROW_UNROLL];
+#pragma unroll
+                    for (int k = 0; k < DYN_ROW_UNROLL; k++) p[k] = j0 + k < e ? (int)__ldcg(G.rarc + j0 + k).x : -1;
+#pragma unroll
+                    for (int k = 0; k < DYN_ROW_UNROLL; k++) hp[k] = p[k] >= 0 ? __ldcg(hops + p[k]) : 0u;
+#pragma unroll
+                    for (int k = 0; k < DYN_ROW_UNROLL; k++) {
+                        if (p[k] < 0 || hu + 1 >= hp[k]) continue;
+                        const uint32_t old = atomicMin(hops + p[k], hu + 1);
+                        if (hu + 1 < old) {
+                            const int s = atomicAdd(counter, 1);
+                            if (s < 2 * B.cap_q) out[s] = p[k];
+                            else atomicOr(&B.ctl->status, ST_OVERFLOW);
+                            atomicAdd(&dc->hops_lowered, 1);
+                        }
+                    }
+                }
+            };
             while (nf > 0) {
+                if (dyn_walk_local<Grp>(grp, nf, fa, fb, dc, lsh, lower_from)) break;
+                // a push past the buffer raised an overflow: its count is not a frontier
+                if (*(volatile int *)&B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) break;
                 int32_t *t = fa;
                 fa = fb;
                 fb = t;
                 const int PH = (it + 1) & 3;
-                for (int i = rank; i < nf; i += size) {
-                    const int u = __ldcg(fa + i);
-                    const uint32_t hu = __ldcg(hops + u);
-                    const int b = row_begin(G.roff, G.roend, u), e = row_end(G.roff, G.roend, u);
-                    for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
-                        int p[DYN_ROW_UNROLL];
-                        uint32_t hp[DYN_ROW_UNROLL];
-#pragma unroll
-                        for (int k = 0; k < DYN_ROW_UNROLL; k++) p[k] = j0 + k < e ? (int)__ldcg(G.rarc + j0 + k).x : -1;
-#pragma unroll
-                        for (int k = 0; k < DYN_ROW_UNROLL; k++) hp[k] = p[k] >= 0 ? __ldcg(hops + p[k]) : 0u;
-#pragma unroll
-                        for (int k = 0; k < DYN_ROW_UNROLL; k++) {
-                            if (p[k] < 0 || hu + 1 >= hp[k]) continue;
-                            const uint32_t old = atomicMin(hops + p[k], hu + 1);
-                            if (hu + 1 < old) {
-                                const int s = atomicAdd(&dc->cnt[PH], 1);
-                                if (s < 2 * B.cap_q) fb[s] = p[k];
-                                else atomicOr(&B.ctl->status, ST_OVERFLOW);
-                                atomicAdd(&dc->hops_lowered, 1);
-                            }
-                        }
-                    }
-                }
+                for (int i = rank; i < nf; i += size) lower_from(__ldcg(fa + i), fb, &dc->cnt[PH]);
                 dyn_level_end(grp, dc, it, nf);
                 it++;
                 if (*(volatile int *)&B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) break;
@@ -563,32 +624,35 @@ __global__ void __launch_bounds__(512, 2)
             }
             dyn_level_end(grp, dc, it, nf);
             it++;
+            // invalidates x's children in the tree (nodes whose parent is x);
+            // a parallel arc's second CAS fails: each node is invalidated once
+            auto invalidate_from = [&](int x, int32_t *out, int *counter) {
+                const int b = row_begin(G.off, G.oend, x), e = row_end(G.off, G.oend, x);
+                for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
+                    int y[DYN_ROW_UNROLL];
+                    uint64_t sy[DYN_ROW_UNROLL];
+#pragma unroll
+                    for (int k = 0; k < DYN_ROW_UNROLL; k++) y[k] = j0 + k < e ? (int)__ldcg(G.arc + j0 + k).x : -1;
+#pragma unroll
+                    for (int k = 0; k < DYN_ROW_UNROLL; k++) sy[k] = y[k] >= 0 ? __ldcg(B.state + y[k]) : ~0ull;
+#pragma unroll
+                    for (int k = 0; k < DYN_ROW_UNROLL; k++) {
+                        if (y[k] >= 0 && st_g(sy[k]) < INF_G && st_parent(sy[k]) == x &&
+                            atomicCAS(B.state + y[k], sy[k], ~0ull) == sy[k]) {
+                            out[atomicAdd(counter, 1)] = y[k];
+                            A.inv[atomicAdd(&dc->inv_n, 1)] = y[k];
+                        }
+                    }
+                }
+            };
             while (nf > 0) {
+                if (dyn_walk_local<Grp>(grp, nf, fa, fb, dc, lsh, invalidate_from)) break;
+                if (*(volatile int *)&B.ctl->status & (ST_OVERFLOW | ST_TIMEOUT)) break;
                 int32_t *t = fa;
                 fa = fb;
                 fb = t;
                 const int PH2 = (it + 1) & 3;
-                for (int i = rank; i < nf; i += size) {
-                    const int x = __ldcg(fa + i);
-                    const int b = row_begin(G.off, G.oend, x), e = row_end(G.off, G.oend, x);
-                    for (int j0 = b; j0 < e; j0 += DYN_ROW_UNROLL) {
-                        int y[DYN_ROW_UNROLL];
-                        uint64_t sy[DYN_ROW_UNROLL];
-#pragma unroll
-                        for (int k = 0; k < DYN_ROW_UNROLL; k++) y[k] = j0 + k < e ? (int)__ldcg(G.arc + j0 + k).x : -1;
-#pragma unroll
-                        for (int k = 0; k < DYN_ROW_UNROLL; k++) sy[k] = y[k] >= 0 ? __ldcg(B.state + y[k]) : ~0ull;
-#pragma unroll
-                        for (int k = 0; k < DYN_ROW_UNROLL; k++) {
-                            // a parallel arc's second CAS fails: each node is invalidated once
-                            if (y[k] >= 0 && st_g(sy[k]) < INF_G && st_parent(sy[k]) == x &&
-                                atomicCAS(B.state + y[k], sy[k], ~0ull) == sy[k]) {
-                                fb[atomicAdd(&dc->cnt[PH2], 1)] = y[k];
-                                A.inv[atomicAdd(&dc->inv_n, 1)] = y[k];
-                            }
-                        }
-                    }
-                }
+                for (int i = rank; i < nf; i += size) invalidate_from(__ldcg(fa + i), fb, &dc->cnt[PH2]);
                 dyn_level_end(grp, dc, it, nf);
                 it++;
             }
