@@ -593,6 +593,19 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                         const uint64_t ng64 = (uint64_t)wr.g[o] + a.y;
                         live = v >= 0 && ng64 < (uint64_t)min(mu, INF_G);
                         ng = (uint32_t)ng64;
+                        // a layout whose records need no claim (dense,
+                        // 16-byte pairs) loads v's record beside v's
+                        // potentials, before the pruning test needs them: one
+                        // dependent round trip less per generation of a long
+                        // chain (a record loaded for a pruned v is not used)
+                        constexpr bool early = Pot::on && !Rec::hashed;
+                        if constexpr (early) {
+                            if (live) {
+                                rv = R.claim(v, ep);
+                                uf = Rec::ld(rv);
+                                ur = Rec::ld(rv + 1);
+                            }
+                        }
                         if constexpr (Pot::on) {
                             if (live) {
                                 // a path through v is at least g + the
@@ -601,7 +614,7 @@ __device__ SearchResult run_bidir_cta(const DevGraph &G, const SlotBufs &B, cons
                                 live = ng64 + (dir ? pv.y : pv.x) < (uint64_t)mu;
                             }
                         }
-                        if (live) {
+                        if (live && !early) {
                             // the node's record: both units, one sector
                             rv = R.claim(v, ep);
                             if (rv) {
