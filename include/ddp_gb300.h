@@ -236,15 +236,21 @@ typedef struct ddp_dyn ddp_dyn;
  * ddp_graph_read_csr returns its current arcs.  One dynamic search per graph
  * at a time.  opts.grid = CTAs of the initial search (0 = half the SMs);
  * opts.group = CTAs of each update batch's repair and resumed search
- * (0 or 1 = one CTA, block barriers; more = a cooperative grid). */
+ * (0 = the initial search's grid; 1 = one CTA, block barriers; more = a
+ * cooperative grid of that many). */
 int ddp_dyn_create(ddp_graph *g, int32_t source, int32_t target, int32_t hkind,
                    const ddp_opts *opts, ddp_dyn **out);
 /* Applies one update batch (DA_dyn_cpu.cu:1295-1326 Updates.txt lines):
  * flag 1 = insert u->v with weight w (appended to row u), flag 0 = delete the
  * first live u->v arc of the pre-batch graph, flag 2 = set the weight of
  * that arc to w (no reference counterpart; a delete plus an insert gives the
- * same arc set).  Repairs the search incrementally and returns the new cost
- * (DDP_INF when the target became unreachable). */
+ * same arc set).  Deletes and weight changes run first, in batch order, each
+ * on the graph as the earlier ones left it; inserts follow.  A batch of up
+ * to 4,096 updates is applied on the device (one upload); larger batches,
+ * and batches whose rows no longer fit the arrays' reserve, are applied on
+ * the host copy of the graph, which is laid out again as needed.  Repairs
+ * the search incrementally and returns the new cost (DDP_INF when the target
+ * became unreachable). */
 int ddp_dyn_update(ddp_dyn *d, int32_t n, const int32_t *flag, const int32_t *u, const int32_t *v,
                    const uint32_t *w, int32_t *out_cost);
 int ddp_dyn_cost(const ddp_dyn *d, int32_t *cost);
