@@ -608,10 +608,13 @@ __device__ void service_loop(const BatchArgs &A) {
 }
 
 // CTAs per SM the bidirectional instance is compiled for (its register
-// budget per thread: 2 -> 64, 3 -> 40).  Measured on the 4M-node batch of
-// 4,096 pairs: 2 -> 243k queries/s, 3 -> 255k (456 slots), 4 -> 236k.
+// budget per thread: 2 -> 64, 3 -> 40, 4 -> 32; the engine spills 220,
+// 472 and 772 bytes per thread at those budgets, and three or four CTAs'
+// spills outgrow the L1 left beside their shared memory).  Measured on the
+// 4M-node batch of 4,096 pairs with ring claims spread over the warps:
+// 2 -> 379k queries/s (304 slots), 3 -> 363k (456), 4 -> 228k (608).
 #ifndef DDP_BIDIR_MIN_BLOCKS
-#define DDP_BIDIR_MIN_BLOCKS 3
+#define DDP_BIDIR_MIN_BLOCKS 2
 #endif
 template <int HK>
 __global__ void __launch_bounds__(512, (bidir_hk(HK) ? DDP_BIDIR_MIN_BLOCKS : 2)) k_batch(DevGraph G, SlotArrays sa, BatchArgs A) {
